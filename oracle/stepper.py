@@ -1,0 +1,757 @@
+"""Restatement of Fluid2d's Python sequencing over the C oracle kernels.
+
+TEST INFRASTRUCTURE ONLY: this is the step-level checker for fluid2d_gb300.
+Only tests/, __graft_entry__.smoke() and the CPU baseline / reference arm of
+bench.py may import it.
+
+It restates, for one MPI rank, the numpy code of
+
+* core/grid.py:12-140               grid, masks, coordinates, areas
+* core/gmg/level.py:24-496          level hierarchy, masks and operators,
+                                    smooth/residual/norm, fine<->coarse
+* core/gmg/hierarchy.py:21-218      Vcycle, Fcycle, solve, twoVcycle
+* core/operators.py:12-236,303-314,421-498
+                                    corner mask, rhs_adv, rhs_torque,
+                                    rhs_diffusion, invert_vorticity
+* core/timescheme.py:6-201          the time schemes
+* core/euler.py, core/boussinesq.py, core/quasigeostrophic.py
+                                    step / dynamics / diagnostics
+* core/fluid2d.py:235-314,376-397   the time loop and set_dt
+
+with the same numpy expressions in the same order, so that it reproduces the
+reference's own Python bit for bit when both run over the same kernels
+(checked by tests/golden/make_golden.py, which imports the reference).
+
+One deliberate difference: when a grid dimension becomes odd before the
+coarsest level is reached, coarsening stops there (the reference would halve
+the odd dimension, giving a coarse grid that no longer covers the fine one).
+Power-of-two grids, which are all the reference supports, are unaffected.
+"""
+import numpy as np
+
+try:  # imported as part of the ``oracle`` package
+    from . import oracle as K
+except ImportError:  # imported with oracle/ itself on sys.path
+    import oracle as K
+
+
+class Param(object):
+    """The defaults of core/defaults.json that the hot path reads."""
+
+    def __init__(self, **kw):
+        self.modelname = 'euler'
+        self.nx = 128
+        self.ny = 128
+        self.Lx = 1.
+        self.Ly = 1.
+        self.nh = 3
+        self.geometry = 'closed'
+        self.order = 5
+        self.aparab = 0.05
+        self.flux_splitting_method = 'parabolic'
+        self.timestepping = 'RK3_SSP'
+        self.hydroepsilon = 1.
+        self.relaxation = 'default'
+        self.diffusion = False
+        self.Kdiff = 0.
+        self.gravity = 1.
+        self.Rd = 1.
+        self.beta = 0.
+        self.adaptable_dt = False
+        self.dt = 0.1
+        self.cfl = 0.5
+        self.dtmax = 5.
+        self.npx = 1
+        self.npy = 1
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+# ------------------------------------------------------------------ grid
+class Grid(object):
+    """core/grid.py:12-140 for one rank (ishift = jshift = 0)."""
+
+    def __init__(self, param):
+        self.nx, self.ny = int(param.nx), int(param.ny)
+        self.Lx, self.Ly = param.Lx, param.Ly
+        self.nh = nh = param.nh
+        self.geometry = param.geometry
+        self.nxl = self.nx + 2 * nh
+        self.nyl = self.ny + 2 * nh
+        self.dx = self.Lx / self.nx
+        self.dy = self.Ly / self.ny
+        self.x1d = (np.arange(self.nxl) + 0.5 - nh + 0) * self.dx
+        self.y1d = (np.arange(self.nyl) + 0.5 - nh + 0) * self.dy
+        self.xr, self.yr = np.meshgrid(self.x1d, self.y1d)
+        self.set_msk()
+
+    def set_msk(self):
+        nh = self.nh
+        self.msk = np.ones((self.nyl, self.nxl), dtype=np.int8)
+        if self.geometry in ['xperio', 'xchannel', 'closed', 'disc']:
+            self.msk[-nh:, :] = 0
+            self.msk[:nh, :] = 0
+        if self.geometry in ['yperio', 'ychannel', 'closed', 'disc']:
+            self.msk[:, -nh:] = 0
+            self.msk[:, :nh] = 0
+        if self.geometry == 'disc':
+            r = np.sqrt((self.xr / self.Lx - 0.5)**2 + (self.yr / self.Ly - 0.5)**2)
+            self.msk[r >= 0.5] = 0
+        self.finalize_msk()
+
+    def finalize_msk(self):
+        msk = self.msk
+        self.area = self.domain_integration(msk)
+        x0 = self.domain_integration(self.xr * msk) / self.area
+        y0 = self.domain_integration(self.yr * msk) / self.area
+        self.xr0 = (self.xr - x0) * msk
+        self.yr0 = (self.yr - y0) * msk
+
+    def domain_integration(self, z2d):
+        nh = self.nh
+        return np.sum(z2d[nh:-nh, nh:-nh]) * 1.
+
+
+# ------------------------------------------------------------------ gmg
+def gridinfo(n, m, dx, dy, n0=4):
+    """core/gmg/level.py:24-117 for one rank, plus the even-coarsening stop."""
+    info = []
+    lev = 0
+    while True:
+        if lev > 0:
+            n = n // 2
+            m = m // 2
+            dx = dx * 2
+            dy = dy * 2
+        last = (n <= n0) or (m <= n0) or (n % 2 == 1) or (m % 2 == 1)
+        info.append({'n': n, 'm': m, 'dx': dx, 'dy': dy, 'lev': lev})
+        lev += 1
+        if last:
+            break
+        if lev > 20:
+            raise RuntimeError('too many levels')
+    return info
+
+
+class Level(object):
+    """core/gmg/level.py:120-442 (one rank, halo method 0)."""
+
+    def __init__(self, info, nh, omega, hydroepsilon, relaxation):
+        self.n, self.m = info['n'], info['m']
+        self.dx, self.dy = info['dx'], info['dy']
+        self.lev = info['lev']
+        self.nh = nh
+        self.nv = self.n + 2 * nh
+        self.mv = self.m + 2 * nh
+        self.omega = omega
+        self.hydroepsilon = hydroepsilon
+        self.relaxation = relaxation
+        if self.hydroepsilon * self.dy / self.dx <= .2:
+            self.relaxation = 'tridiagonal'
+        self.msk = np.ones((self.mv, self.nv), dtype=np.int8)
+
+    def fill(self, x):
+        K.fillhalo(x, self.nh)
+
+    def set_finest(self, mskf):
+        self.msk = mskf
+        self.compute_A_atfinest()
+        self.yo = np.zeros((3, self.nv))
+
+    def set_coarser(self, prev):
+        mskf = prev.msk * 1.0
+        coef = np.ones((self.mv, self.nv))
+        K.restrict(self.msk, mskf, self.nh, coef)
+        self.fill(coef)
+        self.msk[coef <= 0.5] = 0
+        A = K.coarsenmatrix(prev.A, prev.msk, self.msk, prev.nh)
+        for k in range(9):
+            c = A[:, :, k].copy()
+            self.fill(c)
+            A[:, :, k] = c
+        self.A = A
+        self.yo = np.zeros((3, self.nv))
+
+    def compute_A_atfinest(self):
+        bx = self.dy / self.dx * self.hydroepsilon
+        by = self.dx / self.dy
+        a = -2 * (bx + by)
+        c = 0.
+        stencil = np.array([[c, by, c], [bx, a, bx], [c, by, c]]).astype(float)
+        if (self.dx == self.dy) and (self.hydroepsilon == 1):
+            a, b, c = -6. / 2, 1. / 2, 0.5 / 2
+            stencil = np.array([[c, b, c], [b, a, b], [c, b, c]]).astype(float)
+        A = np.zeros((self.mv, self.nv, 9))
+        I, J = np.meshgrid(np.arange(self.nv - 2) + 1, np.arange(self.mv - 2) + 1)
+        coef = 1. / (self.dx * self.dy)
+        for k in range(9):
+            Acoef = np.zeros((self.mv, self.nv))
+            i, j = (k % 3) - 1, (k // 3) - 1
+            Acoef[J, I] = stencil[j + 1, i + 1] * coef * self.msk[J + j, I + i] * self.msk[J, I]
+            self.fill(Acoef)
+            A[:, :, k] = Acoef
+        self.A = A
+
+    def ninetofive(self):
+        self.A = self.A[:, :, :5]
+
+    def smooth(self, x, b, nite):
+        if self.relaxation == 'tridiagonal':
+            nite *= 3
+        for k in range(nite):
+            if self.relaxation == 'tridiagonal':
+                K.smoothtridiag(self.msk, self.A, x, b)
+            else:
+                K.smoothtwicewitha(self.msk, self.A, x, b, self.omega, self.yo)
+            self.fill(x)
+
+    def residual(self, x, b, r):
+        K.computeresidualwitha(self.msk, self.A, x, b, r)
+        self.fill(r)
+
+    def norm(self, x):
+        local_sum = K.computenorm(self.msk, x, self.nh)
+        return np.sqrt(local_sum / 1.0)
+
+
+def coarsetofine(coarse, fine, x, y):
+    K.interpolate(fine.msk, coarse.msk, x, fine.nh, y)
+    if coarse.nh <= 2:
+        fine.fill(y)
+
+
+def finetocoarse(fine, coarse, x, y):
+    K.restrict(coarse.msk, x, coarse.nh, y)
+    coarse.fill(y)
+
+
+class Gmg(object):
+    """core/gmg/hierarchy.py:21-218 for one rank."""
+
+    def __init__(self, pp, mskp):
+        info = gridinfo(pp['n'], pp['m'], pp['dx'], pp['dy'], pp.get('n0', 4))
+        self.nlevs = len(info)
+        self.npre = 1
+        self.npost = 1
+        self.nvcyc = 1
+        self.ndeepest = 16
+        # the QG hierarchy ignores hydroepsilon (core/gmg/level.py:94-103,138-141)
+        he = 1. if pp.get('qgoperator', False) else pp.get('hydroepsilon', 1.)
+        self.grid = [Level(inf, pp['nh'], pp['omega'], he,
+                           pp.get('relaxation', 'default')) for inf in info]
+        msk = mskp.astype(np.int8)
+        self.x, self.b, self.r = [], [], []
+        for lev in range(self.nlevs):
+            g = self.grid[lev]
+            if lev == 0:
+                g.set_finest(msk)
+            else:
+                g.set_coarser(self.grid[lev - 1])
+            self.x.append(np.zeros((g.mv, g.nv)))
+            self.b.append(np.zeros((g.mv, g.nv)))
+            self.r.append(np.zeros((g.mv, g.nv)))
+        for g in self.grid:
+            g.ninetofive()
+        if pp.get('qgoperator', False):
+            for g in self.grid:
+                d = g.A[:, :, 4]
+                g.A[d != 0., 4] -= 1. / (pp['Rd']**2)
+
+    def Vcycle(self, lev1):
+        deepest = self.nlevs - 1
+        for lev in range(lev1, deepest):
+            if lev > lev1:
+                self.x[lev][:, :] = 0.
+            self.grid[lev].smooth(self.x[lev], self.b[lev], self.npre)
+            self.grid[lev].residual(self.x[lev], self.b[lev], self.r[lev])
+            finetocoarse(self.grid[lev], self.grid[lev + 1], self.r[lev], self.b[lev + 1])
+        lev = deepest
+        self.x[lev][:, :] = 0.
+        self.grid[lev].smooth(self.x[lev], self.b[lev], self.ndeepest)
+        for lev in range(deepest - 1, lev1 - 1, -1):
+            coarsetofine(self.grid[lev + 1], self.grid[lev], self.x[lev + 1], self.r[lev])
+            self.x[lev] += self.r[lev]
+            self.grid[lev].smooth(self.x[lev], self.b[lev], self.npost)
+
+    def Fcycle(self, lev1):
+        deepest = self.nlevs - 1
+        for lev in range(lev1, deepest):
+            finetocoarse(self.grid[lev], self.grid[lev + 1], self.b[lev], self.b[lev + 1])
+        lev = deepest
+        self.x[lev][:, :] = 0.
+        self.grid[lev].smooth(self.x[lev], self.b[lev], self.ndeepest)
+        for lev in range(deepest - 1, lev1 - 1, -1):
+            coarsetofine(self.grid[lev + 1], self.grid[lev], self.x[lev + 1], self.x[lev])
+            for k in range(self.nvcyc):
+                self.Vcycle(lev)
+
+    def solve(self, x, b, param):
+        g = self.grid[0]
+        g.residual(x, b, self.b[0])
+        normeb = g.norm(b)
+        if normeb > 0:
+            res0 = (g.norm(self.b[0]) / normeb)
+        else:
+            return 0, 0.
+        res = res0
+        nite = 0
+        nite_diverge = 0
+        while (nite < param['maxite']) and (res0 > param['tol']):
+            self.Fcycle(0)
+            x += self.x[0]
+            g.residual(x, b, self.b[0])
+            res = (g.norm(self.b[0]) / normeb)
+            conv = res0 / res
+            res0 = res
+            nite += 1
+            if conv < 1:
+                nite_diverge += 1
+            if nite_diverge > 4:
+                raise RuntimeError('solver is not converging')
+        return nite, res
+
+    def twoVcycle(self, x, b, param=None):
+        g = self.grid[0]
+        self.x[0][:, :] = x
+        self.b[0][:, :] = b
+        for k in range(2):
+            g.residual(self.x[0], self.b[0], self.r[0])
+            self.Vcycle(0)
+        x[:, :] = self.x[0]
+        return 1, 0.
+
+
+# ------------------------------------------------------------------ operators
+class Operators(object):
+    """core/operators.py:12-155, 214-236, 292-314, 421-498 (no islands)."""
+
+    def __init__(self, param, grid, varname_list, tracer_list, whosetspsi,
+                 qgoperator=False):
+        self.varname_list = varname_list
+        self.tracer_list = tracer_list
+        self.whosetspsi = whosetspsi
+        self.nh = param.nh
+        self.order = param.order
+        self.gravity = param.gravity
+        self.geometry = param.geometry
+        self.Kdiff = param.Kdiff
+        self.msk = grid.msk
+        self.nxl, self.nyl = grid.nxl, grid.nyl
+        self.dx, self.dy = grid.dx, grid.dy
+        self.grid = grid
+        self.area = grid.area
+        self.work = np.zeros((self.nyl, self.nxl))
+        pp = {'nh': param.nh, 'n': param.nx, 'm': param.ny, 'omega': 8. / 9.,
+              'dx': grid.dx, 'dy': grid.dy, 'n0': 4,
+              'hydroepsilon': param.hydroepsilon, 'relaxation': param.relaxation}
+        mskr = self.msk * 1.
+        K.celltocorner(mskr, self.work)
+        self.work[self.work < 1.] = 0.
+        self.mskp = self.msk * 0
+        self.mskp[self.work == 1.] = 1
+        if qgoperator:
+            pp['qgoperator'] = True
+            pp['Rd'] = param.Rd
+        self.gmg = Gmg(pp, self.work)
+        self.fill_halo = self.gmg.grid[0].fill
+        self.cst = np.zeros(5,)
+        if self.order % 2 == 0:
+            self.fortran_adv = K.adv_centered
+            self.cst[0] = grid.dx
+            self.cst[1] = grid.dy
+            self.cst[2] = 0.05
+            self.cst[3] = 0
+            self.cst[4] = 0
+        else:
+            self.fortran_adv = K.adv_upwind
+            self.cst[0] = grid.dx
+            self.cst[1] = grid.dy
+            self.cst[2] = 0.05
+            self.cst[3] = 0
+            self.cst[4] = param.aparab
+        lst = ['minmax', 'parabolic']
+        self.fs_method = lst.index(param.flux_splitting_method) \
+            if param.flux_splitting_method in lst else 1
+        self.last_solve = (0, 0.)
+
+    def rhs_adv(self, x, t, dxdt):
+        iu = self.varname_list.index('u')
+        iv = self.varname_list.index('v')
+        u = x[iu]
+        v = x[iv]
+        for trac in self.tracer_list:
+            ik = self.varname_list.index(trac)
+            y = dxdt[ik]
+            self.fortran_adv(self.msk, x[ik], y, u, v, self.cst, self.nh,
+                             self.fs_method, self.order)
+            self.fill_halo(y)
+            dxdt[ik][:, :] = y
+
+    def rhs_diffusion(self, x, t, dxdt, coef=1.):
+        for trac in self.tracer_list:
+            ik = self.varname_list.index(trac)
+            y = dxdt[ik]
+            K.add_diffusion(self.msk, x[ik], self.dx, self.nh, coef * self.Kdiff, y)
+            self.fill_halo(y)
+            dxdt[ik] = y
+
+    def rhs_torque(self, x, t, dxdt):
+        ib = self.varname_list.index('buoyancy')
+        iw = self.varname_list.index('vorticity')
+        y = dxdt[iw]
+        b = x[ib]
+        y *= self.msk
+        K.add_torque(self.msk, b, self.dx, self.nh, self.gravity, y)
+        self.fill_halo(y)
+        dxdt[iw][:, :] = y
+
+    def invert_vorticity(self, x, flag='full'):
+        iu = self.varname_list.index('u')
+        iv = self.varname_list.index('v')
+        ip = self.varname_list.index('psi')
+        iw = self.varname_list.index(self.whosetspsi)
+        u = x[iu]
+        v = x[iv]
+        psi = x[ip]
+        K.celltocorner(x[iw], self.work)
+        if flag == 'fast':
+            self.gmg.twoVcycle(psi, self.work, {'maxite': 1, 'tol': 1e-6})
+        else:
+            self.last_solve = self.gmg.solve(psi, self.work,
+                                             {'maxite': 4, 'tol': 1e-11})
+            if self.geometry == 'perio':
+                psim = self.grid.domain_integration(psi) / self.area
+                psi -= psim
+        psi = psi * self.mskp
+        K.computeorthogradient(self.msk, psi, self.dx, self.dy, self.nh, u, v)
+        x[iu] = u
+        x[iv] = v
+        x[ip] = psi
+
+
+# ------------------------------------------------------------------ time
+class Timescheme(object):
+    """core/timescheme.py:6-201"""
+
+    def __init__(self, timestepping, x):
+        self.timestepping = timestepping
+        coefondt = {'EF': 1., 'LF': 1., 'Heun': 2., 'AB2': 1., 'AB3': 1.,
+                    'LFAM3': 1., 'RK3_SSP': 1.5, 'RK3': 1., 'RK4_LS': 1.}
+        self.dtcoef = coefondt[timestepping]
+        self.asselin_cst = 0.1
+        self.ab2_epsilon = 0.1
+        self.x = np.zeros_like(x)
+        self.dx0 = np.zeros_like(x)
+        self.dx1 = np.zeros_like(x)
+        if timestepping in ['RK3_SSP', 'AB3', 'RK3']:
+            self.dx2 = np.zeros_like(x)
+        if timestepping in ['LF', 'LFAM3']:
+            self.xb = np.zeros_like(x)
+        self.first = True
+        self.second = True
+        self.kstage = 0
+
+    def set(self, rhs):
+        self.rhs = rhs
+        self.forward = getattr(self, {'EF': 'EulerForward', 'LF': 'LeapFrog'}.get(
+            self.timestepping, self.timestepping))
+        self.kforcing = {'RK4_LS': 3, 'RK3_SSP': 2, 'Heun': 1, 'LFAM3': 1}.get(
+            self.timestepping, 0)
+
+    def EulerForward(self, x, t, dt):
+        self.rhs(x, t, self.dx0)
+        x += dt * self.dx0
+
+    def AB2(self, x, t, dt):
+        self.rhs(x, t, self.dx0)
+        if self.first:
+            x += dt * self.dx0
+            self.first = False
+        else:
+            x += ((1.5 + self.ab2_epsilon) * dt) * self.dx0 \
+                - ((0.5 + self.ab2_epsilon) * dt) * self.dx1
+        self.dx1[:] = self.dx0
+
+    def AB3(self, x, t, dt):
+        self.rhs(x, t, self.dx0)
+        if self.first:
+            x += dt * self.dx0
+            self.first = False
+        elif self.second:
+            x += (1.5 * dt) * self.dx0 - (0.5 * dt) * self.dx1
+            self.second = False
+        else:
+            x += (23 * dt / 12.) * self.dx0 \
+                - (16 * dt / 12.) * self.dx1 + (5 * dt / 12.) * self.dx2
+        self.dx2[:] = self.dx1
+        self.dx1[:] = self.dx0
+
+    def LeapFrog(self, x, t, dt):
+        self.x[:] = x
+        self.rhs(x, t, self.dx0)
+        if self.first:
+            x += dt * self.dx0
+            self.first = False
+        else:
+            x[:] = self.xb + (2 * dt) * self.dx0
+            self.x += self.asselin_cst * (x + self.xb - 2 * self.x)
+        self.xb[:] = self.x
+
+    def LFAM3(self, x, t, dt):
+        self.x[:] = x
+        self.kstage = 0
+        self.rhs(x, t, self.dx0)
+        if self.first:
+            x += dt * self.dx0
+            self.first = False
+        else:
+            x[:] = self.xb + (2 * dt) * self.dx0
+            x[:] = (1. / 12.) * (5. * x + 8. * self.x - self.xb)
+            self.kstage = 1
+            self.rhs(x, t + dt * .5, self.dx0)
+            x[:] = self.x + dt * self.dx0
+        self.xb[:] = self.x
+
+    def Heun(self, x, t, dt):
+        self.kstage = 0
+        self.rhs(x, t, self.dx0)
+        self.x = x + dt * self.dx0
+        self.kstage = 1
+        self.rhs(self.x, t + dt, self.dx1)
+        x += (0.5 * dt) * (self.dx0 + self.dx1)
+
+    def RK3(self, x, t, dt):
+        self.kstage = 0
+        self.rhs(x, t, self.dx0)
+        self.x = x + (dt / 3.) * self.dx0
+        self.kstage = 1
+        self.rhs(self.x, t + dt / 3., self.dx1)
+        self.x = x + (0.5 * dt) * self.dx1
+        self.kstage = 2
+        self.rhs(self.x, t + 0.5 * dt, self.dx2)
+        x += dt * self.dx2
+
+    def RK3_SSP(self, x, t, dt):
+        self.kstage = 0
+        self.rhs(x, t, self.dx0)
+        self.x = x + dt * self.dx0
+        self.kstage = 1
+        self.rhs(self.x, t + dt, self.dx1)
+        self.x = x + (0.25 * dt) * (self.dx0 + self.dx1)
+        self.kstage = 2
+        self.rhs(self.x, t + 0.5 * dt, self.dx2)
+        x += (dt / 6.) * (self.dx0 + self.dx1 + 4 * self.dx2)
+
+    def RK4_LS(self, x, t, dt):
+        self.kstage = 0
+        self.rhs(x, t, self.dx0)
+        self.x = x + (0.25 * dt) * self.dx0
+        self.kstage = 1
+        self.rhs(self.x, t + dt * 0.25, self.dx0)
+        self.x = x + (dt / 3.) * self.dx0
+        self.kstage = 2
+        self.rhs(self.x, t + dt / 3., self.dx0)
+        self.x = x + (dt / 2.) * self.dx0
+        self.kstage = 3
+        self.rhs(self.x, t + 0.5 * dt, self.dx0)
+        x += dt * self.dx0
+
+
+# ------------------------------------------------------------------ models
+class _Model(object):
+    varname_list = []
+    tracer_list = []
+    whosetspsi = 'vorticity'
+    qgoperator = False
+
+    def __init__(self, param, grid=None):
+        self.param = param
+        self.grid = grid if grid is not None else Grid(param)
+        g = self.grid
+        self.msk, self.nh, self.area = g.msk, g.nh, g.area
+        self.xr, self.yr = g.xr, g.yr
+        self.state = np.zeros((len(self.varname_list), g.nyl, g.nxl))
+        self.ope = Operators(param, g, self.varname_list, self.tracer_list,
+                             self.whosetspsi, qgoperator=self.qgoperator)
+        self.tscheme = Timescheme(param.timestepping, self.state)
+        self.tscheme.set(self.dynamics)
+        self.diags = {}
+
+    def get(self, name):
+        return self.state[self.varname_list.index(name)]
+
+
+class Euler(_Model):
+    """core/euler.py:12-223 (no forcing, noslip, sponge, dye, islands)."""
+    varname_list = ['vorticity', 'psi', 'u', 'v', 'source']
+    tracer_list = ['vorticity']
+
+    def step(self, t, dt):
+        self.tscheme.forward(self.state, t, dt)
+        self.set_psi_from_vorticity()
+
+    def dynamics(self, x, t, dxdt):
+        self.ope.rhs_adv(x, t, dxdt)
+        if self.tscheme.kstage == self.tscheme.kforcing:
+            if self.param.diffusion:
+                self.ope.rhs_diffusion(x, t, dxdt)
+                self.ope.invert_vorticity(dxdt, flag='fast')
+        else:
+            self.ope.invert_vorticity(dxdt, flag='fast')
+
+    def set_psi_from_vorticity(self):
+        self.ope.invert_vorticity(self.state)
+
+    def diagnostics(self, t=0.):
+        u, v = self.get('u'), self.get('v')
+        trac, psi, source = self.get('vorticity'), self.get('psi'), self.get('source')
+        ke, maxu = K.computekemaxu(self.msk, u, v, self.nh)
+        z, z2 = K.computesumandnorm(self.msk, trac, self.nh)
+        px = K.computedotprod(self.msk, trac, self.xr, self.nh)
+        py = K.computedotprod(self.msk, trac, self.yr, self.nh)
+        angmom = K.computesum(self.msk, psi, self.nh)
+        sce = K.computedotprod(self.msk, trac, source, self.nh)
+        cst = np.array([maxu, ke, z, z2, px, py, angmom, sce], dtype=float)
+        self.diags['maxspeed'] = cst[0]
+        self.diags['ke'] = cst[1] / self.area
+        self.diags['vorticity'] = cst[2] / self.area
+        self.diags['enstrophy'] = 0.5 * cst[3] / self.area
+        self.diags['px'] = cst[4] / self.area
+        self.diags['py'] = cst[5] / self.area
+        self.diags['angmom'] = cst[6] / self.area
+        self.diags['source'] = cst[7] / self.area
+        return self.diags
+
+
+class Boussinesq(_Model):
+    """core/boussinesq.py:10-153 (no forcing, noslip, islands)."""
+    varname_list = ['vorticity', 'psi', 'u', 'v', 'buoyancy', 'banom']
+    tracer_list = ['vorticity', 'buoyancy']
+
+    def __init__(self, param, grid=None):
+        _Model.__init__(self, param, grid)
+        self.bref = self.get('buoyancy').copy()
+
+    def step(self, t, dt):
+        self.tscheme.forward(self.state, t, dt)
+        banom = self.get('banom')
+        banom[:, :] = self.get('buoyancy') - self.bref
+
+    def dynamics(self, x, t, dxdt):
+        self.ope.rhs_adv(x, t, dxdt)
+        self.ope.rhs_torque(x, t, dxdt)
+        if self.tscheme.kstage == self.tscheme.kforcing:
+            coef = self.tscheme.dtcoef
+            if self.param.diffusion:
+                self.ope.rhs_diffusion(x, t, dxdt, coef=coef)
+        self.ope.invert_vorticity(dxdt, flag='fast')
+
+    def set_psi_from_vorticity(self):
+        self.ope.invert_vorticity(self.state)
+
+    def diagnostics(self, t=0.):
+        nh = self.nh
+        u, v = self.get('u'), self.get('v')
+        vort, buoy = self.get('vorticity'), self.get('buoyancy')
+        ke, maxu = K.computekemaxu(self.msk, u, v, nh)
+        z, z2 = K.computesumandnorm(self.msk, vort, nh)
+        b, b2 = K.computesumandnorm(self.msk, buoy, nh)
+        pe = - self.param.gravity * K.computesum(self.msk, buoy * self.yr, nh)
+        cst = np.array([maxu, ke, z, z2, pe, b, b2], dtype=float)
+        self.diags['maxspeed'] = cst[0]
+        self.diags['ke'] = cst[1] / self.area
+        self.diags['pe'] = cst[4] / self.area
+        self.diags['energy'] = (cst[1] + cst[4]) / self.area
+        self.diags['vorticity'] = cst[2] / self.area
+        self.diags['enstrophy'] = 0.5 * cst[3] / self.area
+        self.diags['buoyancy'] = cst[5] / self.area
+        self.diags['brms'] = np.sqrt(cst[6] / self.area - (cst[5] / self.area)**2)
+        return self.diags
+
+
+class QG(_Model):
+    """core/quasigeostrophic.py:11-218 (no forcing, noslip, bottom torque,
+    ageostrophic diagnosis)."""
+    varname_list = ['pv', 'psi', 'u', 'v', 'pvanom', 'vorticity']
+    tracer_list = ['pv']
+    whosetspsi = 'pvanom'
+    qgoperator = True
+
+    def __init__(self, param, grid=None):
+        _Model.__init__(self, param, grid)
+        g = self.grid
+        self.pvback = param.beta * (g.yr - g.Ly * .5) * g.msk
+        self.ipva = self.varname_list.index('pvanom')
+        self.ipv = self.varname_list.index('pv')
+        self.ivor = self.varname_list.index('vorticity')
+        self.ipsi = self.varname_list.index('psi')
+        self.Rd = param.Rd
+
+    def step(self, t, dt):
+        self.tscheme.forward(self.state, t, dt)
+        self.set_psi_from_pv()
+        self.state[self.ipva] = self.state[self.ipv] - self.pvback
+        self.state[self.ivor] = (self.state[self.ipva]
+                                 - (self.Rd**-2) * self.state[self.ipsi])
+
+    def dynamics(self, x, t, dxdt):
+        dxdt[:] = 0.
+        self.ope.rhs_adv(x, t, dxdt)
+        if self.tscheme.kstage == self.tscheme.kforcing:
+            if self.param.diffusion:
+                self.ope.rhs_diffusion(x, t, dxdt)
+        else:
+            dxdt[self.ipva] = dxdt[self.ipv]
+            self.ope.invert_vorticity(dxdt, flag='fast')
+
+    def set_psi_from_pv(self):
+        state = self.state
+        state[self.ipva] = state[self.ipv] - self.pvback
+        self.ope.invert_vorticity(self.state, flag='full')
+
+    def diagnostics(self, t=0.):
+        u, v = self.get('u'), self.get('v')
+        trac, psi = self.get('pv'), self.get('psi')
+        K.cornertocell(psi, self.ope.work)
+        psim, psi2 = K.computesumandnorm(self.msk, self.ope.work, self.nh)
+        ape = 0.5 * psi2 / self.Rd**2
+        ke, maxu = K.computekemaxu(self.msk, u, v, self.nh)
+        z, z2 = K.computesumandnorm(self.msk, trac, self.nh)
+        cst = np.array([maxu, ke, z, z2, ape], dtype=float)
+        self.diags['maxspeed'] = cst[0]
+        self.diags['ke'] = cst[1] / self.area
+        self.diags['pv'] = cst[2] / self.area
+        self.diags['pv2'] = 0.5 * cst[3] / self.area
+        self.diags['ape'] = cst[4] / self.area
+        self.diags['energy'] = (cst[1] + cst[4]) / self.area
+        return self.diags
+
+
+MODELS = {'euler': Euler, 'boussinesq': Boussinesq, 'quasigeostrophic': QG}
+
+
+def set_dt(model, param, dt0):
+    """core/fluid2d.py:376-397; returns dt and sets cst[3] = maxspeed."""
+    maxspeed = model.diags['maxspeed']
+    if param.adaptable_dt and maxspeed != 0:
+        dt = param.cfl * min(model.grid.dx, model.grid.dy) / maxspeed
+        if dt > param.dtmax:
+            dt = param.dtmax
+    else:
+        dt = dt0
+    model.ope.cst[3] = maxspeed
+    return dt
+
+
+def run(model, param, nsteps, dt0, t=0., callback=None):
+    """The core of Fluid2d.loop (core/fluid2d.py:235-314) without I/O."""
+    if not model.diags:
+        model.diagnostics(t)
+    for kt in range(nsteps):
+        dt = set_dt(model, param, dt0)
+        model.step(t, dt)
+        t += dt
+        model.diagnostics(t)
+        if callback is not None:
+            callback(kt + 1, t, model)
+    return t

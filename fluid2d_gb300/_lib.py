@@ -1,0 +1,187 @@
+"""Build and load libfluid2d_gb300.so (the sm_103a kernels behind a C ABI).
+
+Two variants are built from the same sources:
+
+* ``libfluid2d_gb300.so``        -- the product build (nvcc may contract a*b+c
+  into FMA);
+* ``libfluid2d_gb300_exact.so``  -- ``-DF2D_EXACT -fmad=false``: every
+  operation rounded separately, for bit-for-bit comparison with the CPU
+  oracle in the parity tests.
+
+There is no CPU fallback: ``lib()`` raises if the library cannot be loaded.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(_HERE, "csrc")
+BUILD = os.path.join(_HERE, "_build")
+INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
+SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
+           "kernels_fused.cu"]
+HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+VARIANTS = {
+    "product": ("libfluid2d_gb300.so", []),
+    "exact": ("libfluid2d_gb300_exact.so", ["-DF2D_EXACT", "-fmad=false"]),
+}
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.sep not in c or os.path.exists(c)):
+            return c
+    return "nvcc"
+
+
+def _sources():
+    return [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
+
+
+def _deps():
+    files = [os.path.join(CSRC, s) for s in _sources()]
+    files += [os.path.join(CSRC, h) for h in HEADERS if os.path.exists(os.path.join(CSRC, h))]
+    files.append(os.path.join(INCLUDE, "fluid2d_gb300.h"))
+    return files
+
+
+def so_path(variant="product"):
+    return os.path.join(BUILD, VARIANTS[variant][0])
+
+
+def _stale(target):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(f) > t for f in _deps())
+
+
+def build(variants=("product", "exact"), force=False, verbose=False):
+    """Compile every variant (all translation units in parallel)."""
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    jobs = []
+    for var in variants:
+        so, extra = VARIANTS[var]
+        target = os.path.join(BUILD, so)
+        if not force and not _stale(target):
+            continue
+        objs = []
+        for src in _sources():
+            obj = os.path.join(BUILD, "%s.%s.o" % (src[:-3], var))
+            cmd = [nvcc] + ARCH + NVCC_FLAGS + extra + ["-I", INCLUDE, "-c",
+                                                        os.path.join(CSRC, src), "-o", obj]
+            jobs.append(cmd)
+            objs.append(obj)
+        jobs.append(("link", target, objs))
+
+    compile_jobs = [j for j in jobs if not isinstance(j, tuple)]
+    link_jobs = [j for j in jobs if isinstance(j, tuple)]
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), r.stdout))
+        return r.stdout
+
+    with ThreadPoolExecutor(max_workers=max(2, min(16, os.cpu_count() or 4))) as ex:
+        list(ex.map(run, compile_jobs))
+    for _, target, objs in link_jobs:
+        tmp = target + ".tmp%d" % os.getpid()
+        run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+        os.replace(tmp, target)
+    return [so_path(v) for v in variants]
+
+
+_libs = {}
+_lock = threading.Lock()
+
+
+def lib(variant="product"):
+    """The loaded library (building it first if it is missing or stale)."""
+    with _lock:
+        if variant not in _libs:
+            path = so_path(variant)
+            if _stale(path):
+                build(variants=(variant,))
+            L = ctypes.CDLL(path)
+            _declare(L)
+            _libs[variant] = L
+        return _libs[variant]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+# name -> argtypes (all return int status)
+SIGNATURES = {
+    "f2d_adv_upwind": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
+    "f2d_adv_centered": [_P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
+    "f2d_flx_adv_upwind": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
+    "f2d_flx_adv_centered": [_P, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _P],
+    "f2d_computeorthogradient": [_P, _P, _D, _D, _I, _I, _I, _P, _P, _P],
+    "f2d_celltocorner": [_P, _P, _I, _I, _P],
+    "f2d_cornertocell": [_P, _P, _I, _I, _P],
+    "f2d_add_diffusion": [_P, _P, _D, _I, _D, _P, _I, _I, _P],
+    "f2d_add_torque": [_P, _P, _D, _I, _D, _P, _I, _I, _P],
+    "f2d_computedotprod": [_P, _P, _P, _I, _I, _I, _P, _P],
+    "f2d_computemax": [_P, _P, _I, _I, _I, _P, _P],
+    "f2d_computesum": [_P, _P, _I, _I, _I, _P, _P],
+    "f2d_computesumandnorm": [_P, _P, _I, _I, _I, _P, _P],
+    "f2d_computenormmaxu": [_P, _P, _I, _I, _I, _P, _P],
+    "f2d_computekemaxu": [_P, _P, _P, _I, _I, _I, _P, _P],
+    "f2d_computekemaxuv": [_P, _P, _P, _I, _I, _I, _P, _P],
+    "f2d_computekewithpsi": [_P, _P, _P, _I, _I, _I, _P, _P],
+    "f2d_smoothtwicewitha": [_P, _P, _P, _P, _D, _I, _I, _P],
+    "f2d_computeresidualwitha": [_P, _P, _P, _P, _P, _I, _I, _P],
+    "f2d_fillhalo": [_P, _I, _I, _I, _P],
+    "f2d_interpolate": [_P, _P, _P, _I, _I, _I, _I, _I, _P, _P],
+    "f2d_restrict": [_P, _P, _I, _I, _I, _I, _I, _P, _P],
+    "f2d_coarsenmatrix": [_P, _P, _P, _I, _I, _I, _I, _I, _P, _P],
+    "f2d_computenorm": [_P, _P, _I, _I, _I, _P, _P],
+    "f2d_computeinner": [_P, _P, _P, _I, _I, _I, _P, _P],
+}
+EXTRA = {
+    "f2d_version": ([], _I),
+    "f2d_last_error": ([], ctypes.c_char_p),
+    "f2d_exact_arithmetic": ([], _I),
+}
+
+
+def _declare(L):
+    for name, args in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = _I
+    for name, (args, res) in EXTRA.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    try:
+        from . import _abi_ext
+        _abi_ext.declare(L)
+    except ImportError:
+        pass
+
+
+class F2DError(RuntimeError):
+    """A nonzero status returned by the library (message from f2d_last_error)."""
+
+    def __init__(self, name, code, msg):
+        RuntimeError.__init__(self, "%s failed (status %d): %s" % (name, code, msg))
+        self.code = code
+
+
+def call(name, *args, variant="product"):
+    L = lib(variant)
+    rc = getattr(L, name)(*args)
+    if rc != 0:
+        raise F2DError(name, rc, L.f2d_last_error().decode(errors="replace"))
+    return rc

@@ -1,0 +1,158 @@
+/*
+ * fluid2d_gb300.h -- C ABI of libfluid2d_gb300.so, the GB300 (sm_103a)
+ * implementation of Fluid2d's time-step hot path.
+ *
+ * Conventions
+ *  - Every array argument is a DEVICE pointer.  A field is a row-major
+ *    (m, n) array: m rows along y, n columns along x, halo included, exactly
+ *    the numpy layout of the reference (numpy a[j, i] == Fortran a(j+1, i+1)).
+ *  - Masks are int8 (0 = solid, 1 = fluid), fields are float64.
+ *  - A stencil array "A" is stored plane by plane: A[k*m*n + j*n + i] with
+ *    k = 0..4 for the reference's A(j,i,1..5) (SW, S, SE, W, C of the
+ *    symmetric 9-point operator); 9 planes for coarsenmatrix.
+ *  - "stream" is a cudaStream_t (NULL = the legacy default stream).  Calls
+ *    are asynchronous; outputs are ready when the stream reaches them.
+ *  - Every function returns 0 on success or an F2D_ERR_* code; nothing ever
+ *    exits the process (the reference's Fortran "stop" becomes F2D_ERR_NH).
+ *    f2d_last_error() gives the message of the last failure on this thread.
+ *  - Functions marked (scratch) use a device scratch buffer owned by the
+ *    library (allocated on first use, grown on demand, one per device);
+ *    such calls must not overlap on the GPU with another (scratch) call on
+ *    the same device.
+ *
+ * Each declaration names the reference routine it replaces (file:line in
+ * pvthinker/Fluid2d).
+ */
+#ifndef FLUID2D_GB300_H
+#define FLUID2D_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define F2D_OK 0
+#define F2D_ERR_NH 1       /* nh != 3 where the reference stops */
+#define F2D_ERR_SHAPE 2    /* unusable array dimensions */
+#define F2D_ERR_ARG 3      /* bad argument */
+#define F2D_ERR_CUDA 4     /* CUDA runtime failure */
+#define F2D_ERR_DIVERGED 5 /* multigrid diverged (core/gmg/hierarchy.py:182-188) */
+#define F2D_ERR_LIMIT 6    /* size beyond a fixed capacity */
+
+/* library version, 100*major + minor */
+int f2d_version(void);
+/* message of the last failing call on this host thread ("" if none) */
+const char *f2d_last_error(void);
+/* 1 if this build rounds every operation separately (no FMA contraction) */
+int f2d_exact_arithmetic(void);
+
+/* ------------------------------------------------ fortran_advection ---- */
+/* core/fortran_advection.f90:2-165 adv_upwind(msk,x,y,u,v,cst,nh,method,order[,m,n]),
+ * called from core/operators.py:227-230.  cst: DEVICE pointer to the 5
+ * doubles [dx, dy, logcosh, umax, aparab] (core/operators.py:111-117).
+ * Writes y on the interior only. */
+int f2d_adv_upwind(const int8_t *msk, const double *x, double *y, const double *u,
+                   const double *v, const double *cst, int nh, int method, int order,
+                   int m, int n, void *stream);
+/* core/fortran_advection.f90:169-284 adv_centered (even orders 2/4/6) */
+int f2d_adv_centered(const int8_t *msk, const double *x, double *y, const double *u,
+                     const double *v, const double *cst, int nh, int method, int order,
+                     int m, int n, void *stream);
+
+/* ------------------------------------------------ fortran_fluxes ------- */
+/* core/fortran_fluxes.f90:2-170 adv_upwind(msk,x,y,u,v,xflx,yflx,cst,nh,method,order),
+ * called from core/fluxes.py:199-203 */
+int f2d_flx_adv_upwind(const int8_t *msk, const double *x, double *y, const double *u,
+                       const double *v, double *xflx, double *yflx, const double *cst,
+                       int nh, int method, int order, int m, int n, void *stream);
+/* core/fortran_fluxes.f90:174-279 adv_centered with edge fluxes (orders 2/4) */
+int f2d_flx_adv_centered(const int8_t *msk, const double *x, double *y, const double *u,
+                         const double *v, double *xflx, double *yflx, const double *cst,
+                         int nh, int method, int order, int m, int n, void *stream);
+
+/* ------------------------------------------------ fortran_operators ---- */
+/* core/fortran_operators.f90:2-39 computeorthogradient(msk,psi,dx,dy,nh,u,v),
+ * called from core/operators.py:493 */
+int f2d_computeorthogradient(const int8_t *msk, const double *psi, double dx, double dy,
+                             int nh, int m, int n, double *u, double *v, void *stream);
+/* core/fortran_operators.f90:44-64 celltocorner(xr,xp), core/operators.py:440 */
+int f2d_celltocorner(const double *xr, double *xp, int m, int n, void *stream);
+/* core/fortran_operators.f90:102-122 cornertocell(xp,xr), core/quasigeostrophic.py:199 */
+int f2d_cornertocell(const double *xp, double *xr, int m, int n, void *stream);
+/* core/fortran_operators.f90:125-156 add_diffusion(msk,trac,dx,nh,Kdiff,dtrac),
+ * core/operators.py:298 */
+int f2d_add_diffusion(const int8_t *msk, const double *trac, double dx, int nh, double Kdiff,
+                      double *dtrac, int m, int n, void *stream);
+/* core/fortran_operators.f90:330-381 add_torque(msk,buoy,dx,nh,gravity,domega),
+ * core/operators.py:312 */
+int f2d_add_torque(const int8_t *msk, const double *buoy, double dx, int nh, double gravity,
+                   double *domega, int m, int n, void *stream);
+
+/* ------------------------------------------------ fortran_diag --------- */
+/* The f2py intent(out) scalars are written to the DEVICE array "out".
+ * (scratch: the per-block partial sums) */
+/* core/fortran_diag.f90:3-30 z=computedotprod(msk,x,y,nh) -> out[0]=z */
+int f2d_computedotprod(const int8_t *msk, const double *x, const double *y, int nh, int m,
+                       int n, double *out, void *stream);
+/* core/fortran_diag.f90:33-60 y=computemax(msk,x,nh) -> out[0] */
+int f2d_computemax(const int8_t *msk, const double *x, int nh, int m, int n, double *out,
+                   void *stream);
+/* core/fortran_diag.f90:63-90 y=computesum(msk,x,nh) -> out[0] */
+int f2d_computesum(const int8_t *msk, const double *x, int nh, int m, int n, double *out,
+                   void *stream);
+/* core/fortran_diag.f90:93-120 y,y2=computesumandnorm(msk,x,nh) -> out[0..1] */
+int f2d_computesumandnorm(const int8_t *msk, const double *x, int nh, int m, int n,
+                          double *out, void *stream);
+/* core/fortran_diag.f90:123-152 y,ymax=computenormmaxu(msk,x,nh) -> out[0..1] */
+int f2d_computenormmaxu(const int8_t *msk, const double *x, int nh, int m, int n,
+                        double *out, void *stream);
+/* core/fortran_diag.f90:155-195 ke,maxu=computekemaxu(msk,u,v,nh) -> out[0..1],
+ * called from core/euler.py:197 */
+int f2d_computekemaxu(const int8_t *msk, const double *u, const double *v, int nh, int m,
+                      int n, double *out, void *stream);
+/* core/fortran_diag.f90:198-236 ke,maxu,maxv=computekemaxuv(msk,u,v,nh) -> out[0..2] */
+int f2d_computekemaxuv(const int8_t *msk, const double *u, const double *v, int nh, int m,
+                       int n, double *out, void *stream);
+/* core/fortran_diag.f90:239-267 ke=computekewithpsi(msk,omega,psi,nh) -> out[0] */
+int f2d_computekewithpsi(const int8_t *msk, const double *omega, const double *psi, int nh,
+                         int m, int n, double *out, void *stream);
+
+/* ------------------------------------------------ gmg.fortran_multigrid */
+/* core/gmg/fortran_multigrid.f90:2-127 smoothtwicewitha(msk,A,x,b,coef,yo), called from
+ * core/gmg/level.py:351.  x is updated in place exactly as the Fortran
+ * updates it (including the cells its 3-row buffer writes back along the
+ * edges).  The reference's yo buffer is replaced by a library scratch
+ * array (scratch). */
+int f2d_smoothtwicewitha(const int8_t *msk, const double *A, double *x, const double *b,
+                         double coef, int m, int n, void *stream);
+/* core/gmg/fortran_multigrid.f90:320-362 computeresidualwitha(msk,A,x,b,y),
+ * core/gmg/level.py:374 */
+int f2d_computeresidualwitha(const int8_t *msk, const double *A, const double *x,
+                             const double *b, double *y, int m, int n, void *stream);
+/* core/gmg/fortran_multigrid.f90:365-412 fillhalo(x,nh), core/gmg/halo.py:141 */
+int f2d_fillhalo(double *x, int nh, int m, int n, void *stream);
+/* core/gmg/fortran_multigrid.f90:415-498 interpolate(msk1,msk2,x2,nh,x1),
+ * core/gmg/level.py:460; fine (m1,n1), coarse (m2,n2) */
+int f2d_interpolate(const int8_t *msk1, const int8_t *msk2, const double *x2, int nh, int m2,
+                    int n2, int m1, int n1, double *x1, void *stream);
+/* core/gmg/fortran_multigrid.f90:501-546 restrict(msk2,x1,nh,x2), core/gmg/level.py:483 */
+int f2d_restrict(const int8_t *msk2, const double *x1, int nh, int m2, int n2, int m1, int n1,
+                 double *x2, void *stream);
+/* core/gmg/fortran_multigrid.f90:706-811 Acoarse=coarsenmatrix(Afine,msk1,msk2,nh),
+ * core/gmg/level.py:321.  Afine (9,m1,n1), Acoarse (9,m2,n2) planar; only
+ * coarse rows/columns nh-1..m2-nh-1 (0-based) are written. */
+int f2d_coarsenmatrix(const double *Afine, const int8_t *msk1, const int8_t *msk2, int nh,
+                      int m1, int n1, int m2, int n2, double *Acoarse, void *stream);
+/* core/gmg/fortran_multigrid.f90:813-839 y=computenorm(msk,x,nh) -> out[0] (sum of squares) */
+int f2d_computenorm(const int8_t *msk, const double *x, int nh, int m, int n, double *out,
+                    void *stream);
+/* core/gmg/fortran_multigrid.f90:841-867 z=computeinner(msk,x,y,nh) -> out[0] */
+int f2d_computeinner(const int8_t *msk, const double *x, const double *y, int nh, int m,
+                     int n, double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUID2D_GB300_H */

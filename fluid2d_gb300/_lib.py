@@ -22,9 +22,10 @@ BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
            "kernels_fused.cu"]
-HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh"]
+HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-fvisibility=hidden"]
 VARIANTS = {
     "product": ("libfluid2d_gb300.so", []),
     "exact": ("libfluid2d_gb300_exact.so", ["-DF2D_EXACT", "-fmad=false"]),
@@ -148,7 +149,51 @@ SIGNATURES = {
     "f2d_computenorm": [_P, _P, _I, _I, _I, _P, _P],
     "f2d_computeinner": [_P, _P, _P, _I, _I, _I, _P, _P],
 }
+_PP = ctypes.POINTER(ctypes.c_void_p)
+_PI = ctypes.POINTER(ctypes.c_int)
+_PDd = ctypes.POINTER(ctypes.c_double)
+_PPD = ctypes.POINTER(ctypes.POINTER(ctypes.c_double))
+
+
+class ModelDesc(ctypes.Structure):
+    """f2d_model_desc of include/fluid2d_gb300.h"""
+    _fields_ = [("model", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("Lx", ctypes.c_double), ("Ly", ctypes.c_double), ("perio", ctypes.c_int),
+                ("order", ctypes.c_int), ("flux_method", ctypes.c_int),
+                ("aparab", ctypes.c_double), ("gravity", ctypes.c_double),
+                ("Rd", ctypes.c_double), ("beta", ctypes.c_double),
+                ("hydroepsilon", ctypes.c_double), ("adaptable_dt", ctypes.c_int),
+                ("dt", ctypes.c_double), ("cfl", ctypes.c_double), ("dtmax", ctypes.c_double),
+                ("precision", ctypes.c_int)]
+
+
+SIGNATURES.update({
+    "f2d_gmg_create": [_P, _I, _I, _D, _D, _D, _I, _D, _PP],
+    "f2d_gmg_destroy": [_P],
+    "f2d_gmg_levels": [_P, _PI, _PI, _PI, _PI],
+    "f2d_gmg_twovcycle": [_P, _P, _P, _P],
+    "f2d_gmg_solve": [_P, _P, _P, _I, _D, _P],
+    "f2d_gmg_solve_stats": [_P, _PI, _PDd, _PI],
+    "f2d_gmg_vcycle": [_P, _I, _P],
+    "f2d_gmg_fcycle": [_P, _I, _P],
+    "f2d_model_create": [ctypes.POINTER(ModelDesc), _P, _PP],
+    "f2d_model_destroy": [_P],
+    "f2d_model_info": [_P, _PI, _PI, _PI, _PI, _PI, _PPD, _PPD],
+    "f2d_model_set_psi": [_P, _P],
+    "f2d_model_diagnostics": [_P, _P],
+    "f2d_model_step": [_P, _I, _P],
+    "f2d_model_step_graph": [_P, _I, _P],
+    "f2d_model_set_dt": [_P, _D],
+    "f2d_model_solve_stats": [_P, _PI, _PDd, _PI],
+    "f2d_model_probe": [_P, _I, _PI, _PDd],
+    "f2d_model_graph_kernels": [_P, _PI],
+})
+
 EXTRA = {
+    "f2d_gmg_level_ptr": ([_P, _I, ctypes.c_char_p], _P),
+    "f2d_model_varname": ([_P, _I], ctypes.c_char_p),
+    "f2d_model_diagname": ([_P, _I], ctypes.c_char_p),
+    "f2d_model_buffer": ([_P, ctypes.c_char_p], _P),
     "f2d_version": ([], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),

@@ -1,0 +1,1230 @@
+// engine.cu -- device-resident multigrid and model time steppers.
+//
+//   Gmg    : core/gmg/hierarchy.py (Gridinfo, set_msk_laplacian, Vcycle,
+//            Fcycle, solve, twoVcycle) on one GPU, one rank.
+//   Model  : core/euler.py, core/boussinesq.py, core/quasigeostrophic.py
+//            stepped with core/timescheme.py:167-180 (RK3_SSP), the
+//            Operators of core/operators.py and the set_dt of
+//            core/fluid2d.py:376-397, all on the device: a step makes no
+//            host synchronisation, so it can be captured in a CUDA graph.
+//
+// Set-up reuses the drop-in kernels (restrict, fillhalo, coarsenmatrix) to
+// build every level's mask and Galerkin operator on the device.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/fluid2d_gb300.h"
+#include "f2d_common.cuh"
+#include "f2d_fused.cuh"
+#include "f2d_kernels.cuh"
+#include "f2d_adv.cuh"
+
+namespace f2d {
+
+#define TRY(x)                      \
+    do {                            \
+        int _st = (x);              \
+        if (_st) return _st;        \
+    } while (0)
+
+// ------------------------------------------------------------ arena
+// One cudaMalloc per object; sub-buffers 256-byte aligned.
+struct Arena {
+    std::vector<size_t> sizes;
+    char *base = nullptr;
+    size_t total = 0;
+    size_t add(size_t bytes) {
+        size_t o = total;
+        total += (bytes + 255) & ~(size_t)255;
+        sizes.push_back(bytes);
+        return o;
+    }
+    int alloc() {
+        if (total == 0) total = 256;
+        TRY(cuda_status(cudaMalloc((void **)&base, total), "engine cudaMalloc"));
+        return cuda_status(cudaMemset(base, 0, total), "engine cudaMemset");
+    }
+    template <typename P>
+    P *at(size_t o) const { return (P *)(base + o); }
+    ~Arena() {
+        if (base) cudaFree(base);
+    }
+};
+
+// ------------------------------------------------------------ setup kernels
+// A0 (9 planes) = stencil*coef*msk(nb)*msk on rows/cols 1..m-2
+// (core/gmg/level.py:281-298); the halo is filled afterwards.
+__global__ void k_a0_9(const int8_t *msk, int mv, int nv, const double *sc9, double *A9) {
+    int i = 1 + blockIdx.x * 32 + threadIdx.x;
+    int j = 1 + blockIdx.y * 8 + threadIdx.y;
+    if (i > nv - 2 || j > mv - 2) return;
+    const size_t pl = (size_t)mv * nv;
+    for (int k = 0; k < 9; k++) {
+        int di = k % 3 - 1, dj = k / 3 - 1;
+        A9[k * pl + off(j, i, nv)] =
+            sc9[k] * (double)msk[off(j + dj, i + di, nv)] * (double)msk[off(j, i, nv)];
+    }
+}
+
+__global__ void k_fill_value(double *x, size_t n, double v) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = v;
+}
+
+__global__ void k_i8_to_f64(const int8_t *m, double *x, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = (double)m[q];
+}
+
+// coarse mask: ones, zero where the restricted fine mask <= 0.5 (core/gmg/level.py:233-236)
+__global__ void k_threshold(const double *coef, int8_t *msk, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        msk[q] = coef[q] <= 0.5 ? 0 : 1;
+}
+
+// keep planes 0..4, Helmholtz shift of A5 (core/gmg/hierarchy.py:80-84),
+// C3 = omega/|A5|, plus float copies for the mixed form
+__global__ void k_finalize_A(const double *A9, int qg, double rd2inv, double omega, double *A6,
+                             float *A6f, size_t pl) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < pl;
+         q += (size_t)gridDim.x * blockDim.x) {
+        double a[5];
+        for (int k = 0; k < 5; k++) a[k] = A9[k * pl + q];
+        if (qg && a[4] != 0.) a[4] -= rd2inv;
+        for (int k = 0; k < 5; k++) A6[k * pl + q] = a[k];
+        double c3 = omega / fabs(a[4]);
+        A6[5 * pl + q] = c3;
+        if (A6f) {
+            for (int k = 0; k < 5; k++) A6f[k * pl + q] = (float)a[k];
+            A6f[5 * pl + q] = (float)c3;
+        }
+    }
+}
+
+static int blocks_for(size_t n) {
+    size_t b = (n + 255) / 256;
+    return (int)(b > 4096 ? 4096 : (b ? b : 1));
+}
+
+// ------------------------------------------------------------ solve control
+struct SolveState {
+    double normb, res0, res;
+    int nite, ndiv, active, status, maxite;
+    double tol;
+};
+
+// after the first residual: normb, res0, active (core/gmg/hierarchy.py:158-169)
+__global__ void k_solve_init(SolveState *st, const double *sumb, const double *sumr, int maxite,
+                             double tol) {
+    double normb = sqrt(sumb[0] / 1.0);
+    st->normb = normb;
+    st->nite = 0;
+    st->ndiv = 0;
+    st->status = 0;
+    st->maxite = maxite;
+    st->tol = tol;
+    if (normb > 0) {
+        st->res0 = sqrt(sumr[0] / 1.0) / normb;
+        st->res = st->res0;
+        st->active = (0 < maxite) && (st->res0 > tol);
+    } else {
+        st->res0 = 0.;
+        st->res = 0.;
+        st->active = 0;
+    }
+}
+
+// after each F-cycle's residual (core/gmg/hierarchy.py:172-188)
+__global__ void k_solve_update(SolveState *st, const double *sumr) {
+    if (!st->active) return;
+    double res = sqrt(sumr[0] / 1.0) / st->normb;
+    double conv = st->res0 / res;
+    st->res0 = res;
+    st->res = res;
+    st->nite += 1;
+    if (conv < 1) st->ndiv += 1;
+    if (st->ndiv > 4) {
+        st->status = ERR_DIVERGED;
+        st->active = 0;
+        return;
+    }
+    st->active = (st->nite < st->maxite) && (st->res0 > st->tol);
+}
+
+// ------------------------------------------------------------ Gmg
+struct LevelInfo {
+    int n, m;       // interior
+    double dx, dy;
+};
+
+// core/gmg/level.py:24-117 for one rank, stopping before an odd dimension
+static std::vector<LevelInfo> gridinfo(int n, int m, double dx, double dy, int n0 = 4) {
+    std::vector<LevelInfo> v;
+    for (int lev = 0;; lev++) {
+        if (lev > 0) {
+            n /= 2;
+            m /= 2;
+            dx *= 2;
+            dy *= 2;
+        }
+        bool last = (n <= n0) || (m <= n0) || (n % 2 == 1) || (m % 2 == 1);
+        v.push_back({n, m, dx, dy});
+        if (last || lev >= MAX_LEVELS - 1) break;
+    }
+    return v;
+}
+
+struct Gmg {
+    int nlev = 0;
+    std::vector<LevelInfo> info;
+    int mv[MAX_LEVELS], nv[MAX_LEVELS];
+    double omega = 8. / 9.;
+    int ndeepest = 16;
+    Analytic an{};
+    int cs = 1;  // first level of the coarse CTA (== nlev: none)
+    size_t smem64 = 0, smem32 = 0;
+    Arena mem;
+    LevelView<double> d[MAX_LEVELS];
+    LevelView<float> f[MAX_LEVELS];
+    bool has_f32 = false;
+    double *work = nullptr;      // reduction workspace (RED_MAX_BLOCKS * RED_MAX_VALUES)
+    double *sums = nullptr;      // 4 device scalars
+    SolveState *solve_state = nullptr;
+    double *x0_extra = nullptr;  // level-0 correction for solve (the reference's self.x[0])
+    // optional timing probe: CUDA events around every finest-level smooth
+    // (the two sweep kernels) recorded on the launching stream
+    static constexpr int MAX_PROBES = 64;
+    bool probe = false;
+    int nprobe = 0;
+    cudaEvent_t ev[MAX_PROBES][2] = {};
+    ~Gmg() {
+        for (int k = 0; k < MAX_PROBES; k++)
+            for (int e = 0; e < 2; e++)
+                if (ev[k][e]) cudaEventDestroy(ev[k][e]);
+    }
+
+    int setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, double hydroeps,
+              double om, bool qg, double Rd, bool f32, cudaStream_t s);
+    template <typename T>
+    int smooth(LevelView<T> *L, int l, bool zero, const int *active, cudaStream_t s);
+    template <typename T>
+    int coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int *active,
+               cudaStream_t s);
+    template <typename T>
+    int vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s);
+    template <typename T>
+    int fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s);
+};
+
+template <typename T>
+static T cast(double v) { return (T)v; }
+
+int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, double hydroeps,
+               double om, bool qg, double Rd, bool f32, cudaStream_t s) {
+    omega = om;
+    info = gridinfo(nx, ny, dx, dy);
+    nlev = (int)info.size();
+    for (int l = 0; l < nlev; l++) {
+        if (info[l].n < NH || info[l].m < NH) {
+            set_error("multigrid: level %d is %dx%d, below the halo width", l, info[l].n,
+                      info[l].m);
+            return ERR_SHAPE;
+        }
+        nv[l] = info[l].n + 2 * NH;
+        mv[l] = info[l].m + 2 * NH;
+        if (hydroeps * info[l].dy / info[l].dx <= .2) {
+            set_error("multigrid: aspect ratio %g needs the tridiagonal relaxation "
+                      "(core/gmg/level.py:153-163), not supported on the GPU",
+                      hydroeps * info[l].dy / info[l].dx);
+            return ERR_ARG;
+        }
+    }
+    has_f32 = f32;
+    // first level of the coarse CTA: the largest suffix of levels >= 1 that
+    // fits in shared memory
+    cs = nlev;
+    for (int l = nlev - 1; l >= 1; l--) {
+        if (coarse_smem_bytes<double>(mv + l, nv + l, nlev - l) <= 200 * 1024) cs = l;
+        else break;
+    }
+    if (cs < nlev) {
+        smem64 = coarse_smem_bytes<double>(mv + cs, nv + cs, nlev - cs);
+        smem32 = coarse_smem_bytes<float>(mv + cs, nv + cs, nlev - cs);
+    }
+
+    // ---- memory
+    size_t o_msk[MAX_LEVELS], o_A[MAX_LEVELS], o_Af[MAX_LEVELS], o_x[MAX_LEVELS],
+        o_b[MAX_LEVELS], o_r[MAX_LEVELS], o_t[MAX_LEVELS], o_xf[MAX_LEVELS], o_bf[MAX_LEVELS],
+        o_rf[MAX_LEVELS], o_tf[MAX_LEVELS], o_A9[MAX_LEVELS];
+    size_t maxpl = 0;
+    for (int l = 0; l < nlev; l++) {
+        size_t pl = (size_t)mv[l] * nv[l];
+        maxpl = pl > maxpl ? pl : maxpl;
+        o_msk[l] = mem.add(pl);
+        o_A[l] = l > 0 ? mem.add(6 * pl * sizeof(double)) : 0;
+        o_Af[l] = (l > 0 && f32) ? mem.add(6 * pl * sizeof(float)) : 0;
+        o_A9[l] = mem.add(9 * pl * sizeof(double));  // set-up only
+        o_x[l] = mem.add(pl * sizeof(double));
+        o_b[l] = mem.add(pl * sizeof(double));
+        o_r[l] = mem.add(pl * sizeof(double));
+        o_t[l] = mem.add(pl * sizeof(double));
+        if (f32) {
+            o_xf[l] = mem.add(pl * sizeof(float));
+            o_bf[l] = mem.add(pl * sizeof(float));
+            o_rf[l] = mem.add(pl * sizeof(float));
+            o_tf[l] = mem.add(pl * sizeof(float));
+        }
+    }
+    size_t o_coef = mem.add(maxpl * sizeof(double));
+    size_t o_work = mem.add(sizeof(double) * RED_MAX_BLOCKS * RED_MAX_VALUES);
+    size_t o_sums = mem.add(8 * sizeof(double));
+    size_t o_solve = mem.add(sizeof(SolveState));
+    size_t o_sc9 = mem.add(16 * sizeof(double));
+    size_t o_ones = mem.add(maxpl);
+    TRY(mem.alloc());
+    work = mem.at<double>(o_work);
+    sums = mem.at<double>(o_sums);
+    solve_state = mem.at<SolveState>(o_solve);
+    for (int l = 0; l < nlev; l++) {
+        d[l].mv = f[l].mv = mv[l];
+        d[l].nv = f[l].nv = nv[l];
+        d[l].msk = f[l].msk = mem.at<int8_t>(o_msk[l]);
+        d[l].A = l > 0 ? mem.at<double>(o_A[l]) : nullptr;
+        f[l].A = (l > 0 && f32) ? mem.at<float>(o_Af[l]) : nullptr;
+        d[l].x = mem.at<double>(o_x[l]);
+        d[l].b = mem.at<double>(o_b[l]);
+        d[l].r = mem.at<double>(o_r[l]);
+        d[l].t = mem.at<double>(o_t[l]);
+        if (f32) {
+            f[l].x = mem.at<float>(o_xf[l]);
+            f[l].b = mem.at<float>(o_bf[l]);
+            f[l].r = mem.at<float>(o_rf[l]);
+            f[l].t = mem.at<float>(o_tf[l]);
+        }
+    }
+    x0_extra = d[0].x;
+
+    // ---- finest level: mask and analytic operator (core/gmg/level.py:261-302)
+    size_t pl0 = (size_t)mv[0] * nv[0];
+    TRY(cuda_status(cudaMemcpyAsync((void *)d[0].msk, mskp_host, pl0, cudaMemcpyHostToDevice, s),
+                    "mask upload"));
+    double bx = dy / dx * hydroeps, by = dx / dy;
+    double a = -2 * (bx + by), b = 0., c = 0.;
+    double st[9] = {c, by, c, bx, a, bx, c, by, c};
+    if (dx == dy && hydroeps == 1) {
+        a = -6. / 2;
+        b = 1. / 2;
+        c = 0.5 / 2;
+        double s9[9] = {c, b, c, b, a, b, c, b, c};
+        memcpy(st, s9, sizeof(st));
+    }
+    double coef = 1. / (dx * dy);
+    double sc9[9];
+    for (int k = 0; k < 9; k++) sc9[k] = st[k] * coef;
+    for (int k = 0; k < 5; k++) an.sc[k] = sc9[k];
+    an.a5 = sc9[4] * 1. * 1.;
+    if (qg) an.a5 -= 1. / (Rd * Rd);
+    an.c3 = omega / fabs(an.a5);
+    TRY(cuda_status(cudaMemcpyAsync(mem.at<double>(o_sc9), sc9, sizeof(sc9),
+                                    cudaMemcpyHostToDevice, s),
+                    "stencil upload"));
+    {
+        dim3 bl(32, 8);
+        k_a0_9<<<grid2d(mv[0] - 2, nv[0] - 2, bl), bl, 0, s>>>(
+            d[0].msk, mv[0], nv[0], mem.at<double>(o_sc9), mem.at<double>(o_A9[0]));
+        TRY(launch_status("A0"));
+        for (int k = 0; k < 9; k++)
+            TRY(launch_fillhalo(mem.at<double>(o_A9[0]) + k * pl0, NH, mv[0], nv[0], s));
+    }
+    // ---- coarser levels (core/gmg/level.py:227-243, 304-327)
+    int8_t *ones = mem.at<int8_t>(o_ones);
+    TRY(cuda_status(cudaMemsetAsync(ones, 1, maxpl, s), "ones"));
+    double *coefb = mem.at<double>(o_coef);
+    double rd2inv = qg ? 1. / (Rd * Rd) : 0.;
+    for (int l = 1; l < nlev; l++) {
+        size_t plf = (size_t)mv[l - 1] * nv[l - 1], pl = (size_t)mv[l] * nv[l];
+        double *mskf = d[l].t;  // scratch: the finer mask as float64 (fits: plf <= 4 pl + ...)
+        double *mskf_big = d[l - 1].r;
+        (void)mskf;
+        k_i8_to_f64<<<blocks_for(plf), 256, 0, s>>>(d[l - 1].msk, mskf_big, plf);
+        k_fill_value<<<blocks_for(pl), 256, 0, s>>>(coefb, pl, 1.0);
+        TRY(launch_restrict(ones, mskf_big, NH, mv[l], nv[l], mv[l - 1], nv[l - 1], coefb, s));
+        TRY(launch_fillhalo(coefb, NH, mv[l], nv[l], s));
+        k_threshold<<<blocks_for(pl), 256, 0, s>>>(coefb, (int8_t *)d[l].msk, pl);
+        TRY(launch_status("coarse mask"));
+        TRY(launch_coarsenmatrix(mem.at<double>(o_A9[l - 1]), d[l - 1].msk, d[l].msk, NH,
+                                 mv[l - 1], nv[l - 1], mv[l], nv[l], mem.at<double>(o_A9[l]), s));
+        for (int k = 0; k < 9; k++)
+            TRY(launch_fillhalo(mem.at<double>(o_A9[l]) + k * pl, NH, mv[l], nv[l], s));
+    }
+    for (int l = 1; l < nlev; l++) {
+        size_t pl = (size_t)mv[l] * nv[l];
+        k_finalize_A<<<blocks_for(pl), 256, 0, s>>>(mem.at<double>(o_A9[l]), qg, rd2inv, omega,
+                                                    (double *)d[l].A,
+                                                    f32 ? (float *)f[l].A : nullptr, pl);
+        TRY(launch_status("finalize A"));
+    }
+    for (int l = 0; l < nlev; l++) {
+        size_t pl = (size_t)mv[l] * nv[l];
+        TRY(cuda_status(cudaMemsetAsync(d[l].r, 0, pl * sizeof(double), s), "clear"));
+    }
+    return OK;
+}
+
+template <typename T>
+int Gmg::smooth(LevelView<T> *L, int l, bool zero, const int *active, cudaStream_t s) {
+    const Analytic *a0 = l == 0 ? &an : nullptr;
+    T c1 = (T)omega, c2 = (T)(1. - omega);
+    const bool pr = probe && l == 0 && nprobe < MAX_PROBES;
+    if (pr) {
+        for (int e = 0; e < 2; e++)
+            if (!ev[nprobe][e]) TRY(cuda_status(cudaEventCreate(&ev[nprobe][e]), "probe event"));
+        // external record: inside stream capture it becomes an event-record node
+        TRY(cuda_status(cudaEventRecordWithFlags(ev[nprobe][0], s, cudaEventRecordExternal),
+                        "probe record"));
+    }
+    TRY(mg_sweep1<T>(L[l], a0, c1, c2, zero, active, s));
+    TRY(mg_sweep2<T>(L[l], a0, c1, c2, active, s));
+    if (pr) {
+        TRY(cuda_status(cudaEventRecordWithFlags(ev[nprobe][1], s, cudaEventRecordExternal),
+                        "probe record"));
+        nprobe++;
+    }
+    return OK;
+}
+
+template <typename T>
+int Gmg::coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int *active,
+                cudaStream_t s) {
+    CoarseArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.nlev = nlev - start;
+    for (int l = start; l < nlev; l++) a.lev[l - start] = L[l];
+    a.c1 = (T)omega;
+    a.c2 = (T)(1. - omega);
+    a.mode = mode;
+    a.zero_first = zero_first;
+    a.ndeepest = ndeepest;
+    a.active = active;
+    size_t smem = coarse_smem_bytes<T>(mv + start, nv + start, nlev - start);
+    return mg_coarse<T>(a, smem, s);
+}
+
+// core/gmg/hierarchy.py:98-126
+template <typename T>
+int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s) {
+    const int deep = nlev - 1;
+    if (l1 >= cs) return coarse(L, l1, CYCLE_V, zero_first, active, s);
+    const int stop = cs < deep ? cs : deep;
+    for (int l = l1; l < stop; l++) {
+        TRY(smooth(L, l, zero_first || l > l1, active, s));
+        TRY(mg_residual<T>(L[l], l == 0 ? &an : nullptr, L[l].x, L[l].b, L[l].r, active, s));
+        TRY(mg_restrict<T>(L[l], L[l].r, L[l + 1], L[l + 1].b, active, s));
+    }
+    if (cs <= deep) {
+        TRY(coarse(L, cs, CYCLE_V, true, active, s));
+    } else {
+        for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0, active, s));
+    }
+    for (int l = stop - 1; l >= l1; l--) {
+        TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, false, active, s));
+        TRY(smooth(L, l, false, active, s));
+    }
+    return OK;
+}
+
+// core/gmg/hierarchy.py:131-151
+template <typename T>
+int Gmg::fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s) {
+    const int deep = nlev - 1;
+    if (l1 >= cs) return coarse(L, l1, CYCLE_F, false, active, s);
+    const int stop = cs < deep ? cs : deep;
+    for (int l = l1; l < stop; l++) TRY(mg_restrict<T>(L[l], L[l].b, L[l + 1], L[l + 1].b, active, s));
+    if (cs <= deep) {
+        TRY(coarse(L, cs, CYCLE_F, false, active, s));
+    } else {
+        for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0, active, s));
+    }
+    for (int l = stop - 1; l >= l1; l--) {
+        TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, true, active, s));
+        TRY(vcycle(L, l, false, active, s));
+    }
+    return OK;
+}
+
+// twoVcycle (core/gmg/hierarchy.py:207-218): x is updated in place, b read
+static int two_vcycle(Gmg &g, double *x, const double *b, cudaStream_t s) {
+    LevelView<double> L[MAX_LEVELS];
+    for (int l = 0; l < g.nlev; l++) L[l] = g.d[l];
+    L[0].x = x;
+    L[0].b = (double *)b;
+    for (int k = 0; k < 2; k++) TRY(g.vcycle(L, 0, false, nullptr, s));
+    return OK;
+}
+
+// solve (core/gmg/hierarchy.py:154-192) in correction form, device-resident:
+// every iteration is launched; iterations after convergence are no-ops
+// through the device flag SolveState::active.
+static int solve(Gmg &g, double *x, const double *b, int maxite, double tol, cudaStream_t s) {
+    LevelView<double> L[MAX_LEVELS];
+    for (int l = 0; l < g.nlev; l++) L[l] = g.d[l];
+    LevelView<double> &L0 = L[0];
+    // g.residual(x, b, self.b[0])
+    TRY(mg_residual<double>(L0, &g.an, x, b, L0.b, nullptr, s));
+    TRY(launch_reduce(8, L0.msk, b, nullptr, NH, L0.mv, L0.nv, g.sums + 0, g.work, s));
+    TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
+    k_solve_init<<<1, 1, 0, s>>>(g.solve_state, g.sums + 0, g.sums + 1, maxite, tol);
+    TRY(launch_status("solve init"));
+    const int *active = &g.solve_state->active;
+    const size_t pl = (size_t)L0.mv * L0.nv;
+    for (int it = 0; it < maxite; it++) {
+        TRY(g.fcycle(L, 0, active, s));
+        TRY(vec_add(x, L0.x, pl, active, s));
+        TRY(mg_residual<double>(L0, &g.an, x, b, L0.b, active, s));
+        TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
+        k_solve_update<<<1, 1, 0, s>>>(g.solve_state, g.sums + 1);
+        TRY(launch_status("solve update"));
+    }
+    return OK;
+}
+
+// ------------------------------------------------------------ model
+enum ModelKind { M_EULER = 0, M_BOUSSINESQ = 1, M_QG = 2 };
+
+// names of the state variables (core/euler.py:36-37, core/boussinesq.py:30-31,
+// core/quasigeostrophic.py:32)
+static const char *VARNAMES[3][6] = {
+    {"vorticity", "psi", "u", "v", "source", nullptr},
+    {"vorticity", "psi", "u", "v", "buoyancy", "banom"},
+    {"pv", "psi", "u", "v", "pvanom", "vorticity"}};
+static const int NVAR[3] = {5, 6, 6};
+static const int NDIAG[3] = {8, 8, 6};
+
+struct DiagArgs {
+    int kind;
+    const int8_t *msk;
+    const double *s;  // state
+    size_t pl;
+    int mv, nv;
+    double dx, dy;     // coordinates xr, yr of core/grid.py:49-52
+    double gravity, Rd, area;
+    double *part;      // partials
+    double *out;       // NDIAG values
+};
+
+// diagnostics of core/euler.py:185-223, core/boussinesq.py:123-153,
+// core/quasigeostrophic.py:189-218 in one pass (8 accumulators)
+__global__ void __launch_bounds__(RED_THREADS) k_diag_partial(DiagArgs a, int rpb) {
+    __shared__ double sh[8 * RED_THREADS];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int rows = a.mv - 2 * NH, cols = a.nv - 2 * NH;
+    const int r0 = blockIdx.x * rpb, r1 = min(rows, r0 + rpb);
+    const long long cells = (long long)(r1 - r0) * cols;
+    const double *s = a.s;
+    const size_t pl = a.pl;
+    const int nv = a.nv;
+    for (long long q = threadIdx.x; q < cells; q += RED_THREADS) {
+        const int j = NH + r0 + (int)(q / cols), i = NH + (int)(q % cols);
+        const size_t p = off(j, i, nv);
+        const int mc = a.msk[p];
+        const double *u = s + 2 * pl, *v = s + 3 * pl;
+        if (mc == 1) {  // computekemaxu (core/fortran_diag.f90:179-189)
+            double ua = u[p], ub = u[p - 1], va = v[p], vb = v[p - nv];
+            acc[1] += (ua * ua + ub * ub) + (va * va + vb * vb);
+            double sp = fabs(ua + ub) + fabs(va + vb);
+            acc[0] = acc[0] > sp ? acc[0] : sp;
+        }
+        if (a.kind == M_EULER) {
+            const double w = s[p];
+            if (mc == 1) {
+                acc[2] += w;
+                acc[3] += w * w;
+            }
+            if (mc != 0) {
+                double xr = ((double)i + 0.5 - NH + 0) * a.dx;
+                double yr = ((double)j + 0.5 - NH + 0) * a.dy;
+                acc[4] += w * xr;
+                acc[5] += w * yr;
+                acc[6] += s[pl + p];          // psi
+                acc[7] += w * s[4 * pl + p];  // source
+            }
+        } else if (a.kind == M_BOUSSINESQ) {
+            const double w = s[p], b = s[4 * pl + p];
+            if (mc == 1) {
+                acc[2] += w;
+                acc[3] += w * w;
+                acc[5] += b;
+                acc[6] += b * b;
+            }
+            if (mc != 0) {
+                double yr = ((double)j + 0.5 - NH + 0) * a.dy;
+                acc[4] += b * yr;
+            }
+        } else {
+            const double pv = s[p];
+            const double *psi = s + pl;
+            if (mc == 1) {
+                acc[2] += pv;
+                acc[3] += pv * pv;
+                // cornertocell (core/fortran_operators.f90:118) then sum of squares
+                double wc = 0.25 * (psi[p] + psi[p - 1] + psi[p - nv] + psi[p - nv - 1]);
+                acc[4] += wc * wc;
+            }
+        }
+    }
+    double v8[8];
+    bool mx[8] = {true, false, false, false, false, false, false, false};
+    for (int k = 0; k < 8; k++) v8[k] = acc[k];
+    block_reduce<8>(v8, mx, sh);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 8; k++) a.part[k * RED_MAX_BLOCKS + blockIdx.x] = v8[k];
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a, int nb) {
+    __shared__ double sh[8 * RED_THREADS];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = threadIdx.x; b < nb; b += RED_THREADS)
+        for (int k = 0; k < 8; k++) {
+            double v = a.part[k * RED_MAX_BLOCKS + b];
+            acc[k] = k == 0 ? (acc[k] > v ? acc[k] : v) : acc[k] + v;
+        }
+    bool mx[8] = {true, false, false, false, false, false, false, false};
+    block_reduce<8>(acc, mx, sh);
+    if (threadIdx.x) return;
+    const double area = a.area;
+    const double maxu = acc[0] * 0.5, ke = acc[1] * 0.25;
+    if (a.kind == M_EULER) {
+        a.out[0] = maxu;
+        a.out[1] = ke / area;
+        a.out[2] = acc[2] / area;
+        a.out[3] = 0.5 * acc[3] / area;
+        a.out[4] = acc[4] / area;
+        a.out[5] = acc[5] / area;
+        a.out[6] = acc[6] / area;
+        a.out[7] = acc[7] / area;
+    } else if (a.kind == M_BOUSSINESQ) {
+        const double pe = -a.gravity * acc[4];
+        a.out[0] = maxu;
+        a.out[1] = ke / area;
+        a.out[2] = pe / area;
+        a.out[3] = (ke + pe) / area;
+        a.out[4] = acc[2] / area;
+        a.out[5] = 0.5 * acc[3] / area;
+        a.out[6] = acc[5] / area;
+        a.out[7] = sqrt(acc[6] / area - (acc[5] / area) * (acc[5] / area));
+    } else {
+        const double ape = 0.5 * acc[4] / (a.Rd * a.Rd);
+        a.out[0] = maxu;
+        a.out[1] = ke / area;
+        a.out[2] = acc[2] / area;
+        a.out[3] = 0.5 * acc[3] / area;
+        a.out[4] = ape / area;
+        a.out[5] = (ke + ape) / area;
+    }
+}
+
+static const char *DIAGNAMES[3][8] = {
+    {"maxspeed", "ke", "vorticity", "enstrophy", "px", "py", "angmom", "source"},
+    {"maxspeed", "ke", "pe", "energy", "vorticity", "enstrophy", "buoyancy", "brms"},
+    {"maxspeed", "ke", "pv", "pv2", "ape", "energy", nullptr, nullptr}};
+
+// set_dt (core/fluid2d.py:376-397): dt and cst[3] = maxspeed of the last
+// diagnostics, plus the flux-splitting constants that adv_upwind derives
+// from cst (core/fortran_advection.f90:46-60), computed once per step
+__global__ void k_set_dt(double *dt, double *cst, SplitConst *advc, const double *diag,
+                         int adaptable, double dt0, double cfl, double hmin, double dtmax) {
+    const double maxspeed = diag[0];
+    double d = dt0;
+    if (adaptable && maxspeed != 0) {
+        d = cfl * hmin / maxspeed;
+        if (d > dtmax) d = dtmax;
+    }
+    *dt = d;
+    cst[3] = maxspeed;
+    *advc = split_const(cst);
+}
+
+// QG fields after the step (core/quasigeostrophic.py:120-122, :186) and the
+// Boussinesq anomaly (core/boussinesq.py:99-100)
+__global__ void k_qg_post(double *s, size_t pl, const double *pvback, double rdm2, int which) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < pl;
+         q += (size_t)gridDim.x * blockDim.x) {
+        double pva = s[q] - pvback[q];  // pvanom = pv - pvback
+        s[4 * pl + q] = pva;
+        if (which) s[5 * pl + q] = pva - rdm2 * s[pl + q];  // vorticity = pvanom - Rd^-2 psi
+    }
+}
+
+__global__ void k_banom(double *s, size_t pl, const double *bref) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < pl;
+         q += (size_t)gridDim.x * blockDim.x)
+        s[5 * pl + q] = s[4 * pl + q] - bref[q];
+}
+
+struct Model {
+    f2d_model_desc desc;
+    int kind, nvar, mv, nv;
+    size_t pl;
+    double dx, dy, area;
+    Gmg gmg;
+    Arena mem;
+    int8_t *msk = nullptr, *mskp = nullptr, *ones = nullptr;
+    double *X, *D[3], *S1, *S2, *B, *cst, *advc, *dt, *diag, *pvback, *bref, *part;
+    int last_nite = 0;
+    int probe_per_step = -1;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+
+    double *plane(double *base, const char *name) {
+        for (int k = 0; k < nvar; k++)
+            if (!strcmp(VARNAMES[kind][k], name)) return base + k * pl;
+        return nullptr;
+    }
+    int create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t s);
+    int invert(double *xs, const char *who, bool full, cudaStream_t s, double *ubase_out = nullptr);
+    int stage(int k, cudaStream_t s);
+    int step(cudaStream_t s);
+    int diagnostics(cudaStream_t s);
+    int set_psi(cudaStream_t s);
+};
+
+int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t s) {
+    desc = *d;
+    kind = d->model;
+    if (kind < 0 || kind > 2) {
+        set_error("model: unknown kind %d", kind);
+        return ERR_ARG;
+    }
+    nvar = NVAR[kind];
+    nv = d->nx + 2 * NH;
+    mv = d->ny + 2 * NH;
+    pl = (size_t)mv * nv;
+    dx = d->Lx / d->nx;
+    dy = d->Ly / d->ny;
+    // corner mask (core/operators.py:47-67): 1 where the 4 cells around the
+    // corner are fluid; the last row and column stay 0 as celltocorner leaves them
+    std::vector<int8_t> mp(pl, 0);
+    double a = 0.;
+    for (int j = 0; j < mv; j++)
+        for (int i = 0; i < nv; i++) {
+            if (j < mv - 1 && i < nv - 1) {
+                double w = 0.25 * ((double)msk_host[off(j, i, nv)] + (double)msk_host[off(j, i + 1, nv)]
+                                   + (double)msk_host[off(j + 1, i, nv)]
+                                   + (double)msk_host[off(j + 1, i + 1, nv)]);
+                mp[off(j, i, nv)] = (w == 1.) ? 1 : 0;
+            }
+            if (j >= NH && j < mv - NH && i >= NH && i < nv - NH) a += msk_host[off(j, i, nv)];
+        }
+    area = a * 1.;
+    if (area <= 0) {
+        set_error("model: the mask has no fluid cell");
+        return ERR_ARG;
+    }
+    size_t o_msk = mem.add(pl), o_mskp = mem.add(pl), o_ones = mem.add(pl);
+    size_t o_X = mem.add(nvar * pl * 8), o_D0 = mem.add(nvar * pl * 8),
+           o_D1 = mem.add(nvar * pl * 8), o_D2 = mem.add(nvar * pl * 8),
+           o_S1 = mem.add(nvar * pl * 8), o_S2 = mem.add(nvar * pl * 8), o_B = mem.add(pl * 8),
+           o_cst = mem.add(8 * 8), o_advc = mem.add(sizeof(SplitConst)), o_dt = mem.add(8),
+           o_diag = mem.add(8 * 8),
+           o_pvb = mem.add(kind == M_QG ? pl * 8 : 8), o_bref = mem.add(kind == M_BOUSSINESQ ? pl * 8 : 8),
+           o_part = mem.add(8 * RED_MAX_BLOCKS * 8);
+    TRY(mem.alloc());
+    msk = mem.at<int8_t>(o_msk);
+    mskp = mem.at<int8_t>(o_mskp);
+    ones = mem.at<int8_t>(o_ones);
+    TRY(cuda_status(cudaMemsetAsync(ones, 1, pl, s), "ones"));
+    X = mem.at<double>(o_X);
+    D[0] = mem.at<double>(o_D0);
+    D[1] = mem.at<double>(o_D1);
+    D[2] = mem.at<double>(o_D2);
+    S1 = mem.at<double>(o_S1);
+    S2 = mem.at<double>(o_S2);
+    B = mem.at<double>(o_B);
+    cst = mem.at<double>(o_cst);
+    advc = mem.at<double>(o_advc);
+    dt = mem.at<double>(o_dt);
+    diag = mem.at<double>(o_diag);
+    pvback = mem.at<double>(o_pvb);
+    bref = mem.at<double>(o_bref);
+    part = mem.at<double>(o_part);
+    TRY(cuda_status(cudaMemcpyAsync(msk, msk_host, pl, cudaMemcpyHostToDevice, s), "msk"));
+    TRY(cuda_status(cudaMemcpyAsync(mskp, mp.data(), pl, cudaMemcpyHostToDevice, s), "mskp"));
+    // cst (core/operators.py:99-119)
+    double c[8] = {dx, dy, 0.05, 0., (d->order % 2 == 0) ? 0. : d->aparab, 0, 0, 0};
+    TRY(cuda_status(cudaMemcpyAsync(cst, c, sizeof(c), cudaMemcpyHostToDevice, s), "cst"));
+    if (kind == M_QG) {
+        // pvback = beta*(yr - Ly*0.5)*msk (core/quasigeostrophic.py:50)
+        std::vector<double> pb(pl);
+        for (int j = 0; j < mv; j++) {
+            double yr = ((double)j + 0.5 - NH + 0) * dy;
+            for (int i = 0; i < nv; i++)
+                pb[off(j, i, nv)] = d->beta * (yr - d->Ly * .5) * (double)msk_host[off(j, i, nv)];
+        }
+        TRY(cuda_status(cudaMemcpyAsync(pvback, pb.data(), pl * 8, cudaMemcpyHostToDevice, s),
+                        "pvback"));
+        TRY(cuda_status(cudaStreamSynchronize(s), "pvback sync"));
+    }
+    TRY(cuda_status(cudaStreamSynchronize(s), "model upload"));
+    return gmg.setup(mp.data(), d->nx, d->ny, dx, dy, kind == M_QG ? 1. : d->hydroepsilon, 8. / 9.,
+                     kind == M_QG, d->Rd, d->precision != 0, s);
+}
+
+// invert_vorticity (core/operators.py:421-498), up to (not including) the
+// psi*mskp + orthogradient pass, which the caller fuses with RK updates
+int Model::invert(double *xs, const char *who, bool full, cudaStream_t s, double *) {
+    double *w = plane(xs, who), *psi = plane(xs, "psi");
+    TRY(launch_celltocorner(w, B, mv, nv, s));
+    if (!full) return two_vcycle(gmg, psi, B, s);
+    TRY(solve(gmg, psi, B, 4, 1e-11, s));
+    if (desc.perio) {
+        // psi -= sum(psi[interior])/area (core/operators.py:474-477), an unmasked sum
+        TRY(launch_reduce(2, ones, psi, nullptr, NH, mv, nv, gmg.sums + 2, gmg.work, s));
+        TRY(vec_axpy_const(psi, area, gmg.sums + 2, pl, s));
+    }
+    return OK;
+}
+
+static OrthoStage ortho_base(Model &M, double *xs) {
+    OrthoStage o;
+    memset(&o, 0, sizeof(o));
+    o.msk = M.msk;
+    o.mskp = M.mskp;
+    o.psi = M.plane(xs, "psi");
+    o.u = M.plane(xs, "u");
+    o.v = M.plane(xs, "v");
+    o.zdx = 1. / M.dx;
+    o.zdy = 1. / M.dy;
+    o.dt = M.dt;
+    o.mv = M.mv;
+    o.nv = M.nv;
+    return o;
+}
+
+static AdvStage adv_base(Model &M, const double *xs, const char *tracer, double *dq) {
+    AdvStage a;
+    memset(&a, 0, sizeof(a));
+    a.msk = M.msk;
+    a.q = M.plane((double *)xs, tracer);
+    a.u = M.plane((double *)xs, "u");
+    a.v = M.plane((double *)xs, "v");
+    a.advc = M.advc;
+    a.dq = M.plane(dq, tracer);
+    a.dt = M.dt;
+    a.kind = (M.desc.order % 2 == 0) ? 1 : 0;
+    a.method = M.desc.flux_method;
+    a.order = M.desc.order;
+    a.mv = M.mv;
+    a.nv = M.nv;
+    return a;
+}
+
+// One RK3_SSP stage k (core/timescheme.py:167-180): rhs(x_k, dx_k) with the
+// next stage state (k = 0: S1, k = 1: S2) or the final update (k = 2)
+// written by the kernels that produce the tendencies.
+int Model::stage(int k, cudaStream_t s) {
+    double *xs = k == 0 ? X : (k == 1 ? S1 : S2);
+    double *dk = D[k];
+    double *out = k == 0 ? S1 : (k == 1 ? S2 : X);
+    const int rk = k + 1;
+    const char *tracers[2] = {kind == M_QG ? "pv" : "vorticity", "buoyancy"};
+    const int ntr = kind == M_BOUSSINESQ ? 2 : 1;
+    for (int t = 0; t < ntr; t++) {
+        AdvStage a = adv_base(*this, xs, tracers[t], dk);
+        if (kind == M_BOUSSINESQ && t == 0) {  // rhs_torque (core/operators.py:303-314)
+            a.buoy = plane(xs, "buoyancy");
+            a.torque_coef = 0.5 * desc.gravity / dx;
+        }
+        a.rk = rk;
+        a.base = plane(X, tracers[t]);
+        a.d0 = k >= 1 ? plane(D[0], tracers[t]) : nullptr;
+        a.d1 = k >= 2 ? plane(D[1], tracers[t]) : nullptr;
+        a.out = plane(out, tracers[t]);
+        TRY(stage_advection(a, s));
+    }
+    // Euler and QG do not invert at the forcing stage (kforcing = 2,
+    // core/euler.py:156-169, core/quasigeostrophic.py:160-168); Boussinesq
+    // inverts at every stage (core/boussinesq.py:114)
+    const bool inv = (kind == M_BOUSSINESQ) || k < 2;
+    if (!inv) return OK;
+    if (kind == M_QG) {
+        // dxdt[:] = 0 then dxdt[pvanom] = dxdt[pv]: the warm start is zero
+        TRY(cuda_status(cudaMemsetAsync(plane(dk, "psi"), 0, pl * 8, s), "qg warm start"));
+        TRY(invert(dk, "pv", false, s));
+    } else {
+        TRY(invert(dk, "vorticity", false, s));
+    }
+    OrthoStage o = ortho_base(*this, dk);
+    o.rk = rk;
+    o.ubase = plane(X, "u");
+    o.vbase = plane(X, "v");
+    o.u0 = k >= 1 ? plane(D[0], "u") : nullptr;
+    o.v0 = k >= 1 ? plane(D[0], "v") : nullptr;
+    o.u1 = k >= 2 ? plane(D[1], "u") : nullptr;
+    o.v1 = k >= 2 ? plane(D[1], "v") : nullptr;
+    o.uout = plane(out, "u");
+    o.vout = plane(out, "v");
+    if (kind != M_BOUSSINESQ && k == 1) {
+        // x[psi] += (dt/6)*(dx0 + dx1 + 4*0): the last stage leaves dx2[psi] = 0
+        o.psi_rk = 1;
+        o.psibase = plane(X, "psi");
+        o.psi0 = plane(D[0], "psi");
+        o.psi1 = nullptr;
+        o.psiout = plane(X, "psi");
+    } else if (kind == M_BOUSSINESQ && k == 2) {
+        o.psi_rk = 1;
+        o.psibase = plane(X, "psi");
+        o.psi0 = plane(D[0], "psi");
+        o.psi1 = plane(D[1], "psi");
+        o.psiout = plane(X, "psi");
+    }
+    if (kind != M_BOUSSINESQ && k == 2) o.rk = 0;
+    return stage_ortho(o, s);
+}
+
+int Model::set_psi(cudaStream_t s) {
+    if (kind == M_QG) {
+        k_qg_post<<<blocks_for(pl), 256, 0, s>>>(X, pl, pvback, 0., 0);  // pvanom = pv - pvback
+        TRY(launch_status("pvanom"));
+        TRY(invert(X, "pvanom", true, s));
+    } else {
+        TRY(invert(X, "vorticity", true, s));
+    }
+    OrthoStage o = ortho_base(*this, X);
+    return stage_ortho(o, s);
+}
+
+int Model::diagnostics(cudaStream_t s) {
+    DiagArgs a;
+    a.kind = kind;
+    a.msk = msk;
+    a.s = X;
+    a.pl = pl;
+    a.mv = mv;
+    a.nv = nv;
+    a.dx = dx;
+    a.dy = dy;
+    a.gravity = desc.gravity;
+    a.Rd = desc.Rd;
+    a.area = area;
+    a.part = part;
+    a.out = diag;
+    int rows = mv - 2 * NH;
+    int nb = reduce_blocks(rows);
+    int rpb = (rows + nb - 1) / nb;
+    nb = (rows + rpb - 1) / rpb;
+    k_diag_partial<<<nb, RED_THREADS, 0, s>>>(a, rpb);
+    k_diag_final<<<1, RED_THREADS, 0, s>>>(a, nb);
+    return launch_status("diagnostics");
+}
+
+// Fluid2d.loop body (core/fluid2d.py:237-268): set_dt, model.step, diagnostics
+int Model::step(cudaStream_t s) {
+    gmg.nprobe = 0;
+    k_set_dt<<<1, 1, 0, s>>>(dt, cst, (SplitConst *)advc, diag, desc.adaptable_dt, desc.dt,
+                             desc.cfl, dx < dy ? dx : dy, desc.dtmax);
+    TRY(launch_status("set_dt"));
+    for (int k = 0; k < 3; k++) TRY(stage(k, s));
+    if (kind == M_BOUSSINESQ) {
+        k_banom<<<blocks_for(pl), 256, 0, s>>>(X, pl, bref);
+        TRY(launch_status("banom"));
+    } else {
+        TRY(set_psi(s));
+        if (kind == M_QG) {
+            k_qg_post<<<blocks_for(pl), 256, 0, s>>>(X, pl, pvback, std::pow(desc.Rd, -2.0), 1);
+            TRY(launch_status("qg post"));
+        }
+    }
+    return diagnostics(s);
+}
+
+}  // namespace f2d
+
+using namespace f2d;
+
+extern "C" {
+
+int f2d_model_create(const f2d_model_desc *d, const int8_t *msk_host, void **model) {
+    if (!d || !msk_host || !model) {
+        set_error("f2d_model_create: null argument");
+        return ERR_ARG;
+    }
+    if (d->nx < 3 || d->ny < 3 || d->Lx <= 0 || d->Ly <= 0) {
+        set_error("f2d_model_create: bad grid %dx%d", d->nx, d->ny);
+        return ERR_SHAPE;
+    }
+    Model *M = new (std::nothrow) Model();
+    if (!M) return ERR_CUDA;
+    cudaStream_t s = nullptr;
+    int st = M->create(d, msk_host, s);
+    if (!st) st = cuda_status(cudaStreamSynchronize(s), "model setup");
+    if (st) {
+        delete M;
+        return st;
+    }
+    *model = M;
+    return OK;
+}
+
+int f2d_model_destroy(void *model) {
+    Model *M = (Model *)model;
+    if (!M) return OK;
+    if (M->gexec) cudaGraphExecDestroy(M->gexec);
+    if (M->graph) cudaGraphDestroy(M->graph);
+    delete M;
+    return OK;
+}
+
+int f2d_model_info(void *model, int *nvar, int *mv, int *nv, int *nlev, int *coarse_level,
+                   double **state, double **diag) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    if (nvar) *nvar = M->nvar;
+    if (mv) *mv = M->mv;
+    if (nv) *nv = M->nv;
+    if (nlev) *nlev = M->gmg.nlev;
+    if (coarse_level) *coarse_level = M->gmg.cs;
+    if (state) *state = M->X;
+    if (diag) *diag = M->diag;
+    return OK;
+}
+
+const char *f2d_model_varname(void *model, int k) {
+    Model *M = (Model *)model;
+    if (!M || k < 0 || k >= M->nvar) return nullptr;
+    return VARNAMES[M->kind][k];
+}
+
+const char *f2d_model_diagname(void *model, int k) {
+    Model *M = (Model *)model;
+    if (!M || k < 0 || k >= NDIAG[M->kind]) return nullptr;
+    return DIAGNAMES[M->kind][k];
+}
+
+double *f2d_model_buffer(void *model, const char *which) {
+    Model *M = (Model *)model;
+    if (!M || !which) return nullptr;
+    if (!strcmp(which, "state")) return M->X;
+    if (!strcmp(which, "dx0")) return M->D[0];
+    if (!strcmp(which, "dx1")) return M->D[1];
+    if (!strcmp(which, "dx2")) return M->D[2];
+    if (!strcmp(which, "cst")) return M->cst;
+    if (!strcmp(which, "dt")) return M->dt;
+    if (!strcmp(which, "diag")) return M->diag;
+    if (!strcmp(which, "work")) return M->B;
+    return nullptr;
+}
+
+int f2d_model_set_psi(void *model, void *stream) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    return M->set_psi((cudaStream_t)stream);
+}
+
+int f2d_model_diagnostics(void *model, void *stream) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    return M->diagnostics((cudaStream_t)stream);
+}
+
+int f2d_model_step(void *model, int nsteps, void *stream) {
+    Model *M = (Model *)model;
+    if (!M || nsteps < 0) return ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int k = 0; k < nsteps; k++) TRY(M->step(s));
+    return OK;
+}
+
+int f2d_model_set_dt(void *model, double dt) {
+    Model *M = (Model *)model;
+    if (!M || !(dt > 0)) return ERR_ARG;
+    M->desc.dt = dt;
+    if (M->gexec) {  // the captured step bakes dt in: capture again
+        cudaGraphExecDestroy(M->gexec);
+        cudaGraphDestroy(M->graph);
+        M->gexec = nullptr;
+        M->graph = nullptr;
+    }
+    return OK;
+}
+
+// Capture one step in a CUDA graph (on `stream`, which must not be the
+// legacy default stream) and replay it nsteps times.
+int f2d_model_step_graph(void *model, int nsteps, void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || nsteps < 0 || !s) {
+        set_error("f2d_model_step_graph: needs a model and a non-default stream");
+        return ERR_ARG;
+    }
+    if (!M->gexec) {
+        TRY(cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                        "begin capture"));
+        int st = M->step(s);
+        cudaGraph_t g = nullptr;
+        int st2 = cuda_status(cudaStreamEndCapture(s, &g), "end capture");
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        TRY(st2);
+        M->graph = g;
+        TRY(cuda_status(cudaGraphInstantiate(&M->gexec, g, 0), "graph instantiate"));
+    }
+    for (int k = 0; k < nsteps; k++) TRY(cuda_status(cudaGraphLaunch(M->gexec, s), "graph launch"));
+    return OK;
+}
+
+// Finest-level smoother probe: enable (resets the count; a captured graph is
+// dropped so that the next capture records the probe events), or read the
+// average duration (ms) of the probed smooth calls of the last step.
+int f2d_model_probe(void *model, int enable, int *count, double *avg_ms) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    if (enable >= 0) {
+        M->gmg.probe = enable != 0;
+        M->gmg.nprobe = 0;
+        M->probe_per_step = -1;
+        if (M->gexec) {
+            cudaGraphExecDestroy(M->gexec);
+            cudaGraphDestroy(M->graph);
+            M->gexec = nullptr;
+            M->graph = nullptr;
+        }
+        return OK;
+    }
+    int n = M->gmg.nprobe;
+    double tot = 0.;
+    for (int k = 0; k < n; k++) {
+        float ms = 0.f;
+        TRY(cuda_status(cudaEventElapsedTime(&ms, M->gmg.ev[k][0], M->gmg.ev[k][1]), "probe time"));
+        tot += ms;
+    }
+    if (count) *count = n;
+    if (avg_ms) *avg_ms = n ? tot / n : 0.;
+    return OK;
+}
+
+// kernel nodes of the captured step graph (0 before the first capture)
+int f2d_model_graph_kernels(void *model, int *nkernels) {
+    Model *M = (Model *)model;
+    if (!M || !nkernels) return ERR_ARG;
+    *nkernels = 0;
+    if (!M->graph) return OK;
+    size_t n = 0;
+    TRY(cuda_status(cudaGraphGetNodes(M->graph, nullptr, &n), "graph nodes"));
+    std::vector<cudaGraphNode_t> nodes(n);
+    TRY(cuda_status(cudaGraphGetNodes(M->graph, nodes.data(), &n), "graph nodes"));
+    int k = 0;
+    for (size_t q = 0; q < n; q++) {
+        cudaGraphNodeType t;
+        TRY(cuda_status(cudaGraphNodeGetType(nodes[q], &t), "node type"));
+        if (t == cudaGraphNodeTypeKernel) k++;
+    }
+    *nkernels = k;
+    return OK;
+}
+
+int f2d_model_solve_stats(void *model, int *nite, double *res, int *status) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    SolveState st;
+    TRY(cuda_status(cudaMemcpy(&st, M->gmg.solve_state, sizeof(st), cudaMemcpyDeviceToHost),
+                    "solve stats"));
+    if (nite) *nite = st.nite;
+    if (res) *res = st.res;
+    if (status) *status = st.status;
+    return OK;
+}
+
+// ---- multigrid on caller arrays (core/gmg/hierarchy.py:154-218)
+int f2d_gmg_create(const int8_t *mskp_host, int nx, int ny, double dx, double dy,
+                   double hydroepsilon, int qg, double Rd, void **gmg) {
+    if (!mskp_host || !gmg || nx < 3 || ny < 3) {
+        set_error("f2d_gmg_create: bad argument");
+        return ERR_ARG;
+    }
+    Gmg *G = new (std::nothrow) Gmg();
+    if (!G) return ERR_CUDA;
+    int st = G->setup(mskp_host, nx, ny, dx, dy, qg ? 1. : hydroepsilon, 8. / 9., qg != 0, Rd,
+                      false, nullptr);
+    if (!st) st = cuda_status(cudaDeviceSynchronize(), "gmg setup");
+    if (st) {
+        delete G;
+        return st;
+    }
+    *gmg = G;
+    return OK;
+}
+
+int f2d_gmg_destroy(void *gmg) {
+    delete (Gmg *)gmg;
+    return OK;
+}
+
+int f2d_gmg_levels(void *gmg, int *nlev, int *mv, int *nv, int *coarse_level) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G) return ERR_ARG;
+    if (nlev) *nlev = G->nlev;
+    for (int l = 0; l < G->nlev; l++) {
+        if (mv) mv[l] = G->mv[l];
+        if (nv) nv[l] = G->nv[l];
+    }
+    if (coarse_level) *coarse_level = G->cs;
+    return OK;
+}
+
+int f2d_gmg_twovcycle(void *gmg, double *x, const double *b, void *stream) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G || !x || !b) return ERR_ARG;
+    return two_vcycle(*G, x, b, (cudaStream_t)stream);
+}
+
+int f2d_gmg_solve(void *gmg, double *x, const double *b, int maxite, double tol, void *stream) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G || !x || !b || maxite < 0) return ERR_ARG;
+    return solve(*G, x, b, maxite, tol, (cudaStream_t)stream);
+}
+
+int f2d_gmg_solve_stats(void *gmg, int *nite, double *res, int *status) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G) return ERR_ARG;
+    SolveState st;
+    TRY(cuda_status(cudaMemcpy(&st, G->solve_state, sizeof(st), cudaMemcpyDeviceToHost),
+                    "solve stats"));
+    if (nite) *nite = st.nite;
+    if (res) *res = st.res;
+    if (status) *status = st.status;
+    return OK;
+}
+
+// level data: which = "msk" (int8), "A" (6 planes), "x", "b", "r"
+void *f2d_gmg_level_ptr(void *gmg, int lev, const char *which) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G || lev < 0 || lev >= G->nlev || !which) return nullptr;
+    LevelView<double> &L = G->d[lev];
+    if (!strcmp(which, "msk")) return (void *)L.msk;
+    if (!strcmp(which, "A")) return (void *)L.A;
+    if (!strcmp(which, "x")) return L.x;
+    if (!strcmp(which, "b")) return L.b;
+    if (!strcmp(which, "r")) return L.r;
+    return nullptr;
+}
+
+int f2d_gmg_vcycle(void *gmg, int lev1, void *stream) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G || lev1 < 0 || lev1 >= G->nlev) return ERR_ARG;
+    return G->vcycle(G->d, lev1, false, nullptr, (cudaStream_t)stream);
+}
+
+int f2d_gmg_fcycle(void *gmg, int lev1, void *stream) {
+    Gmg *G = (Gmg *)gmg;
+    if (!G || lev1 < 0 || lev1 >= G->nlev) return ERR_ARG;
+    return G->fcycle(G->d, lev1, nullptr, (cudaStream_t)stream);
+}
+
+}  // extern "C"

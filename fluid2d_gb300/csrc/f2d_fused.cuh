@@ -1,0 +1,114 @@
+// f2d_fused.cuh -- device views and launchers of the engine kernels
+// (multigrid levels, single-CTA coarse solve, fused stage kernels).
+#pragma once
+#include "f2d_common.cuh"
+
+namespace f2d {
+
+constexpr int NH = 3;           // halo width (the reference requires 3)
+constexpr int MAX_LEVELS = 24;  // core/gmg/level.py:112-115 aborts beyond 20
+
+// One multigrid level on the device.  Arrays are (mv, nv) row-major with
+// the 3-cell halo.  A holds 6 planes: A1..A5 (SW, S, SE, W, C of the
+// symmetric 9-point operator, core/gmg/level.py:332-335) and C3 = omega/|A5|
+// (precomputed: the smoother's per-point division of
+// core/gmg/fortran_multigrid.f90:67,103, same value).  The finest level has
+// no stored A: its operator is analytic in the mask (core/gmg/level.py:261-302).
+template <typename T>
+struct LevelView {
+    int mv, nv;
+    const int8_t *msk;
+    const T *A;
+    T *x, *b, *r, *t;
+};
+
+// Analytic finest-level operator: A_k(J,I) = sc[k] where msk(J',I') and
+// msk(J'+dj_k, I'+di_k) are fluid, (J',I') the periodic image of (J,I)
+// (the reference fills the halo of A periodically, core/gmg/level.py:297).
+struct Analytic {
+    double sc[5];  // stencil*coef of planes SW, S, SE, W, C
+    double a5;     // A5 on fluid points, after the Helmholtz shift (QG)
+    double c3;     // omega / |a5|
+};
+
+enum CycleMode { CYCLE_V = 0, CYCLE_F = 1 };
+
+template <typename T>
+struct CoarseArgs {
+    int nlev;                    // levels in the CTA: [0, nlev) of lev[]
+    LevelView<T> lev[MAX_LEVELS];
+    T c1, c2;                    // omega, 1 - omega
+    int mode;                    // CYCLE_V or CYCLE_F, started at lev[0]
+    int zero_first;              // V-cycle: the first level starts from x = 0
+    int ndeepest;                // smoothing calls on the coarsest level
+    const int *active;           // skip everything when *active == 0
+};
+
+// launchers (kernels_fused.cu)
+template <typename T>
+int mg_sweep1(const LevelView<T> &L, const Analytic *an, T c1, T c2, bool zero_x,
+              const int *active, cudaStream_t s);
+template <typename T>
+int mg_sweep2(const LevelView<T> &L, const Analytic *an, T c1, T c2, const int *active,
+              cudaStream_t s);
+template <typename T>
+int mg_residual(const LevelView<T> &L, const Analytic *an, const T *x, const T *b, T *r,
+                const int *active, cudaStream_t s);
+template <typename T>
+int mg_restrict(const LevelView<T> &fine, const T *src, const LevelView<T> &coarse, T *dst,
+                const int *active, cudaStream_t s);
+template <typename T>
+int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine, T *dst,
+              bool assign, const int *active, cudaStream_t s);
+template <typename T>
+int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s);
+template <typename T>
+size_t coarse_smem_bytes(const int *mv, const int *nv, int nlev);
+
+// stage kernels (kernels_fused.cu), float64 state
+struct AdvStage {
+    const int8_t *msk;
+    const double *q;          // advected tracer (stage state)
+    const double *u, *v;      // stage velocities
+    const double *advc;       // device SplitConst derived from cst (written by set_dt)
+    double *dq;               // tendency out (interior + periodic halo)
+    // torque (Boussinesq, core/operators.py:303-314): dq = dq*msk + g db/dx
+    const double *buoy;       // null: no torque
+    double torque_coef;       // 0.5*gravity/dx
+    // RK combination written in the same pass: out = base + c*(sum of tendencies)
+    int rk;                   // 0 none, 1: out = base + dt*dq, 2: out = base + (dt/4)(d0+dq),
+                              // 3: out = base + (dt/6)(d0 + d1 + 4 dq)
+    const double *base, *d0, *d1;
+    double *out;
+    const double *dt;         // device scalar
+    int kind, method, order;  // flux kind (0 upwind, 1 centred), splitting, order
+    int mv, nv;
+};
+int stage_advection(const AdvStage &a, cudaStream_t s);
+
+struct OrthoStage {
+    const int8_t *msk, *mskp;
+    double *psi;                 // in/out: psi <- psi*mskp (whole array)
+    double *u, *v;               // out: rows/cols 1..m-2
+    double zdx, zdy;
+    // RK combination of the velocities (rows/cols 1..m-2), as AdvStage::rk,
+    // with the current u, v as the newest tendency
+    int rk;
+    const double *ubase, *vbase, *u0, *v0, *u1, *v1;
+    double *uout, *vout;
+    // psi_rk != 0: psiout = psibase + (dt/6)*(psi0 + psi1 + 4*psi2) over the
+    // whole array; psi1 == null means the current psi is dx1 and dx2 = 0
+    // (Euler, whose last stage does not invert), else the current psi is dx2
+    int psi_rk;
+    const double *psibase, *psi0, *psi1;
+    double *psiout;
+    const double *dt;
+    int mv, nv;
+};
+int stage_ortho(const OrthoStage &a, cudaStream_t s);
+
+int vec_add(double *x, const double *y, size_t count, const int *active, cudaStream_t s);
+int vec_axpy_const(double *x, double alpha_sub, const double *dev_scalar, size_t count,
+                   cudaStream_t s);
+
+}  // namespace f2d

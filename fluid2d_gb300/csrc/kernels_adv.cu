@@ -15,114 +15,9 @@
 // evaluated 1 + 1/32 (x) or 1 + 1/8 (y) times instead of twice.
 #include "f2d_common.cuh"
 #include "f2d_kernels.cuh"
+#include "f2d_adv.cuh"
 
 namespace f2d {
-
-// Flux-splitting constants derived from cst = [dx, dy, logcosh, umax, aparab]
-// exactly as core/fortran_advection.f90:46-60 derives them.
-struct SplitConst {
-    double zdx, zdy, a, KK, u1, aa, bb;
-};
-
-F2D_DEV SplitConst split_const(const double *cst) {
-    SplitConst c;
-    double dx = cst[0], dy = cst[1], logcosh = cst[2], umax = cst[3], aparab = cst[4];
-    c.zdx = 1. / dx;
-    c.zdy = 1. / dy;
-    c.a = logcosh / umax;
-    c.KK = (umax - log(cosh(umax * c.a)) / c.a) * 0.5;
-    c.u1 = aparab * umax;
-    c.aa = 1. / (2. * c.u1);
-    c.bb = c.u1 * 0.5;
-    return c;
-}
-
-// |U| of the flux splitting (core/fortran_advection.f90:77-83)
-F2D_DEV double split_speed(double uu, int method, const SplitConst &c) {
-    double UU = 0.;
-    if (method == 0) UU = fabs(uu);
-    if (method == 1) {
-        UU = fabs(uu);
-        if (UU < c.u1) UU = c.aa * (uu * uu) + c.bb;
-    }
-    if (method == 2) UU = 2 * c.KK + log(cosh(uu * c.a)) / c.a;
-    return UU;
-}
-
-// Upwind edge flux between cells p0 and p1 along a line with stride s;
-// q[k] = x at p0 + (k-2)*s for k = 0..5 (cells p0-2 .. p0+3), mk likewise.
-// core/fortran_advection.f90:72-111 (x) and :113-146 (y).
-F2D_DEV double upwind_flux(const double *q, const int *mk, double vel, int method,
-                           int order, const SplitConst &c) {
-    if (mk[2] + mk[3] != 2) return 0.;
-    const double d1 = r4(1.f / 30.f), d2 = r4(-13.f / 60.f), d3 = r4(47.f / 60.f),
-                 d4 = r4(9.f / 20.f), d5 = r4(-1.f / 20.f);
-    const double c1 = r4(-1.f / 6.f), c2 = r4(5.f / 6.f), c3 = r4(2.f / 6.f);
-    double UU = split_speed(vel, method, c);
-    double up = 0.5 * (vel + UU);
-    double um = 0.5 * (vel - UU);
-    int m5p = mk[0] + mk[1] + mk[2] + mk[3] + mk[4];
-    int m3p = mk[1] + mk[2] + mk[3];
-    int m5m = mk[1] + mk[2] + mk[3] + mk[4] + mk[5];
-    int m3m = mk[2] + mk[3] + mk[4];
-    double qp, qm;
-    if (m5p == 5 && order == 5)
-        qp = d1 * q[0] + d2 * q[1] + d3 * q[2] + d4 * q[3] + d5 * q[4];
-    else if (m3p == 3 && order >= 3)
-        qp = c1 * q[1] + c2 * q[2] + c3 * q[3];
-    else
-        qp = q[2];
-    if (m5m == 5 && order == 5)
-        qm = d5 * q[1] + d4 * q[2] + d3 * q[3] + d2 * q[4] + d1 * q[5];
-    else if (m3m == 3 && order >= 3)
-        qm = c3 * q[2] + c2 * q[3] + c1 * q[4];
-    else
-        qm = q[3];
-    return up * qp + um * qm;
-}
-
-// Centred edge flux (orders 2/4/6), core/fortran_advection.f90:228-262;
-// the fortran_fluxes copy (core/fortran_fluxes.f90:225-258) has no 6th
-// order branch (allow6 = false).
-F2D_DEV double centered_flux(const double *q, const int *mk, double vel, int order,
-                             bool allow6) {
-    int m2 = mk[2] + mk[3];
-    if (m2 != 2) return 0.;
-    const double e1 = r4(1.f / 60.f), e2 = r4(-2.f / 15.f), e3 = r4(37.f / 60.f);
-    const double d1 = r4(-1.f / 12.f), d2 = r4(7.f / 12.f);
-    const double c1 = r4(1.f / 2.f);
-    int m6 = mk[0] + mk[1] + mk[2] + mk[3] + mk[4] + mk[5];
-    int m4 = mk[1] + mk[2] + mk[3] + mk[4];
-    double qp = 0.;
-    if (allow6 && m6 == 6 && order == 6) {
-        qp = e1 * (q[0] + q[5]) + e2 * (q[1] + q[4]);
-        qp = qp + e3 * (q[2] + q[3]);
-    } else if (m4 == 4 && order == 4) {
-        qp = d1 * (q[1] + q[4]) + d2 * (q[2] + q[3]);
-    } else if (m2 == 2 && order >= 2) {
-        qp = c1 * (q[2] + q[3]);
-    }
-    return vel * qp;
-}
-
-template <int KIND>  // 0 upwind, 1 centred (advection), 2 centred (fluxes copy)
-F2D_DEV double edge_flux(const int8_t *msk, const double *x, const double *vel,
-                         size_t p0, ptrdiff_t s, int method, int order,
-                         const SplitConst &c) {
-    double q[6];
-    int mk[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        ptrdiff_t o = (ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s;
-        mk[k] = msk[o];
-    }
-    if (mk[2] + mk[3] != 2) return 0.;
-#pragma unroll
-    for (int k = 0; k < 6; k++) q[k] = __ldg(x + (ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s);
-    double w = __ldg(vel + p0);
-    if (KIND == 0) return upwind_flux(q, mk, w, method, order, c);
-    return centered_flux(q, mk, w, order, KIND == 1);
-}
 
 constexpr int ADV_TX = 32, ADV_TY = 8;
 
@@ -139,8 +34,12 @@ k_advection(const int8_t *__restrict__ msk, const double *__restrict__ x,
             int nh, int method, int order, int m, int n) {
     __shared__ double sfx[ADV_TY][ADV_TX + 1];
     __shared__ double sfy[ADV_TY + 1][ADV_TX];
-    const SplitConst c = split_const(cst);
+    __shared__ SplitConst sc;
     const int tx = threadIdx.x, ty = threadIdx.y;
+    // the constants (two divisions, log, cosh) once per CTA
+    if (tx == 0 && ty == 0) sc = split_const(cst);
+    __syncthreads();
+    const SplitConst c = sc;
     const int I = nh + blockIdx.x * ADV_TX + tx;
     const int J = nh + blockIdx.y * ADV_TY + ty;
     const bool in = (I <= n - nh - 1) && (J <= m - nh - 1);

@@ -1,0 +1,582 @@
+// kernels_fused.cu -- engine kernels: multigrid levels, the single-CTA
+// coarse solve, and the fused stage kernels of the time step.
+//
+// Multigrid semantics follow core/gmg/hierarchy.py:98-151 over the routines
+// of core/gmg/fortran_multigrid.f90, with every halo fill
+// (core/gmg/halo.py:136-141) folded into the kernel that produces the
+// interior: a thread that computes an interior value also writes it to the
+// halo cells that are its periodic images.  Only the cells each reference
+// routine's output depends on are computed:
+//   smooth   = sweep 1 on rows/cols 2..m-3 (0-based) into t, sweep 2 on the
+//              interior into x, x's halo = periodic images
+//              (the Fortran's edge write-backs all land in the halo, which
+//              the fill that follows overwrites);
+//   residual = interior + periodic halo;
+//   restrict = coarse interior + periodic halo;
+//   interpolate + (x += r) = fine rows/cols 1..m-2 (what the next smooth
+//              reads), so the correction array r is never stored.
+#include "f2d_common.cuh"
+#include "f2d_fused.cuh"
+#include "f2d_kernels.cuh"
+#include "f2d_adv.cuh"
+
+namespace f2d {
+
+// ------------------------------------------------------------ point math
+__constant__ int c_dj[5] = {-1, -1, -1, 0, 0};
+__constant__ int c_di[5] = {-1, 0, 1, -1, 0};
+
+template <typename T>
+F2D_DEV T analytic_coef(const LevelView<T> &L, const Analytic &an, int k, int J, int I) {
+    const int Jw = wrap(J, L.mv, NH), Iw = wrap(I, L.nv, NH);
+    const size_t pc = off(Jw, Iw, L.nv);
+    if (L.msk[pc] == 0) return (T)0;
+    if (L.msk[off(Jw + c_dj[k], Iw + c_di[k], L.nv)] == 0) return (T)0;
+    return (T)(k == 4 ? an.a5 : an.sc[k]);
+}
+
+// the 8 off-diagonal coefficients of point (j, i) in the reference's order
+// A1(j,i) A2(j,i) A3(j,i) A4(j,i) A4(j,i+1) A3(j+1,i-1) A2(j+1,i) A1(j+1,i+1)
+template <typename T, bool L0>
+F2D_DEV void offdiag(const LevelView<T> &L, const Analytic *an, int j, int i, T (&a)[8]) {
+    if (L0) {
+        a[0] = analytic_coef(L, *an, 0, j, i);
+        a[1] = analytic_coef(L, *an, 1, j, i);
+        a[2] = analytic_coef(L, *an, 2, j, i);
+        a[3] = analytic_coef(L, *an, 3, j, i);
+        a[4] = analytic_coef(L, *an, 3, j, i + 1);
+        a[5] = analytic_coef(L, *an, 2, j + 1, i - 1);
+        a[6] = analytic_coef(L, *an, 1, j + 1, i);
+        a[7] = analytic_coef(L, *an, 0, j + 1, i + 1);
+    } else {
+        const size_t pl = (size_t)L.mv * L.nv, p = off(j, i, L.nv);
+        const int nv = L.nv;
+        const T *A1 = L.A, *A2 = L.A + pl, *A3 = L.A + 2 * pl, *A4 = L.A + 3 * pl;
+        a[0] = A1[p];
+        a[1] = A2[p];
+        a[2] = A3[p];
+        a[3] = A4[p];
+        a[4] = A4[p + 1];
+        a[5] = A3[p + nv - 1];
+        a[6] = A2[p + nv];
+        a[7] = A1[p + nv + 1];
+    }
+}
+
+template <typename T, bool L0>
+F2D_DEV T diag_coef(const LevelView<T> &L, const Analytic *an, int j, int i) {
+    if (L0) return analytic_coef(L, *an, 4, j, i);
+    return L.A[4 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
+}
+
+template <typename T, bool L0>
+F2D_DEV T c3_coef(const LevelView<T> &L, const Analytic *an, int j, int i, T c1) {
+    if (L0) {
+        T a5 = analytic_coef(L, *an, 4, j, i);
+        return a5 != (T)0 ? (T)an->c3 : c1 / fabs(a5);
+    }
+    return L.A[5 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
+}
+
+// damped Jacobi (core/gmg/fortran_multigrid.f90:66-85); q == null: x = 0
+template <typename T, bool L0>
+F2D_DEV T jacobi(const LevelView<T> &L, const Analytic *an, const T *q, const T *b, int j,
+                 int i, T c1, T c2) {
+    const int nv = L.nv;
+    const size_t p = off(j, i, nv);
+    if (L.msk[p] == 0) return (T)0;
+    const T c3 = c3_coef<T, L0>(L, an, j, i, c1);
+    if (q == nullptr) return c3 * (-b[p]);
+    T a[8];
+    offdiag<T, L0>(L, an, j, i, a);
+    return q[p] * c2 + c3 * (+a[0] * q[p - nv - 1]
+                             + a[1] * q[p - nv]
+                             + a[2] * q[p - nv + 1]
+                             + a[3] * q[p - 1]
+                             + a[4] * q[p + 1]
+                             + a[5] * q[p + nv - 1]
+                             + a[6] * q[p + nv]
+                             + a[7] * q[p + nv + 1]
+                             - b[p]);
+}
+
+// r = b - A x (core/gmg/fortran_multigrid.f90:340-357)
+template <typename T, bool L0>
+F2D_DEV T residual(const LevelView<T> &L, const Analytic *an, const T *x, const T *b, int j,
+                   int i) {
+    const int nv = L.nv;
+    const size_t p = off(j, i, nv);
+    if (L.msk[p] == 0) return (T)0;
+    T a[8];
+    offdiag<T, L0>(L, an, j, i, a);
+    const T a5 = diag_coef<T, L0>(L, an, j, i);
+    return b[p]
+        - a[0] * x[p - nv - 1]
+        - a[1] * x[p - nv]
+        - a[2] * x[p - nv + 1]
+        - a[3] * x[p - 1]
+        - a5 * x[p]
+        - a[4] * x[p + 1]
+        - a[5] * x[p + nv - 1]
+        - a[6] * x[p + nv]
+        - a[7] * x[p + nv + 1];
+}
+
+// full weighting around fine (2*J2-2, 2*I2-2) (core/gmg/fortran_multigrid.f90:531-537)
+template <typename T>
+F2D_DEV T restrict_value(const int8_t *msk2, int nv2, const T *r, int nv1, int J2, int I2) {
+    if (msk2[off(J2, I2, nv2)] == 0) return (T)0;
+    const size_t c = off(2 * J2 - 2, 2 * I2 - 2, nv1);
+    return (T)0.25 * r[c]
+        + (T)0.125 * (r[c - 1] + r[c + 1] + r[c - nv1] + r[c + nv1])
+        + (T)0.0625 * (r[c - nv1 - 1] + r[c - nv1 + 1] + r[c + nv1 - 1] + r[c + nv1 + 1]);
+}
+
+// bilinear prolongation value at fine (J1, I1), nh = 3
+// (core/gmg/fortran_multigrid.f90:449-496)
+template <typename T>
+F2D_DEV T interp_value(const int8_t *msk1, int nv1, const int8_t *msk2, const T *x2, int nv2,
+                       int J1, int I1) {
+    if (msk1[off(J1, I1, nv1)] <= 0) return (T)0;
+    const int J2 = (J1 >> 1) + 1, I2 = (I1 >> 1) + 1;
+    const int dj = J1 & 1, di = I1 & 1;
+    const size_t q = off(J2, I2, nv2);
+    const T c2[3] = {(T)0, (T)1, (T)0.5};
+    if (!dj && !di) return x2[q];
+    if (!dj) return (x2[q] + x2[q + 1]) * c2[msk2[q] + msk2[q + 1]];
+    if (!di) return (x2[q] + x2[q + nv2]) * c2[msk2[q] + msk2[q + nv2]];
+    const T c3[5] = {(T)0, (T)1, (T)0.5, (T)r4(0.3333333333333333333333333333f), (T)0.25};
+    const int s = msk2[q] + msk2[q + 1] + msk2[q + nv2] + msk2[q + nv2 + 1];
+    return c3[s] * (x2[q] + x2[q + 1] + x2[q + nv2] + x2[q + nv2 + 1]);
+}
+
+// store an interior value and its periodic halo images
+// (core/gmg/fortran_multigrid.f90:365-412)
+template <typename T>
+F2D_DEV void store_images(T *a, int J, int I, int mv, int nv, T v) {
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    int rows[3], cols[3], nr = 0, nc = 0;
+    rows[nr++] = J;
+    if (J >= m2 && J < m2 + NH) rows[nr++] = J - m2;
+    if (J >= NH && J < 2 * NH) rows[nr++] = J + m2;
+    cols[nc++] = I;
+    if (I >= n2 && I < n2 + NH) cols[nc++] = I - n2;
+    if (I >= NH && I < 2 * NH) cols[nc++] = I + n2;
+    for (int r = 0; r < nr; r++)
+        for (int c = 0; c < nc; c++) a[off(rows[r], cols[c], nv)] = v;
+}
+
+F2D_DEV bool inactive(const int *active) { return active != nullptr && *active == 0; }
+
+// ------------------------------------------------------------ level kernels
+constexpr int LV_TX = 32, LV_TY = 8;
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(LV_TX *LV_TY)
+k_sweep1(LevelView<T> L, Analytic an, T c1, T c2, int zero_x, const int *active) {
+    if (inactive(active)) return;
+    const int i = 2 + blockIdx.x * LV_TX + threadIdx.x;
+    const int j = 2 + blockIdx.y * LV_TY + threadIdx.y;
+    if (i > L.nv - 3 || j > L.mv - 3) return;
+    L.t[off(j, i, L.nv)] = jacobi<T, L0>(L, &an, zero_x ? nullptr : L.x, L.b, j, i, c1, c2);
+}
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(LV_TX *LV_TY)
+k_sweep2(LevelView<T> L, Analytic an, T c1, T c2, const int *active) {
+    if (inactive(active)) return;
+    const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
+    const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
+    if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
+    T v = jacobi<T, L0>(L, &an, L.t, L.b, j, i, c1, c2);
+    store_images(L.x, j, i, L.mv, L.nv, v);
+}
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(LV_TX *LV_TY)
+k_residual(LevelView<T> L, Analytic an, const T *x, const T *b, T *r, const int *active) {
+    if (inactive(active)) return;
+    const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
+    const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
+    if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
+    store_images(r, j, i, L.mv, L.nv, residual<T, L0>(L, &an, x, b, j, i));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LV_TX *LV_TY)
+k_restrict(const T *src, int nv1, const int8_t *msk2, int mv2, int nv2, T *dst,
+           const int *active) {
+    if (inactive(active)) return;
+    const int I2 = NH + blockIdx.x * LV_TX + threadIdx.x;
+    const int J2 = NH + blockIdx.y * LV_TY + threadIdx.y;
+    if (I2 > nv2 - NH - 1 || J2 > mv2 - NH - 1) return;
+    store_images(dst, J2, I2, mv2, nv2, restrict_value(msk2, nv2, src, nv1, J2, I2));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LV_TX *LV_TY)
+k_interp(const int8_t *msk1, int mv1, int nv1, const int8_t *msk2, const T *x2, int nv2, T *dst,
+         int assign, const int *active) {
+    if (inactive(active)) return;
+    const int I1 = 1 + blockIdx.x * LV_TX + threadIdx.x;
+    const int J1 = 1 + blockIdx.y * LV_TY + threadIdx.y;
+    if (I1 > nv1 - 2 || J1 > mv1 - 2) return;
+    const T v = interp_value(msk1, nv1, msk2, x2, nv2, J1, I1);
+    const size_t p = off(J1, I1, nv1);
+    dst[p] = assign ? v : dst[p] + v;
+}
+
+static inline dim3 lv_grid(int rows, int cols) {
+    return grid2d(rows > 0 ? rows : 1, cols > 0 ? cols : 1, dim3(LV_TX, LV_TY));
+}
+
+template <typename T>
+int mg_sweep1(const LevelView<T> &L, const Analytic *an, T c1, T c2, bool zero_x,
+              const int *active, cudaStream_t s) {
+    dim3 g = lv_grid(L.mv - 4, L.nv - 4), b(LV_TX, LV_TY);
+    if (an)
+        k_sweep1<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, zero_x, active);
+    else
+        k_sweep1<T, false><<<g, b, 0, s>>>(L, Analytic{}, c1, c2, zero_x, active);
+    return launch_status("mg_sweep1");
+}
+
+template <typename T>
+int mg_sweep2(const LevelView<T> &L, const Analytic *an, T c1, T c2, const int *active,
+              cudaStream_t s) {
+    dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), b(LV_TX, LV_TY);
+    if (an)
+        k_sweep2<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, active);
+    else
+        k_sweep2<T, false><<<g, b, 0, s>>>(L, Analytic{}, c1, c2, active);
+    return launch_status("mg_sweep2");
+}
+
+template <typename T>
+int mg_residual(const LevelView<T> &L, const Analytic *an, const T *x, const T *b, T *r,
+                const int *active, cudaStream_t s) {
+    dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
+    if (an)
+        k_residual<T, true><<<g, bl, 0, s>>>(L, *an, x, b, r, active);
+    else
+        k_residual<T, false><<<g, bl, 0, s>>>(L, Analytic{}, x, b, r, active);
+    return launch_status("mg_residual");
+}
+
+template <typename T>
+int mg_restrict(const LevelView<T> &fine, const T *src, const LevelView<T> &coarse, T *dst,
+                const int *active, cudaStream_t s) {
+    dim3 g = lv_grid(coarse.mv - 2 * NH, coarse.nv - 2 * NH), b(LV_TX, LV_TY);
+    k_restrict<T><<<g, b, 0, s>>>(src, fine.nv, coarse.msk, coarse.mv, coarse.nv, dst, active);
+    return launch_status("mg_restrict");
+}
+
+template <typename T>
+int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine, T *dst,
+              bool assign, const int *active, cudaStream_t s) {
+    dim3 g = lv_grid(fine.mv - 2, fine.nv - 2), b(LV_TX, LV_TY);
+    k_interp<T><<<g, b, 0, s>>>(fine.msk, fine.mv, fine.nv, coarse.msk, src, coarse.nv, dst,
+                                assign, active);
+    return launch_status("mg_interp");
+}
+
+// ------------------------------------------------------------ coarse CTA
+// All levels below a size threshold are processed by one CTA out of shared
+// memory: the recursion of core/gmg/hierarchy.py:98-151 runs as a sequence
+// of block-wide phases separated by __syncthreads().
+constexpr int CO_THREADS = 1024;
+
+F2D_HD size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+template <typename T>
+size_t coarse_smem_bytes(const int *mv, const int *nv, int nlev) {
+    size_t tot = 0;
+    for (int l = 0; l < nlev; l++) {
+        size_t pts = (size_t)mv[l] * nv[l];
+        tot += align16(pts) + align16(sizeof(T) * pts * 10);  // msk, A(6), x, b, r, t
+    }
+    return tot;
+}
+
+template <typename T>
+F2D_DEV void co_smooth(const LevelView<T> &L, T c1, T c2, bool zero_x) {
+    const int w1 = L.nv - 4, h1 = L.mv - 4;
+    for (int q = threadIdx.x; q < w1 * h1; q += blockDim.x) {
+        int j = 2 + q / w1, i = 2 + q % w1;
+        L.t[off(j, i, L.nv)] = jacobi<T, false>(L, nullptr, zero_x ? nullptr : L.x, L.b, j, i,
+                                                c1, c2);
+    }
+    __syncthreads();
+    const int w2 = L.nv - 2 * NH, h2 = L.mv - 2 * NH;
+    for (int q = threadIdx.x; q < w2 * h2; q += blockDim.x) {
+        int j = NH + q / w2, i = NH + q % w2;
+        store_images(L.x, j, i, L.mv, L.nv, jacobi<T, false>(L, nullptr, L.t, L.b, j, i, c1, c2));
+    }
+    __syncthreads();
+}
+
+template <typename T>
+F2D_DEV void co_residual(const LevelView<T> &L) {
+    const int w = L.nv - 2 * NH, h = L.mv - 2 * NH;
+    for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
+        int j = NH + q / w, i = NH + q % w;
+        store_images(L.r, j, i, L.mv, L.nv, residual<T, false>(L, nullptr, L.x, L.b, j, i));
+    }
+    __syncthreads();
+}
+
+template <typename T>
+F2D_DEV void co_restrict(const LevelView<T> &F, const T *src, const LevelView<T> &Cl, T *dst) {
+    const int w = Cl.nv - 2 * NH, h = Cl.mv - 2 * NH;
+    for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
+        int j = NH + q / w, i = NH + q % w;
+        store_images(dst, j, i, Cl.mv, Cl.nv, restrict_value(Cl.msk, Cl.nv, src, F.nv, j, i));
+    }
+    __syncthreads();
+}
+
+template <typename T>
+F2D_DEV void co_interp(const LevelView<T> &Cl, const LevelView<T> &F, bool assign) {
+    const int w = F.nv - 2, h = F.mv - 2;
+    for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
+        int j = 1 + q / w, i = 1 + q % w;
+        T v = interp_value(F.msk, F.nv, Cl.msk, Cl.x, Cl.nv, j, i);
+        size_t p = off(j, i, F.nv);
+        F.x[p] = assign ? v : F.x[p] + v;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+F2D_DEV void co_vcycle(const LevelView<T> *lev, int l1, int deep, bool zero_first, T c1, T c2,
+                       int ndeepest) {
+    for (int l = l1; l < deep; l++) {
+        co_smooth(lev[l], c1, c2, zero_first || l > l1);
+        co_residual(lev[l]);
+        co_restrict(lev[l], lev[l].r, lev[l + 1], lev[l + 1].b);
+    }
+    for (int k = 0; k < ndeepest; k++) co_smooth(lev[deep], c1, c2, k == 0);
+    for (int l = deep - 1; l >= l1; l--) {
+        co_interp(lev[l + 1], lev[l], false);
+        co_smooth(lev[l], c1, c2, false);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
+    if (inactive(a.active)) return;
+    extern __shared__ __align__(16) unsigned char sm[];
+    LevelView<T> lev[MAX_LEVELS];
+    size_t o = 0;
+    for (int l = 0; l < a.nlev; l++) {
+        const LevelView<T> &g = a.lev[l];
+        const size_t pts = (size_t)g.mv * g.nv;
+        LevelView<T> s = g;
+        int8_t *msk = (int8_t *)(sm + o);
+        o += align16(pts);
+        T *base = (T *)(sm + o);
+        o += align16(sizeof(T) * pts * 10);
+        s.msk = msk;
+        s.A = base;
+        s.x = base + 6 * pts;
+        s.b = base + 7 * pts;
+        s.r = base + 8 * pts;
+        s.t = base + 9 * pts;
+        for (size_t q = threadIdx.x; q < pts; q += blockDim.x) msk[q] = g.msk[q];
+        for (size_t q = threadIdx.x; q < 6 * pts; q += blockDim.x) ((T *)s.A)[q] = g.A[q];
+        if (l == 0) {
+            for (size_t q = threadIdx.x; q < pts; q += blockDim.x) {
+                s.b[q] = g.b[q];
+                s.x[q] = (a.mode == CYCLE_V && !a.zero_first) ? g.x[q] : (T)0;
+            }
+        }
+        lev[l] = s;
+    }
+    __syncthreads();
+    const int deep = a.nlev - 1;
+    if (a.mode == CYCLE_V) {
+        co_vcycle(lev, 0, deep, a.zero_first != 0, a.c1, a.c2, a.ndeepest);
+    } else {
+        for (int l = 0; l < deep; l++) co_restrict(lev[l], lev[l].b, lev[l + 1], lev[l + 1].b);
+        for (int k = 0; k < a.ndeepest; k++) co_smooth(lev[deep], a.c1, a.c2, k == 0);
+        for (int l = deep - 1; l >= 0; l--) {
+            co_interp(lev[l + 1], lev[l], true);
+            co_vcycle(lev, l, deep, false, a.c1, a.c2, a.ndeepest);
+        }
+    }
+    const size_t pts0 = (size_t)lev[0].mv * lev[0].nv;
+    for (size_t q = threadIdx.x; q < pts0; q += blockDim.x) a.lev[0].x[q] = lev[0].x[q];
+}
+
+namespace {
+// per library and device: the opt-in shared-memory size of k_coarse
+bool g_coarse_configured[2][64];
+}
+
+template <typename T>
+int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s) {
+    int idx = sizeof(T) == 8 ? 0 : 1, dev = 0;
+    int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st) return st;
+    if (dev < 0 || dev >= 64 || !g_coarse_configured[idx][dev]) {
+        st = cuda_status(cudaFuncSetAttribute(k_coarse<T>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              227 * 1024),
+                         "coarse smem attribute");
+        if (st) return st;
+        if (dev >= 0 && dev < 64) g_coarse_configured[idx][dev] = true;
+    }
+    k_coarse<T><<<1, CO_THREADS, smem, s>>>(args);
+    return launch_status("mg_coarse");
+}
+
+// ------------------------------------------------------------ stage kernels
+F2D_DEV double rk_combine(int rk, double base, double d0, double d1, double dq, double dt) {
+    if (rk == 1) return base + dt * dq;                                  // x + dt*dx0
+    if (rk == 2) return base + (0.25 * dt) * (d0 + dq);                  // x + (dt/4)(dx0+dx1)
+    return base + (dt / 6.) * (d0 + d1 + 4 * dq);                        // x + (dt/6)(...)
+}
+
+// Advection of one tracer with the halo fill, the Boussinesq torque and the
+// RK combination fused (core/operators.py:214-236,303-314,
+// core/timescheme.py:167-180).
+__global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
+    __shared__ double sfx[8][33];
+    __shared__ double sfy[9][32];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nv = a.nv, mv = a.mv;
+    const int I = NH + blockIdx.x * 32 + tx;
+    const int J = NH + blockIdx.y * 8 + ty;
+    const bool in = (I <= nv - NH - 1) && (J <= mv - NH - 1);
+    const SplitConst c = *(const SplitConst *)a.advc;
+    if (in) {
+        const size_t p = off(J, I, nv);
+        sfx[ty][tx + 1] = edge_flux_rt(a.kind, a.msk, a.q, a.u, p, 1, a.method, a.order, c);
+        sfy[ty + 1][tx] = edge_flux_rt(a.kind, a.msk, a.q, a.v, p, nv, a.method, a.order, c);
+        if (tx == 0) sfx[ty][0] = edge_flux_rt(a.kind, a.msk, a.q, a.u, p - 1, 1, a.method, a.order, c);
+        if (ty == 0) sfy[0][tx] = edge_flux_rt(a.kind, a.msk, a.q, a.v, p - nv, nv, a.method, a.order, c);
+    }
+    __syncthreads();
+    if (!in) return;
+    const size_t p = off(J, I, nv);
+    double y = -(c.zdx * (sfx[ty][tx + 1] - sfx[ty][tx])) - c.zdy * (sfy[ty + 1][tx] - sfy[ty][tx]);
+    if (a.buoy) {
+        const int mc = a.msk[p];
+        y = y * (double)mc;
+        const int sl = mc + a.msk[p - 1], sr = a.msk[p + 1] + mc;
+        const int ml = sl > 1 ? sl : 1, mr = sr > 1 ? sr : 1;
+        if (ml + mr == 4) y = y + (a.buoy[p + 1] - a.buoy[p - 1]) * a.torque_coef * (double)mc;
+    }
+    const double dt = a.rk ? *a.dt : 0.;
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    int rows[3], cols[3], nr = 0, nc = 0;
+    rows[nr++] = J;
+    if (J >= m2 && J < m2 + NH) rows[nr++] = J - m2;
+    if (J >= NH && J < 2 * NH) rows[nr++] = J + m2;
+    cols[nc++] = I;
+    if (I >= n2 && I < n2 + NH) cols[nc++] = I - n2;
+    if (I >= NH && I < 2 * NH) cols[nc++] = I + n2;
+    for (int r = 0; r < nr; r++)
+        for (int k = 0; k < nc; k++) {
+            const size_t q = off(rows[r], cols[k], nv);
+            a.dq[q] = y;
+            if (a.rk)
+                a.out[q] = rk_combine(a.rk, a.base[q], a.d0 ? a.d0[q] : 0., a.d1 ? a.d1[q] : 0., y,
+                                      dt);
+        }
+}
+
+int stage_advection(const AdvStage &a, cudaStream_t s) {
+    dim3 b(32, 8);
+    dim3 g = grid2d(a.mv - 2 * NH, a.nv - 2 * NH, b);
+    k_stage_adv<<<g, b, 0, s>>>(a);
+    return launch_status("stage_advection");
+}
+
+// psi <- psi*mskp (whole array, core/operators.py:481) and
+// u,v = orthogradient(psi) (core/fortran_operators.f90:22-37), with the RK
+// combinations of u, v (rows/cols 1..m-2) and of psi fused.
+__global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int nv = a.nv, mv = a.mv;
+    if (i >= nv || j >= mv) return;
+    const size_t p = off(j, i, nv);
+    // masking is idempotent, so neighbours read before or after their own
+    // thread masks them give the same value
+    const double pc = a.mskp[p] ? a.psi[p] : 0.;
+    const double dt = (a.rk || a.psi_rk) ? *a.dt : 0.;
+    a.psi[p] = pc;
+    if (a.psi_rk) {
+        // x += (dt/6)*(dx0 + dx1 + 4*dx2) (core/timescheme.py:180)
+        const double d1 = a.psi1 ? a.psi1[p] : pc;
+        const double d2 = a.psi1 ? pc : 0.;
+        a.psiout[p] = a.psibase[p] + (dt / 6.) * (a.psi0[p] + d1 + 4 * d2);
+    }
+    if (i < 1 || j < 1 || i > nv - 2 || j > mv - 2) return;
+    const double ps = a.mskp[p - nv] ? a.psi[p - nv] : 0.;
+    const double pw = a.mskp[p - 1] ? a.psi[p - 1] : 0.;
+    const int mc = a.msk[p];
+    const double u = (mc + a.msk[p + 1] == 2) ? a.zdy * (ps - pc) : 0.;
+    const double v = (mc + a.msk[p + nv] == 2) ? a.zdx * (pc - pw) : 0.;
+    a.u[p] = u;
+    a.v[p] = v;
+    if (a.rk) {
+        a.uout[p] = rk_combine(a.rk, a.ubase[p], a.u0 ? a.u0[p] : 0., a.u1 ? a.u1[p] : 0., u, dt);
+        a.vout[p] = rk_combine(a.rk, a.vbase[p], a.v0 ? a.v0[p] : 0., a.v1 ? a.v1[p] : 0., v, dt);
+    }
+}
+
+int stage_ortho(const OrthoStage &a, cudaStream_t s) {
+    dim3 b(32, 8);
+    k_stage_ortho<<<grid2d(a.mv, a.nv, b), b, 0, s>>>(a);
+    return launch_status("stage_ortho");
+}
+
+__global__ void k_vec_add(double *x, const double *y, size_t n, const int *active) {
+    if (inactive(active)) return;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = x[q] + y[q];
+}
+
+int vec_add(double *x, const double *y, size_t count, const int *active, cudaStream_t s) {
+    int blocks = (int)((count + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_vec_add<<<blocks, 256, 0, s>>>(x, y, count, active);
+    return launch_status("vec_add");
+}
+
+// x -= dev_scalar[0] / area (core/operators.py:474-477)
+__global__ void k_sub_mean(double *x, double area, const double *sum, size_t n) {
+    const double m = *sum / area;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = x[q] - m;
+}
+
+int vec_axpy_const(double *x, double area, const double *sum, size_t count, cudaStream_t s) {
+    int blocks = (int)((count + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_sub_mean<<<blocks, 256, 0, s>>>(x, area, sum, count);
+    return launch_status("sub_mean");
+}
+
+// explicit instantiations
+#define F2D_INST(T)                                                                              \
+    template int mg_sweep1<T>(const LevelView<T> &, const Analytic *, T, T, bool, const int *,   \
+                              cudaStream_t);                                                     \
+    template int mg_sweep2<T>(const LevelView<T> &, const Analytic *, T, T, const int *,         \
+                              cudaStream_t);                                                     \
+    template int mg_residual<T>(const LevelView<T> &, const Analytic *, const T *, const T *,    \
+                                T *, const int *, cudaStream_t);                                 \
+    template int mg_restrict<T>(const LevelView<T> &, const T *, const LevelView<T> &, T *,      \
+                                const int *, cudaStream_t);                                      \
+    template int mg_interp<T>(const LevelView<T> &, const T *, const LevelView<T> &, T *, bool,  \
+                              const int *, cudaStream_t);                                        \
+    template int mg_coarse<T>(const CoarseArgs<T> &, size_t, cudaStream_t);                     \
+    template size_t coarse_smem_bytes<T>(const int *, const int *, int);
+F2D_INST(double)
+F2D_INST(float)
+
+}  // namespace f2d

@@ -1,0 +1,249 @@
+"""Device-resident multigrid and model steppers (Python side of the engine).
+
+``Gmg``   -- core/gmg/hierarchy.py's Gmg: ``twoVcycle(x, b)`` and
+             ``solve(x, b, param)`` on CUDA tensors, same names and argument
+             meaning (x updated in place).
+``Model`` -- an Euler / Boussinesq / QG model whose state lives on the GPU,
+             with the reference's model API: ``var.state``, ``get(name)``,
+             ``step(t, dt)``, ``diagnostics(var, t)``, ``diags``,
+             ``set_psi_from_vorticity()``.  ``run(nsteps)`` chains the loop
+             body of core/fluid2d.py:237-268 (set_dt, step, diagnostics) with
+             no host synchronisation, optionally replaying a CUDA graph.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import workloads
+
+MODEL_KIND = {"euler": 0, "boussinesq": 1, "quasigeostrophic": 2}
+
+
+class _DevArray(object):
+    """__cuda_array_interface__ view of library-owned device memory."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
+                                         "data": (int(ptr), False), "version": 3,
+                                         "strides": None}
+
+
+def device_view(ptr, shape, dtype=torch.float64):
+    ts = {torch.float64: "<f8", torch.int8: "|i1", torch.float32: "<f4"}[dtype]
+    return torch.as_tensor(_DevArray(ptr, shape, ts), device="cuda")
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+class Gmg(object):
+    """Geometric multigrid of core/gmg/hierarchy.py on the GPU.
+
+    ``mskp`` is the corner mask (core/operators.py:59-67), int8 (ny+6, nx+6)."""
+
+    def __init__(self, mskp, nx, ny, dx, dy, hydroepsilon=1., qgoperator=False, Rd=1.,
+                 variant="product"):
+        self.variant = variant
+        self.L = _lib.lib(variant)
+        m = np.ascontiguousarray(np.asarray(mskp).astype(np.int8))
+        h = ctypes.c_void_p()
+        self._call("f2d_gmg_create", m.ctypes.data, int(nx), int(ny), float(dx), float(dy),
+                   float(hydroepsilon), int(bool(qgoperator)), float(Rd), ctypes.byref(h))
+        self.h = h
+        nlev, cs = ctypes.c_int(), ctypes.c_int()
+        mv = (ctypes.c_int * 32)()
+        nv = (ctypes.c_int * 32)()
+        self._call("f2d_gmg_levels", self.h, ctypes.byref(nlev), mv, nv, ctypes.byref(cs))
+        self.nlevs = nlev.value
+        self.coarse_level = cs.value
+        self.shapes = [(mv[k], nv[k]) for k in range(self.nlevs)]
+
+    def _call(self, name, *args):
+        _lib.call(name, *args, variant=self.variant)
+
+    def level_array(self, lev, which):
+        ptr = self.L.f2d_gmg_level_ptr(self.h, lev, which.encode())
+        if not ptr:
+            raise KeyError(which)
+        mv, nv = self.shapes[lev]
+        if which == "msk":
+            return device_view(ptr, (mv, nv), torch.int8)
+        if which == "A":
+            return device_view(ptr, (6, mv, nv))
+        return device_view(ptr, (mv, nv))
+
+    def twoVcycle(self, x, b, param=None):
+        """core/gmg/hierarchy.py:207-218; x (warm start) updated in place."""
+        self._call("f2d_gmg_twovcycle", self.h, x.data_ptr(), b.data_ptr(), _stream())
+        return 1, 0.
+
+    def solve(self, x, b, param=None):
+        """core/gmg/hierarchy.py:154-192; returns (nite, res) (synchronises)."""
+        param = param or {"maxite": 4, "tol": 1e-11}
+        self._call("f2d_gmg_solve", self.h, x.data_ptr(), b.data_ptr(), int(param["maxite"]),
+                   float(param["tol"]), _stream())
+        torch.cuda.current_stream().synchronize()
+        nite, res, st = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+        self._call("f2d_gmg_solve_stats", self.h, ctypes.byref(nite), ctypes.byref(res),
+                   ctypes.byref(st))
+        if st.value:
+            raise _lib.F2DError("solve", st.value, "solver is not converging")
+        return nite.value, res.value
+
+    def Vcycle(self, lev1):
+        self._call("f2d_gmg_vcycle", self.h, int(lev1), _stream())
+
+    def Fcycle(self, lev1):
+        self._call("f2d_gmg_fcycle", self.h, int(lev1), _stream())
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.f2d_gmg_destroy(self.h)
+        except Exception:
+            pass
+
+
+class _Var(object):
+    def __init__(self, state, names):
+        self.state = state
+        self.varname_list = names
+
+    def get(self, name):
+        return self.state[self.varname_list.index(name)]
+
+
+class Model(object):
+    """A Fluid2d model (Euler, Boussinesq or QG) stepped on the GPU."""
+
+    def __init__(self, modelname="euler", nx=128, ny=128, Lx=1., Ly=1., geometry="closed",
+                 msk=None, order=5, flux_splitting_method="parabolic", aparab=0.05,
+                 gravity=1., Rd=1., beta=0., hydroepsilon=1., adaptable_dt=False, dt=0.1,
+                 cfl=0.5, dtmax=5., precision="fp64", variant="product"):
+        self.variant = variant
+        self.L = _lib.lib(variant)
+        self.modelname = modelname
+        if msk is None:
+            msk = workloads.base_mask(nx, ny, geometry)
+        self.msk = np.ascontiguousarray(msk, dtype=np.int8)
+        d = _lib.ModelDesc()
+        d.model = MODEL_KIND[modelname]
+        d.nx, d.ny, d.Lx, d.Ly = int(nx), int(ny), float(Lx), float(Ly)
+        d.perio = int(geometry == "perio")
+        d.order = int(order)
+        d.flux_method = 0 if flux_splitting_method == "minmax" else 1
+        d.aparab, d.gravity, d.Rd, d.beta = float(aparab), float(gravity), float(Rd), float(beta)
+        d.hydroepsilon = float(hydroepsilon)
+        d.adaptable_dt = int(bool(adaptable_dt))
+        d.dt, d.cfl, d.dtmax = float(dt), float(cfl), float(dtmax)
+        d.precision = {"fp64": 0, "mixed": 1}[precision]
+        self.desc = d
+        h = ctypes.c_void_p()
+        self._call("f2d_model_create", ctypes.byref(d), self.msk.ctypes.data, ctypes.byref(h))
+        self.h = h
+        nvar, mv, nv, nlev, cs = (ctypes.c_int() for _ in range(5))
+        st, dg = ctypes.POINTER(ctypes.c_double)(), ctypes.POINTER(ctypes.c_double)()
+        self._call("f2d_model_info", self.h, ctypes.byref(nvar), ctypes.byref(mv),
+                   ctypes.byref(nv), ctypes.byref(nlev), ctypes.byref(cs), ctypes.byref(st),
+                   ctypes.byref(dg))
+        self.nvar, self.nyl, self.nxl = nvar.value, mv.value, nv.value
+        self.nlevs, self.coarse_level = nlev.value, cs.value
+        names = [self.L.f2d_model_varname(self.h, k).decode() for k in range(self.nvar)]
+        self.var = _Var(device_view(ctypes.cast(st, ctypes.c_void_p).value,
+                                    (self.nvar, self.nyl, self.nxl)), names)
+        self.diag_names = []
+        k = 0
+        while True:
+            nm = self.L.f2d_model_diagname(self.h, k)
+            if nm is None:
+                break
+            self.diag_names.append(nm.decode())
+            k += 1
+        self._diag = device_view(ctypes.cast(dg, ctypes.c_void_p).value, (8,))
+        self.diags = {}
+        self.dx, self.dy = d.Lx / d.nx, d.Ly / d.ny
+
+    def _call(self, name, *args):
+        _lib.call(name, *args, variant=self.variant)
+
+    def buffer(self, which):
+        ptr = self.L.f2d_model_buffer(self.h, which.encode())
+        if which in ("state", "dx0", "dx1", "dx2"):
+            return device_view(ptr, (self.nvar, self.nyl, self.nxl))
+        if which == "work":
+            return device_view(ptr, (self.nyl, self.nxl))
+        return device_view(ptr, (8,))
+
+    def get(self, name):
+        return self.var.get(name)
+
+    def set_psi_from_vorticity(self):
+        self._call("f2d_model_set_psi", self.h, _stream())
+
+    set_psi_from_pv = set_psi_from_vorticity
+
+    def diagnostics(self, var=None, t=0.):
+        self._call("f2d_model_diagnostics", self.h, _stream())
+        return self.read_diags()
+
+    def read_diags(self):
+        vals = self._diag.cpu().numpy()
+        self.diags = {n: float(vals[k]) for k, n in enumerate(self.diag_names)}
+        return self.diags
+
+    def set_dt(self, dt):
+        self._call("f2d_model_set_dt", self.h, float(dt))
+
+    def step(self, t=0., dt=None):
+        """One iteration of the Fluid2d loop body: set_dt (dt fixed unless
+        adaptable_dt), the RK3 step, the diagnostics (kept on the device)."""
+        if dt is not None and dt != self.desc.dt:
+            self.desc.dt = dt
+            self.set_dt(dt)
+        self._call("f2d_model_step", self.h, 1, _stream())
+
+    def run(self, nsteps, graph=False):
+        if graph:
+            self._call("f2d_model_step_graph", self.h, int(nsteps), _stream())
+        else:
+            self._call("f2d_model_step", self.h, int(nsteps), _stream())
+
+    def probe(self, enable=None):
+        """Enable/disable the finest-level smoother probe, or (enable=None)
+        return (count, mean ms) over the probed calls of the last step."""
+        c, ms = ctypes.c_int(), ctypes.c_double()
+        if enable is None:
+            self._call("f2d_model_probe", self.h, -1, ctypes.byref(c), ctypes.byref(ms))
+            return c.value, ms.value
+        self._call("f2d_model_probe", self.h, int(bool(enable)), None, None)
+
+    def graph_kernels(self):
+        n = ctypes.c_int()
+        self._call("f2d_model_graph_kernels", self.h, ctypes.byref(n))
+        return n.value
+
+    def solve_stats(self):
+        nite, res, st = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+        self._call("f2d_model_solve_stats", self.h, ctypes.byref(nite), ctypes.byref(res),
+                   ctypes.byref(st))
+        return nite.value, res.value, st.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.f2d_model_destroy(self.h)
+        except Exception:
+            pass
+
+
+def from_workload(wl, variant="product", precision="fp64", **kw):
+    """A Model initialised from a workloads.* dict (fields uploaded, psi set)."""
+    m = Model(wl["model"], wl["nx"], wl["ny"], wl["Lx"], wl["Ly"], wl["geometry"],
+              msk=wl["msk"], gravity=wl.get("gravity", 1.), variant=variant,
+              precision=precision, **kw)
+    for name, f in wl["fields"].items():
+        m.get(name).copy_(torch.from_numpy(np.ascontiguousarray(f)).cuda())
+    return m

@@ -33,6 +33,11 @@
 extern "C" {
 #endif
 
+/* the library is built with hidden visibility; only these entry points are exported */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 #define F2D_OK 0
 #define F2D_ERR_NH 1       /* nh != 3 where the reference stops */
 #define F2D_ERR_SHAPE 2    /* unusable array dimensions */
@@ -151,6 +156,85 @@ int f2d_computenorm(const int8_t *msk, const double *x, int nh, int m, int n, do
 /* core/gmg/fortran_multigrid.f90:841-867 z=computeinner(msk,x,y,nh) -> out[0] */
 int f2d_computeinner(const int8_t *msk, const double *x, const double *y, int nh, int m,
                      int n, double *out, void *stream);
+
+/* ------------------------------------------------ device engine -------- */
+/* Multigrid hierarchy on caller arrays: core/gmg/hierarchy.py:21-84 (Gmg,
+ * setup_hierarchy) built from the corner mask mskp (HOST int8, (ny+6, nx+6)),
+ * then twoVcycle (:207-218, operators.py:447) and solve (:154-192,
+ * operators.py:470) on DEVICE arrays x (in place) and b.  The solve's
+ * iteration count and residual stay on the device (f2d_gmg_solve_stats reads
+ * them back, synchronously).  Coarsening stops before a level would have an
+ * odd dimension (the reference supports power-of-two grids only, on which
+ * nothing changes). */
+int f2d_gmg_create(const int8_t *mskp_host, int nx, int ny, double dx, double dy,
+                   double hydroepsilon, int qg, double Rd, void **gmg);
+int f2d_gmg_destroy(void *gmg);
+int f2d_gmg_levels(void *gmg, int *nlev, int *mv, int *nv, int *coarse_level);
+int f2d_gmg_twovcycle(void *gmg, double *x, const double *b, void *stream);
+int f2d_gmg_solve(void *gmg, double *x, const double *b, int maxite, double tol, void *stream);
+int f2d_gmg_solve_stats(void *gmg, int *nite, double *res, int *status);
+/* the hierarchy's own arrays of level lev: "msk" (int8), "A" (6 planes:
+ * A1..A5 and omega/|A5|, levels >= 1), "x", "b", "r" */
+void *f2d_gmg_level_ptr(void *gmg, int lev, const char *which);
+/* core/gmg/hierarchy.py:98 Vcycle(lev1) and :131 Fcycle(lev1) on the
+ * hierarchy's own x/b arrays */
+int f2d_gmg_vcycle(void *gmg, int lev1, void *stream);
+int f2d_gmg_fcycle(void *gmg, int lev1, void *stream);
+
+/* Model time stepper: core/euler.py, core/boussinesq.py,
+ * core/quasigeostrophic.py with core/timescheme.py:167-180 (RK3_SSP), the
+ * Operators of core/operators.py and the loop body of core/fluid2d.py:237-268
+ * (set_dt, step, diagnostics), all device-resident. */
+#define F2D_EULER 0
+#define F2D_BOUSSINESQ 1
+#define F2D_QG 2
+typedef struct f2d_model_desc {
+    int model;           /* F2D_EULER, F2D_BOUSSINESQ or F2D_QG */
+    int nx, ny;          /* interior cells (core/grid.py:31-32) */
+    double Lx, Ly;
+    int perio;           /* geometry 'perio': remove the mean of psi after the full solve */
+    int order;           /* advection order (odd: upwind, even: centred) */
+    int flux_method;     /* 0 minmax, 1 parabolic (core/operators.py:121-131) */
+    double aparab;
+    double gravity;      /* Boussinesq */
+    double Rd, beta;     /* QG */
+    double hydroepsilon;
+    int adaptable_dt;    /* core/fluid2d.py:378-391 */
+    double dt, cfl, dtmax;
+    int precision;       /* 0: float64 */
+} f2d_model_desc;
+/* msk_host: HOST int8 cell mask (ny+6, nx+6) including the geometry's halo */
+int f2d_model_create(const f2d_model_desc *d, const int8_t *msk_host, void **model);
+int f2d_model_destroy(void *model);
+/* state: DEVICE (nvar, ny+6, nx+6) float64, the reference's Var.state layout;
+ * diag: DEVICE array of the model's diagnostics (f2d_model_diagname) */
+int f2d_model_info(void *model, int *nvar, int *mv, int *nv, int *nlev, int *coarse_level,
+                   double **state, double **diag);
+const char *f2d_model_varname(void *model, int k);
+const char *f2d_model_diagname(void *model, int k);
+/* internal buffers: "state", "dx0", "dx1", "dx2" (RK tendencies, whose psi
+ * planes are the warm starts), "cst", "dt", "diag", "work" */
+double *f2d_model_buffer(void *model, const char *which);
+/* set_psi_from_vorticity / set_psi_from_pv: full solve and psi -> u, v */
+int f2d_model_set_psi(void *model, void *stream);
+int f2d_model_diagnostics(void *model, void *stream);
+/* nsteps iterations of (set_dt, step, diagnostics) */
+int f2d_model_step(void *model, int nsteps, void *stream);
+/* the same, replaying one step captured in a CUDA graph (non-default stream) */
+int f2d_model_step_graph(void *model, int nsteps, void *stream);
+int f2d_model_set_dt(void *model, double dt);
+int f2d_model_solve_stats(void *model, int *nite, double *res, int *status);
+/* Timing probe of the finest-level smoother (one smoothtwicewitha call =
+ * the engine's two sweep kernels): enable >= 0 switches it on/off (and drops
+ * a captured graph); enable < 0 reads the mean duration in ms over the
+ * probed calls of the last step (synchronous). */
+int f2d_model_probe(void *model, int enable, int *count, double *avg_ms);
+/* number of kernel nodes in the captured step graph */
+int f2d_model_graph_kernels(void *model, int *nkernels);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

@@ -755,3 +755,24 @@ def run(model, param, nsteps, dt0, t=0., callback=None):
         if callback is not None:
             callback(kt + 1, t, model)
     return t
+
+
+def from_workload(wl, **kw):
+    """An oracle model for a fluid2d_gb300.workloads dict: mask, fields,
+    initial inversion (set_psi_from_vorticity / set_psi_from_pv) and
+    diagnostics, as a Fluid2d experiment script sets them up."""
+    p = Param(modelname=wl["model"], nx=wl["nx"], ny=wl["ny"], Lx=wl["Lx"], Ly=wl["Ly"],
+              geometry=wl["geometry"], gravity=wl.get("gravity", 1.), **kw)
+    g = Grid(p)
+    g.msk = wl["msk"].copy()
+    g.finalize_msk()
+    M = MODELS[wl["model"]](p, grid=g)
+    for name, f in wl["fields"].items():
+        M.get(name)[:] = f
+    if wl["model"] == "quasigeostrophic":
+        M.get("pv")[:] += M.pvback
+        M.set_psi_from_pv()
+    else:
+        M.set_psi_from_vorticity()
+    M.diagnostics()
+    return p, M

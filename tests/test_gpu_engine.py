@@ -1,0 +1,147 @@
+"""Step-level parity of the device engine against the oracle stepper.
+
+With the exact build, closed-domain Euler, Boussinesq and QG states after
+several RK3 steps are bit-identical to the oracle (the only reductions that
+feed the state are maxima); the periodic Euler case differs by the rounding
+of the mean of psi (a sum), so it is compared with a tolerance.  The product
+build (FMA contraction) is compared at 1e-10 relative L-inf, the north-star
+parity bar after 10 steps.
+"""
+import numpy as np
+import pytest
+
+from tests import _cases as C
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def eng():
+    import torch
+    from fluid2d_gb300 import engine
+    assert torch.cuda.is_available()
+    return engine
+
+
+def relerr(a, b):
+    return np.abs(a - b).max() / max(1e-300, np.abs(b).max())
+
+
+def _workloads():
+    from fluid2d_gb300 import workloads as W
+    qg = W.dipole(64, 64, seed=7)
+    qg["model"] = "quasigeostrophic"
+    qg["fields"] = {"pv": qg["fields"]["vorticity"]}
+    isl = W.dipole(64, 48, seed=9)
+    isl["msk"] = C.mask(54, 70, "closed", 2, 9)
+    isl["fields"]["vorticity"] = isl["fields"]["vorticity"] * isl["msk"]
+    return {
+        "euler-closed-dipole": W.dipole(64, 64),
+        "euler-closed-islands": isl,
+        "euler-perio-turb": W.turbulence(64, 64, seed=5),
+        "boussinesq-xchannel": W.shear(128, 32, seed=3),
+        "qg-closed": qg,
+    }
+
+
+WL = list(_workloads().keys())
+
+
+def _pair(eng, name, variant, steps):
+    import torch
+    wl = _workloads()[name]
+    kw = {"Rd": 0.3, "beta": 2.0} if wl["model"] == "quasigeostrophic" else {}
+    p, O = C.oracle_model(wl, **kw)
+    dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
+    G = eng.from_workload(wl, variant=variant, dt=dt, **kw)
+    if wl["model"] == "quasigeostrophic":
+        G.get("pv").copy_(torch.from_numpy(O.get("pv")).cuda())
+    G.set_psi_from_vorticity()
+    G.diagnostics()
+    s0 = G.var.state.cpu().numpy()
+    from oracle import stepper
+    stepper.run(O, p, steps, dt)
+    G.run(steps)
+    torch.cuda.synchronize()
+    return O, G, s0
+
+
+@pytest.mark.parametrize("name", WL)
+def test_initial_solve(eng, name):
+    import torch
+    wl = _workloads()[name]
+    kw = {"Rd": 0.3, "beta": 2.0} if wl["model"] == "quasigeostrophic" else {}
+    p, O = C.oracle_model(wl, **kw)
+    G = eng.from_workload(wl, variant="exact", **kw)
+    if wl["model"] == "quasigeostrophic":
+        G.get("pv").copy_(torch.from_numpy(O.get("pv")).cuda())
+    G.set_psi_from_vorticity()
+    d = G.diagnostics()
+    st = G.var.state.cpu().numpy()
+    tol = 1e-13 if wl["geometry"] == "perio" else 0.
+    for k, nm in enumerate(G.var.varname_list):
+        assert relerr(st[k], O.state[k]) <= tol, (nm, relerr(st[k], O.state[k]))
+    assert d["maxspeed"] == O.diags["maxspeed"] or tol
+    assert G.solve_stats()[0] == O.ope.last_solve[0]
+
+
+@pytest.mark.parametrize("variant", ["exact", "product"])
+@pytest.mark.parametrize("name", WL)
+def test_steps(eng, name, variant):
+    steps = 5
+    O, G, _ = _pair(eng, name, variant, steps)
+    st = G.var.state.cpu().numpy()
+    d = G.read_diags()
+    exact = variant == "exact" and "perio" not in name
+    for k, nm in enumerate(G.var.varname_list):
+        e = relerr(st[k], O.state[k])
+        if exact:
+            assert np.array_equal(st[k], O.state[k]), (nm, e)
+        else:
+            assert e <= 1e-10, (nm, e)
+    for k, v in d.items():
+        assert abs(v - O.diags[k]) <= 1e-9 * max(1e-12, abs(O.diags[k])) + 1e-300 or \
+            abs(v - O.diags[k]) < 1e-14, (k, v, O.diags[k])
+
+
+@pytest.mark.parametrize("name", ["euler-closed-dipole", "boussinesq-xchannel"])
+def test_graph_replay_matches_eager(eng, name):
+    import torch
+    wl = _workloads()[name]
+    A = eng.from_workload(wl, variant="product", dt=1e-3)
+    B = eng.from_workload(wl, variant="product", dt=1e-3)
+    for M in (A, B):
+        M.set_psi_from_vorticity()
+        M.diagnostics()
+    A.run(4)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        B.run(4, graph=True)
+    s.synchronize()
+    torch.cuda.synchronize()
+    assert torch.equal(A.var.state, B.var.state)
+
+
+def test_gmg_twovcycle_and_solve(eng):
+    import torch
+    from oracle import stepper
+    for (m, n, geom, isl, seed) in [(70, 70, "closed", 2, 1), (38, 134, "perio", 0, 2),
+                                   (134, 70, "xchannel", 3, 3)]:
+        msk = C.corner_mask(C.mask(m, n, geom, isl, seed))
+        dx = 1. / (n - 6)
+        pp = {'nh': 3, 'n': n - 6, 'm': m - 6, 'omega': 8. / 9., 'dx': dx, 'dy': dx}
+        O = stepper.Gmg(pp, msk * 1.)
+        G = eng.Gmg(msk, n - 6, m - 6, dx, dx, variant="exact")
+        x, b = C.field(m, n, seed), C.field(m, n, seed + 1)
+        xo = x.copy()
+        O.twoVcycle(xo, b)
+        xg = torch.from_numpy(x).cuda()
+        G.twoVcycle(xg, torch.from_numpy(b).cuda())
+        assert np.array_equal(xg.cpu().numpy(), xo), relerr(xg.cpu().numpy(), xo)
+        xo = x.copy()
+        nite_o, res_o = O.solve(xo, b, {'maxite': 4, 'tol': 1e-11})
+        xg = torch.from_numpy(x).cuda()
+        nite_g, res_g = G.solve(xg, torch.from_numpy(b).cuda())
+        assert nite_g == nite_o
+        assert abs(res_g - res_o) <= 1e-6 * res_o
+        assert np.array_equal(xg.cpu().numpy(), xo), relerr(xg.cpu().numpy(), xo)

@@ -48,12 +48,14 @@ def host(t):
 
 
 def check(got, ref, variant, rtol=1e-12):
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
     if variant == "exact":
-        assert np.array_equal(got, ref), "max |diff| %g" % np.abs(got - ref).max()
+        assert np.array_equal(got, ref, equal_nan=True), "max |diff| %g" % np.nanmax(
+            np.abs(got - ref))
     else:
-        scale = max(1e-300, np.abs(ref).max())
-        assert np.abs(got - ref).max() <= rtol * scale, "max rel diff %g" % (
-            np.abs(got - ref).max() / scale)
+        scale = max(1e-300, np.nanmax(np.abs(ref)))
+        d = np.nanmax(np.abs(got - ref))
+        assert d <= rtol * scale, "max rel diff %g" % (d / scale)
 
 
 def cases():
@@ -170,7 +172,10 @@ def test_diagnostics(gk, variant, m, n, geom, islands, seed):
                 assert abs(a[k] - b[k]) <= 1e-12 * max(1., abs(b[k])), (k, a, b)
 
     close(gk.computekemaxu(M, U, V, 3), K().computekemaxu(msk, u, v, 3), exact_max=(1,))
-    close(gk.computekemaxuv(M, U, V, 3), K().computekemaxuv(msk, u, v, 3), exact_max=(1, 2))
+    # maxu/maxv of computekemaxuv are maxima of u^2+u'^2, which FMA contraction
+    # may round differently: exact only in the exact build
+    close(gk.computekemaxuv(M, U, V, 3), K().computekemaxuv(msk, u, v, 3),
+          exact_max=(1, 2) if variant == "exact" else ())
     close(gk.computesumandnorm(M, X, 3), K().computesumandnorm(msk, x, 3))
     close(gk.computenormmaxu(M, X, 3), K().computenormmaxu(msk, x, 3), exact_max=(1,))
     close(gk.computedotprod(M, X, U, 3), K().computedotprod(msk, x, u, 3))

@@ -21,7 +21,7 @@ CSRC = os.path.join(_HERE, "csrc")
 BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
-           "kernels_fused.cu"]
+           "kernels_fused.cu", "noalloc.cu"]
 HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -141,6 +141,7 @@ SIGNATURES = {
     "f2d_computekemaxuv": [_P, _P, _P, _I, _I, _I, _P, _P],
     "f2d_computekewithpsi": [_P, _P, _P, _I, _I, _I, _P, _P],
     "f2d_smoothtwicewitha": [_P, _P, _P, _P, _D, _I, _I, _P],
+    "f2d_smoothtwicewitha_noalloc": [_P, _P, _P, _P, _D, _I, _I, _P],
     "f2d_computeresidualwitha": [_P, _P, _P, _P, _P, _I, _I, _P],
     "f2d_fillhalo": [_P, _I, _I, _I, _P],
     "f2d_interpolate": [_P, _P, _P, _I, _I, _I, _I, _I, _P, _P],

@@ -132,6 +132,17 @@ int f2d_computekewithpsi(const int8_t *msk, const double *omega, const double *p
  * array (scratch). */
 int f2d_smoothtwicewitha(const int8_t *msk, const double *A, double *x, const double *b,
                          double coef, int m, int n, void *stream);
+/* No counterpart in the reference.  The same smoother as f2d_smoothtwicewitha
+ * for callers that must not allocate device memory (their memory comes from
+ * their own allocator or a fixed budget, or they may not call cudaMalloc or
+ * synchronise the device where they smooth): its work array is a fixed
+ * 16 MiB static device buffer instead of library-allocated scratch, so
+ * m*n may be at most 2^21 points (larger grids: F2D_ERR_LIMIT).  The first
+ * call on a device looks up that buffer's device address (no allocation);
+ * make that first call before any stream capture.  All calls share the
+ * buffer, so calls that overlap on the GPU race with each other. */
+int f2d_smoothtwicewitha_noalloc(const int8_t *msk, const double *A, double *x,
+                                 const double *b, double coef, int m, int n, void *stream);
 /* core/gmg/fortran_multigrid.f90:320-362 computeresidualwitha(msk,A,x,b,y),
  * core/gmg/level.py:374 */
 int f2d_computeresidualwitha(const int8_t *msk, const double *A, const double *x,

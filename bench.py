@@ -198,6 +198,7 @@ def run_ours(a, rank, world, local):
     d0 = M.diagnostics()
     dt = 0.8 * min(M.dx, M.dy) / d0["maxspeed"]
     M.set_dt(dt)
+    s0 = M.var.state.clone()
     stream = torch.cuda.Stream()
     # warm-up: capture the step graph and run W steps
     with torch.cuda.stream(stream):
@@ -231,6 +232,14 @@ def run_ours(a, rank, world, local):
     value = world * n * n * a.steps / (ms * 1e-3)
     nite, res, st = M.solve_stats()
     diags = M.read_diags()
+
+    # ---- the mixed form on the same workload (FP32 fluxes and multigrid
+    # cycles inside an FP64 defect correction; FP64 state, RK and diagnostics)
+    mixed = None
+    try:
+        mixed = bench_mixed(engine, wl, dt, s0, a, stream, world)
+    except Exception as exc:
+        print("mixed form failed: %s" % exc, file=sys.stderr)
 
     # ---- roofline of the dominant kernel (the finest-level smoother, timed
     # with CUDA events around every call inside the replayed step graph)
@@ -322,6 +331,7 @@ def run_ours(a, rank, world, local):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": a.e2e_steps},
+        "mixed": mixed,
         "gpu_launches": kernels_per_step * a.steps,
         "clocks": clk.summary(),
         "libraries": [os.path.basename(so_path("product"))],
@@ -329,6 +339,48 @@ def run_ours(a, rank, world, local):
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def bench_mixed(engine, wl, dt, s0, a, stream, world):
+    """Throughput of the mixed form, and its single-step error against the
+    float64 path from the same state (per field, relative L2)."""
+    import torch
+    n = wl["nx"]
+    Mm = engine.from_workload(wl, dt=dt, precision="mixed")
+    Mm.var.state.copy_(s0)
+    Mm.diagnostics()
+    with torch.cuda.stream(stream):
+        Mm.run(a.warmup, graph=True)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        Mm.run(a.steps, graph=True)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    nite, res, st = Mm.solve_stats()
+    del Mm
+    # one step of each form from the same (fresh) state
+    A = engine.from_workload(wl, dt=dt)
+    B = engine.from_workload(wl, dt=dt, precision="mixed")
+    for M in (A, B):
+        M.var.state.copy_(s0)
+        M.diagnostics()
+        M.run(1)
+    torch.cuda.synchronize()
+    err = {}
+    for k, nm in enumerate(A.var.varname_list):
+        ref = A.var.state[k]
+        nrm = float(torch.linalg.vector_norm(ref))
+        if nrm > 0:
+            err[nm] = float(torch.linalg.vector_norm(B.var.state[k] - ref)) / nrm
+    return {"value": world * n * n * a.steps / (ms * 1e-3), "unit": UNIT,
+            "ms_per_step": ms / a.steps, "dtype": "f32 fluxes and multigrid, f64 defect "
+            "correction, RK accumulation and diagnostics",
+            "single_step_rel_l2_vs_f64": err, "solve_iterations_last_step": nite,
+            "solve_residual_last_step": res}
 
 
 def main():

@@ -493,6 +493,48 @@ static int solve(Gmg &g, double *x, const double *b, int maxite, double tol, cud
     return OK;
 }
 
+// ---- mixed form: FP32 cycles inside an FP64 defect correction.
+// twoVcycle: x <- x + V32(b - A x), twice.  A V-cycle is linear in its
+// right-hand side and initial guess, so V(x, b) = x + V(0, b - A x): in
+// exact arithmetic this is the reference's two V-cycles (hierarchy.py:207-218).
+static int two_vcycle_mixed(Gmg &g, double *x, const double *b, cudaStream_t s) {
+    LevelView<double> L0 = g.d[0];
+    LevelView<float> Lf[MAX_LEVELS];
+    for (int l = 0; l < g.nlev; l++) Lf[l] = g.f[l];
+    const size_t pl = (size_t)L0.mv * L0.nv;
+    for (int k = 0; k < 2; k++) {
+        TRY(mg_residual_mixed(L0, g.an, x, b, L0.r, Lf[0].b, nullptr, s));
+        TRY(g.vcycle(Lf, 0, true, nullptr, s));
+        TRY(vec_add_f32(x, Lf[0].x, pl, nullptr, s));
+    }
+    return OK;
+}
+
+// solve (hierarchy.py:154-192) is already in correction form: the F-cycles
+// run in FP32 on the FP64 residual, the correction is accumulated in FP64.
+static int solve_mixed(Gmg &g, double *x, const double *b, int maxite, double tol,
+                       cudaStream_t s) {
+    LevelView<double> L0 = g.d[0];
+    LevelView<float> Lf[MAX_LEVELS];
+    for (int l = 0; l < g.nlev; l++) Lf[l] = g.f[l];
+    const size_t pl = (size_t)L0.mv * L0.nv;
+    TRY(mg_residual_mixed(L0, g.an, x, b, L0.b, Lf[0].b, nullptr, s));
+    TRY(launch_reduce(8, L0.msk, b, nullptr, NH, L0.mv, L0.nv, g.sums + 0, g.work, s));
+    TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
+    k_solve_init<<<1, 1, 0, s>>>(g.solve_state, g.sums + 0, g.sums + 1, maxite, tol);
+    TRY(launch_status("solve init"));
+    const int *active = &g.solve_state->active;
+    for (int it = 0; it < maxite; it++) {
+        TRY(g.fcycle(Lf, 0, active, s));
+        TRY(vec_add_f32(x, Lf[0].x, pl, active, s));
+        TRY(mg_residual_mixed(L0, g.an, x, b, L0.b, Lf[0].b, active, s));
+        TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
+        k_solve_update<<<1, 1, 0, s>>>(g.solve_state, g.sums + 1);
+        TRY(launch_status("solve update"));
+    }
+    return OK;
+}
+
 // ------------------------------------------------------------ model
 enum ModelKind { M_EULER = 0, M_BOUSSINESQ = 1, M_QG = 2 };
 
@@ -778,9 +820,13 @@ int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t 
 // psi*mskp + orthogradient pass, which the caller fuses with RK updates
 int Model::invert(double *xs, const char *who, bool full, cudaStream_t s, double *) {
     double *w = plane(xs, who), *psi = plane(xs, "psi");
+    const bool mixed = desc.precision != 0;
     TRY(launch_celltocorner(w, B, mv, nv, s));
-    if (!full) return two_vcycle(gmg, psi, B, s);
-    TRY(solve(gmg, psi, B, 4, 1e-11, s));
+    if (!full) return mixed ? two_vcycle_mixed(gmg, psi, B, s) : two_vcycle(gmg, psi, B, s);
+    if (mixed)
+        TRY(solve_mixed(gmg, psi, B, 4, 1e-11, s));
+    else
+        TRY(solve(gmg, psi, B, 4, 1e-11, s));
     if (desc.perio) {
         // psi -= sum(psi[interior])/area (core/operators.py:474-477), an unmasked sum
         TRY(launch_reduce(2, ones, psi, nullptr, NH, mv, nv, gmg.sums + 2, gmg.work, s));
@@ -816,6 +862,7 @@ static AdvStage adv_base(Model &M, const double *xs, const char *tracer, double 
     a.dq = M.plane(dq, tracer);
     a.dt = M.dt;
     a.kind = (M.desc.order % 2 == 0) ? 1 : 0;
+    a.fp32 = M.desc.precision != 0;
     a.method = M.desc.flux_method;
     a.order = M.desc.order;
     a.mv = M.mv;

@@ -25,9 +25,21 @@ F2D_DEV SplitConst split_const(const double *cst) {
     return c;
 }
 
+// Split constants in the compute type T (float for the mixed form)
+template <typename T>
+struct SplitT {
+    T zdx, zdy, a, KK, u1, aa, bb;
+};
+
+template <typename T>
+F2D_DEV SplitT<T> split_cast(const SplitConst &c) {
+    return SplitT<T>{(T)c.zdx, (T)c.zdy, (T)c.a, (T)c.KK, (T)c.u1, (T)c.aa, (T)c.bb};
+}
+
 // |U| of the flux splitting (core/fortran_advection.f90:77-83)
-F2D_DEV double split_speed(double uu, int method, const SplitConst &c) {
-    double UU = 0.;
+template <typename T>
+F2D_DEV T split_speed(T uu, int method, const SplitT<T> &c) {
+    T UU = 0;
     if (method == 0) UU = fabs(uu);
     if (method == 1) {
         UU = fabs(uu);
@@ -39,21 +51,23 @@ F2D_DEV double split_speed(double uu, int method, const SplitConst &c) {
 
 // Upwind edge flux between cells p0 and p1 along a line with stride s;
 // q[k] = x at p0 + (k-2)*s for k = 0..5 (cells p0-2 .. p0+3), mk likewise.
-// core/fortran_advection.f90:72-111 (x) and :113-146 (y).
-F2D_DEV double upwind_flux(const double *q, const int *mk, double vel, int method,
-                           int order, const SplitConst &c) {
-    if (mk[2] + mk[3] != 2) return 0.;
-    const double d1 = r4(1.f / 30.f), d2 = r4(-13.f / 60.f), d3 = r4(47.f / 60.f),
-                 d4 = r4(9.f / 20.f), d5 = r4(-1.f / 20.f);
-    const double c1 = r4(-1.f / 6.f), c2 = r4(5.f / 6.f), c3 = r4(2.f / 6.f);
-    double UU = split_speed(vel, method, c);
-    double up = 0.5 * (vel + UU);
-    double um = 0.5 * (vel - UU);
+// core/fortran_advection.f90:72-111 (x) and :113-146 (y).  The weights are
+// the Fortran's REAL*4 literals, exact in float and widened in double.
+template <typename T>
+F2D_DEV T upwind_flux(const T *q, const int *mk, T vel, int method, int order,
+                      const SplitT<T> &c) {
+    if (mk[2] + mk[3] != 2) return 0;
+    const T d1 = (T)r4(1.f / 30.f), d2 = (T)r4(-13.f / 60.f), d3 = (T)r4(47.f / 60.f),
+            d4 = (T)r4(9.f / 20.f), d5 = (T)r4(-1.f / 20.f);
+    const T c1 = (T)r4(-1.f / 6.f), c2 = (T)r4(5.f / 6.f), c3 = (T)r4(2.f / 6.f);
+    T UU = split_speed(vel, method, c);
+    T up = (T)0.5 * (vel + UU);
+    T um = (T)0.5 * (vel - UU);
     int m5p = mk[0] + mk[1] + mk[2] + mk[3] + mk[4];
     int m3p = mk[1] + mk[2] + mk[3];
     int m5m = mk[1] + mk[2] + mk[3] + mk[4] + mk[5];
     int m3m = mk[2] + mk[3] + mk[4];
-    double qp, qm;
+    T qp, qm;
     if (m5p == 5 && order == 5)
         qp = d1 * q[0] + d2 * q[1] + d3 * q[2] + d4 * q[3] + d5 * q[4];
     else if (m3p == 3 && order >= 3)
@@ -72,16 +86,16 @@ F2D_DEV double upwind_flux(const double *q, const int *mk, double vel, int metho
 // Centred edge flux (orders 2/4/6), core/fortran_advection.f90:228-262;
 // the fortran_fluxes copy (core/fortran_fluxes.f90:225-258) has no 6th
 // order branch (allow6 = false).
-F2D_DEV double centered_flux(const double *q, const int *mk, double vel, int order,
-                             bool allow6) {
+template <typename T>
+F2D_DEV T centered_flux(const T *q, const int *mk, T vel, int order, bool allow6) {
     int m2 = mk[2] + mk[3];
-    if (m2 != 2) return 0.;
-    const double e1 = r4(1.f / 60.f), e2 = r4(-2.f / 15.f), e3 = r4(37.f / 60.f);
-    const double d1 = r4(-1.f / 12.f), d2 = r4(7.f / 12.f);
-    const double c1 = r4(1.f / 2.f);
+    if (m2 != 2) return 0;
+    const T e1 = (T)r4(1.f / 60.f), e2 = (T)r4(-2.f / 15.f), e3 = (T)r4(37.f / 60.f);
+    const T d1 = (T)r4(-1.f / 12.f), d2 = (T)r4(7.f / 12.f);
+    const T c1 = (T)r4(1.f / 2.f);
     int m6 = mk[0] + mk[1] + mk[2] + mk[3] + mk[4] + mk[5];
     int m4 = mk[1] + mk[2] + mk[3] + mk[4];
-    double qp = 0.;
+    T qp = 0;
     if (allow6 && m6 == 6 && order == 6) {
         qp = e1 * (q[0] + q[5]) + e2 * (q[1] + q[4]);
         qp = qp + e3 * (q[2] + q[3]);
@@ -93,23 +107,37 @@ F2D_DEV double centered_flux(const double *q, const int *mk, double vel, int ord
     return vel * qp;
 }
 
-template <int KIND>  // 0 upwind, 1 centred (advection), 2 centred (fluxes copy)
-F2D_DEV double edge_flux(const int8_t *msk, const double *x, const double *vel,
-                         size_t p0, ptrdiff_t s, int method, int order,
-                         const SplitConst &c) {
-    double q[6];
+// edge flux in compute type T from float64 arrays
+template <int KIND, typename T>
+F2D_DEV T edge_flux_t(const int8_t *msk, const double *x, const double *vel, size_t p0,
+                      ptrdiff_t s, int method, int order, const SplitT<T> &c) {
+    T q[6];
     int mk[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) {
         ptrdiff_t o = (ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s;
         mk[k] = msk[o];
     }
-    if (mk[2] + mk[3] != 2) return 0.;
+    if (mk[2] + mk[3] != 2) return 0;
 #pragma unroll
-    for (int k = 0; k < 6; k++) q[k] = __ldg(x + (ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s);
-    double w = __ldg(vel + p0);
-    if (KIND == 0) return upwind_flux(q, mk, w, method, order, c);
-    return centered_flux(q, mk, w, order, KIND == 1);
+    for (int k = 0; k < 6; k++) q[k] = (T)__ldg(x + (ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s);
+    T w = (T)__ldg(vel + p0);
+    if (KIND == 0) return upwind_flux<T>(q, mk, w, method, order, c);
+    return centered_flux<T>(q, mk, w, order, KIND == 1);
+}
+
+template <int KIND>
+F2D_DEV double edge_flux(const int8_t *msk, const double *x, const double *vel, size_t p0,
+                         ptrdiff_t s, int method, int order, const SplitConst &c) {
+    return edge_flux_t<KIND, double>(msk, x, vel, p0, s, method, order, split_cast<double>(c));
+}
+
+template <typename T>
+F2D_DEV T edge_flux_rt_t(int kind, const int8_t *msk, const double *x, const double *vel,
+                         size_t p0, ptrdiff_t s, int method, int order, const SplitT<T> &c) {
+    if (kind == 0) return edge_flux_t<0, T>(msk, x, vel, p0, s, method, order, c);
+    if (kind == 1) return edge_flux_t<1, T>(msk, x, vel, p0, s, method, order, c);
+    return edge_flux_t<2, T>(msk, x, vel, p0, s, method, order, c);
 }
 
 // runtime-kind dispatch (uniform across the grid)

@@ -82,6 +82,7 @@ struct AdvStage {
     double *out;
     const double *dt;         // device scalar
     int kind, method, order;  // flux kind (0 upwind, 1 centred), splitting, order
+    int fp32;                 // fluxes computed in float (mixed form)
     int mv, nv;
 };
 int stage_advection(const AdvStage &a, cudaStream_t s);
@@ -108,6 +109,9 @@ struct OrthoStage {
 int stage_ortho(const OrthoStage &a, cudaStream_t s);
 
 int vec_add(double *x, const double *y, size_t count, const int *active, cudaStream_t s);
+int vec_add_f32(double *x, const float *e, size_t count, const int *active, cudaStream_t s);
+int mg_residual_mixed(const LevelView<double> &L, const Analytic &an, const double *x,
+                      const double *b, double *r, float *rf, const int *active, cudaStream_t s);
 int vec_axpy_const(double *x, double alpha_sub, const double *dev_scalar, size_t count,
                    cudaStream_t s);
 

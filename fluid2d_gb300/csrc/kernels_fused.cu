@@ -171,6 +171,10 @@ F2D_DEV bool inactive(const int *active) { return active != nullptr && *active =
 // ------------------------------------------------------------ level kernels
 constexpr int LV_TX = 32, LV_TY = 8;
 
+static inline dim3 lv_grid(int rows, int cols) {
+    return grid2d(rows > 0 ? rows : 1, cols > 0 ? cols : 1, dim3(LV_TX, LV_TY));
+}
+
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY)
 k_sweep1(LevelView<T> L, Analytic an, T c1, T c2, int zero_x, const int *active) {
@@ -202,6 +206,42 @@ k_residual(LevelView<T> L, Analytic an, const T *x, const T *b, T *r, const int 
     store_images(r, j, i, L.mv, L.nv, residual<T, L0>(L, &an, x, b, j, i));
 }
 
+// FP64 residual of the finest level with a float copy (the right-hand side
+// of the FP32 correction cycles of the mixed form)
+__global__ void __launch_bounds__(LV_TX *LV_TY)
+k_residual_mixed(LevelView<double> L, Analytic an, const double *x, const double *b, double *r,
+                 float *rf, const int *active) {
+    if (inactive(active)) return;
+    const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
+    const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
+    if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
+    const double v = residual<double, true>(L, &an, x, b, j, i);
+    store_images(r, j, i, L.mv, L.nv, v);
+    store_images(rf, j, i, L.mv, L.nv, (float)v);
+}
+
+int mg_residual_mixed(const LevelView<double> &L, const Analytic &an, const double *x,
+                      const double *b, double *r, float *rf, const int *active, cudaStream_t s) {
+    dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
+    k_residual_mixed<<<g, bl, 0, s>>>(L, an, x, b, r, rf, active);
+    return launch_status("mg_residual_mixed");
+}
+
+// x (float64) += e (float32), whole array
+__global__ void k_add_f32(double *x, const float *e, size_t n, const int *active) {
+    if (inactive(active)) return;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = x[q] + (double)e[q];
+}
+
+int vec_add_f32(double *x, const float *e, size_t count, const int *active, cudaStream_t s) {
+    int blocks = (int)((count + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_add_f32<<<blocks, 256, 0, s>>>(x, e, count, active);
+    return launch_status("vec_add_f32");
+}
+
 template <typename T>
 __global__ void __launch_bounds__(LV_TX *LV_TY)
 k_restrict(const T *src, int nv1, const int8_t *msk2, int mv2, int nv2, T *dst,
@@ -224,10 +264,6 @@ k_interp(const int8_t *msk1, int mv1, int nv1, const int8_t *msk2, const T *x2, 
     const T v = interp_value(msk1, nv1, msk2, x2, nv2, J1, I1);
     const size_t p = off(J1, I1, nv1);
     dst[p] = assign ? v : dst[p] + v;
-}
-
-static inline dim3 lv_grid(int rows, int cols) {
-    return grid2d(rows > 0 ? rows : 1, cols > 0 ? cols : 1, dim3(LV_TX, LV_TY));
 }
 
 template <typename T>
@@ -439,27 +475,33 @@ F2D_DEV double rk_combine(int rk, double base, double d0, double d1, double dq, 
 
 // Advection of one tracer with the halo fill, the Boussinesq torque and the
 // RK combination fused (core/operators.py:214-236,303-314,
-// core/timescheme.py:167-180).
+// core/timescheme.py:167-180).  TC is the type the fluxes are computed in
+// (double, or float in the mixed form); loads, tendency and RK combination
+// stay float64.
+template <typename TC>
 __global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
-    __shared__ double sfx[8][33];
-    __shared__ double sfy[9][32];
+    __shared__ TC sfx[8][33];
+    __shared__ TC sfy[9][32];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nv = a.nv, mv = a.mv;
     const int I = NH + blockIdx.x * 32 + tx;
     const int J = NH + blockIdx.y * 8 + ty;
     const bool in = (I <= nv - NH - 1) && (J <= mv - NH - 1);
-    const SplitConst c = *(const SplitConst *)a.advc;
+    const SplitT<TC> c = split_cast<TC>(*(const SplitConst *)a.advc);
     if (in) {
         const size_t p = off(J, I, nv);
-        sfx[ty][tx + 1] = edge_flux_rt(a.kind, a.msk, a.q, a.u, p, 1, a.method, a.order, c);
-        sfy[ty + 1][tx] = edge_flux_rt(a.kind, a.msk, a.q, a.v, p, nv, a.method, a.order, c);
-        if (tx == 0) sfx[ty][0] = edge_flux_rt(a.kind, a.msk, a.q, a.u, p - 1, 1, a.method, a.order, c);
-        if (ty == 0) sfy[0][tx] = edge_flux_rt(a.kind, a.msk, a.q, a.v, p - nv, nv, a.method, a.order, c);
+        sfx[ty][tx + 1] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.u, p, 1, a.method, a.order, c);
+        sfy[ty + 1][tx] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.v, p, nv, a.method, a.order, c);
+        if (tx == 0)
+            sfx[ty][0] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.u, p - 1, 1, a.method, a.order, c);
+        if (ty == 0)
+            sfy[0][tx] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.v, p - nv, nv, a.method, a.order, c);
     }
     __syncthreads();
     if (!in) return;
     const size_t p = off(J, I, nv);
-    double y = -(c.zdx * (sfx[ty][tx + 1] - sfx[ty][tx])) - c.zdy * (sfy[ty + 1][tx] - sfy[ty][tx]);
+    TC yc = -(c.zdx * (sfx[ty][tx + 1] - sfx[ty][tx])) - c.zdy * (sfy[ty + 1][tx] - sfy[ty][tx]);
+    double y = (double)yc;
     if (a.buoy) {
         const int mc = a.msk[p];
         y = y * (double)mc;
@@ -489,7 +531,10 @@ __global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
 int stage_advection(const AdvStage &a, cudaStream_t s) {
     dim3 b(32, 8);
     dim3 g = grid2d(a.mv - 2 * NH, a.nv - 2 * NH, b);
-    k_stage_adv<<<g, b, 0, s>>>(a);
+    if (a.fp32)
+        k_stage_adv<float><<<g, b, 0, s>>>(a);
+    else
+        k_stage_adv<double><<<g, b, 0, s>>>(a);
     return launch_status("stage_advection");
 }
 

@@ -45,3 +45,19 @@ def oracle_model(wl, **kw):
     """The oracle stepper model for a workloads.* dict (mask, fields, psi)."""
     from oracle import stepper
     return stepper.from_workload(wl, **kw)
+
+
+def island_workload():
+    """Euler, closed 96x64 box (dx = dy) with two circular islands."""
+    from fluid2d_gb300 import workloads as W
+    wl = W.dipole(96, 64, seed=13)
+    wl["Lx"], wl["Ly"] = 1.5, 1.
+    xr, yr = W.cell_coords(96, 64, 1.5, 1.)
+    msk = W.base_mask(96, 64, "closed")
+    for cx, cy, r in ((0.35, 0.3, 0.08), (1.1, 0.65, 0.1)):
+        msk[(xr - cx) ** 2 + (yr - cy) ** 2 < r * r] = 0
+    wl["msk"] = msk
+    w = (np.exp(-((xr - 0.7) ** 2 + (yr - 0.5) ** 2) / 0.05 ** 2)
+         - np.exp(-((xr - 0.85) ** 2 + (yr - 0.5) ** 2) / 0.05 ** 2))
+    wl["fields"] = {"vorticity": w * msk}
+    return wl

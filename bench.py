@@ -24,6 +24,9 @@ Under torchrun (N > 1) every rank steps an independent replica (the path
 has no data-path collective); value sums the replicas.
 """
 import argparse
+import os as _os
+# independent simulations overlap on up to 32 hardware queues
+_os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import json
 import os
 import statistics
@@ -52,6 +55,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ensemble-steps", type=int, default=20)
+    ap.add_argument("--served-requests", type=int, default=24)
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the ensemble and served-stream measurements")
     return ap.parse_args()
 
 
@@ -301,6 +308,13 @@ def run_ours(a, rank, world, local):
         e2e_ms = float(t.item())
     e2e_val = world * n * n * a.e2e_steps / (e2e_ms * 1e-3)
 
+    extra = {}
+    if not a.no_extra and rank == 0:
+        for key, fn in (("ensemble", bench_ensemble), ("served", bench_served)):
+            try:
+                extra[key] = fn(a)
+            except Exception as exc:
+                print("%s failed: %s" % (key, exc), file=sys.stderr)
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -332,6 +346,8 @@ def run_ours(a, rank, world, local):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": a.e2e_steps},
         "mixed": mixed,
+        "ensemble": extra.get("ensemble"),
+        "served": extra.get("served"),
         "gpu_launches": kernels_per_step * a.steps,
         "clocks": clk.summary(),
         "libraries": [os.path.basename(so_path("product"))],
@@ -381,6 +397,73 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
             "correction, RK accumulation and diagnostics",
             "single_step_rel_l2_vs_f64": err, "solve_iterations_last_step": nite,
             "solve_residual_last_step": res}
+
+
+def bench_ensemble(a):
+    """Config: 96 independent Euler instances (sides log-uniform 64-768,
+    multiples of 64, islands, 3-12 vortices; seed 4).  Batched = every
+    instance's step graph replayed on 32 streams; comparator = the plain
+    float64 path, one instance at a time."""
+    import torch
+    from fluid2d_gb300 import engine, workloads as W
+    wls = W.ensemble(96, seed=4)
+    cells = sum(w["nx"] * w["ny"] for w in wls)
+    out = {"instances": len(wls), "cells": cells, "steps": a.ensemble_steps}
+    for prec in ("mixed", "fp64"):
+        E = engine.ensemble_from_workloads(wls, precision=prec, nstreams=32)
+        E.run(2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        E.run(a.ensemble_steps)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec + "_batched"] = {"cell_steps_per_s": cells * a.ensemble_steps / (ms * 1e-3),
+                                  "ms_per_ensemble_step": ms / a.ensemble_steps}
+        del E
+        torch.cuda.synchronize()
+    # one at a time, plain float64
+    tot_ms = 0.
+    nst = max(2, a.ensemble_steps // 4)
+    s = torch.cuda.Stream()
+    for w in wls:
+        E = engine.ensemble_from_workloads([w], precision="fp64", nstreams=1)
+        m = E.models[0]
+        with torch.cuda.stream(s):
+            m.run(1, graph=True)
+            s.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            m.run(nst, graph=True)
+            e1.record(s)
+            e1.synchronize()
+        tot_ms += e0.elapsed_time(e1) / nst
+        del E, m
+    out["fp64_one_at_a_time"] = {"cell_steps_per_s": cells / (tot_ms * 1e-3),
+                                 "ms_per_ensemble_step": tot_ms, "steps_timed_each": nst}
+    out["mixed_batched_vs_fp64_one_at_a_time"] = (
+        out["mixed_batched"]["cell_steps_per_s"] / out["fp64_one_at_a_time"]["cell_steps_per_s"])
+    return out
+
+
+def bench_served(a):
+    """Config: served stream with Poisson arrivals at 40/s, 70 % Euler /
+    30 % Boussinesq, sides 128-2048 (multiples of 128), HBM budget 150 GB.
+    Bounded sample: the first --served-requests requests, step counts drawn
+    from U[5, 50] (the full stream draws U[50, 500])."""
+    from fluid2d_gb300 import serve, workloads as W
+    stream = W.served_stream(count=a.served_requests, rate=40., seed=5, steps_min=5,
+                             steps_max=50)
+    srv = serve.Server(150e9, precision="mixed", nstreams=32)
+    served = srv.run(stream)
+    alone = serve.run_one_at_a_time(stream, precision="fp64")
+    return {"sample": "%d requests, steps U[5,50], sides 128-2048, 70%% Euler / 30%% "
+                      "Boussinesq, Poisson 40/s, budget 150 GB" % len(stream),
+            "served_mixed_continuous_batching": served,
+            "fp64_one_at_a_time": alone,
+            "throughput_ratio": served["cell_steps_per_s"] / max(1e-300,
+                                                                 alone["cell_steps_per_s"])}
 
 
 def main():

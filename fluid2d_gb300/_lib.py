@@ -21,8 +21,8 @@ CSRC = os.path.join(_HERE, "csrc")
 BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
-           "kernels_fused.cu", "noalloc.cu"]
-HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh"]
+           "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu"]
+HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-fvisibility=hidden"]
@@ -187,6 +187,7 @@ SIGNATURES.update({
     "f2d_model_set_dt": [_P, _D],
     "f2d_model_solve_stats": [_P, _PI, _PDd, _PI],
     "f2d_model_probe": [_P, _I, _PI, _PDd],
+    "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],
 })
 

@@ -23,6 +23,9 @@ void set_error(const char *fmt, ...) {
 int cuda_status(cudaError_t e, const char *where) {
     if (e == cudaSuccess) return OK;
     set_error("%s: %s", where, cudaGetErrorString(e));
+    // clear a non-sticky error so that it is not reported again by the next
+    // launch check of an unrelated kernel
+    cudaGetLastError();
     return ERR_CUDA;
 }
 

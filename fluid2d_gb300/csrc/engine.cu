@@ -20,6 +20,7 @@
 #include "f2d_fused.cuh"
 #include "f2d_kernels.cuh"
 #include "f2d_adv.cuh"
+#include "f2d_mixed.cuh"
 
 namespace f2d {
 
@@ -186,6 +187,9 @@ struct Gmg {
     double omega = 8. / 9.;
     int ndeepest = 16;
     Analytic an{};
+    AnalyticT<float> anf{};
+    template <typename T>
+    const AnalyticT<T> *analytic() const;
     int cs = 1;  // first level of the coarse CTA (== nlev: none)
     size_t smem64 = 0, smem32 = 0;
     Arena mem;
@@ -221,8 +225,10 @@ struct Gmg {
     int fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s);
 };
 
-template <typename T>
-static T cast(double v) { return (T)v; }
+template <>
+const AnalyticT<double> *Gmg::analytic<double>() const { return &an; }
+template <>
+const AnalyticT<float> *Gmg::analytic<float>() const { return &anf; }
 
 int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, double hydroeps,
                double om, bool qg, double Rd, bool f32, cudaStream_t s) {
@@ -330,6 +336,9 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
     an.a5 = sc9[4] * 1. * 1.;
     if (qg) an.a5 -= 1. / (Rd * Rd);
     an.c3 = omega / fabs(an.a5);
+    for (int k = 0; k < 5; k++) anf.sc[k] = (float)an.sc[k];
+    anf.a5 = (float)an.a5;
+    anf.c3 = (float)an.c3;
     TRY(cuda_status(cudaMemcpyAsync(mem.at<double>(o_sc9), sc9, sizeof(sc9),
                                     cudaMemcpyHostToDevice, s),
                     "stencil upload"));
@@ -378,7 +387,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
 
 template <typename T>
 int Gmg::smooth(LevelView<T> *L, int l, bool zero, const int *active, cudaStream_t s) {
-    const Analytic *a0 = l == 0 ? &an : nullptr;
+    const AnalyticT<T> *a0 = l == 0 ? analytic<T>() : nullptr;
     T c1 = (T)omega, c2 = (T)(1. - omega);
     const bool pr = probe && l == 0 && nprobe < MAX_PROBES;
     if (pr) {
@@ -423,7 +432,8 @@ int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cud
     const int stop = cs < deep ? cs : deep;
     for (int l = l1; l < stop; l++) {
         TRY(smooth(L, l, zero_first || l > l1, active, s));
-        TRY(mg_residual<T>(L[l], l == 0 ? &an : nullptr, L[l].x, L[l].b, L[l].r, active, s));
+        TRY(mg_residual<T>(L[l], l == 0 ? analytic<T>() : nullptr, L[l].x, L[l].b, L[l].r, active,
+                           s));
         TRY(mg_restrict<T>(L[l], L[l].r, L[l + 1], L[l + 1].b, active, s));
     }
     if (cs <= deep) {
@@ -717,6 +727,17 @@ struct Model {
     Arena mem;
     int8_t *msk = nullptr, *mskp = nullptr, *ones = nullptr;
     double *X, *D[3], *S1, *S2, *B, *cst, *advc, *dt, *diag, *pvback, *bref, *part;
+    // mixed form: float stage states, float tendencies, float split constants
+    float *Xf = nullptr, *S1f = nullptr, *S2f = nullptr, *Df[3] = {nullptr, nullptr, nullptr};
+    float *dtf = nullptr;
+    void *advf = nullptr;
+    template <typename P>
+    P *planef(P *base, const char *name) {
+        for (int k = 0; k < nvar; k++)
+            if (!strcmp(VARNAMES[kind][k], name)) return base + k * pl;
+        return nullptr;
+    }
+    int stage_mixed(int k, cudaStream_t s);
     int last_nite = 0;
     int probe_per_step = -1;
     cudaGraph_t graph = nullptr;
@@ -775,7 +796,22 @@ int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t 
            o_diag = mem.add(8 * 8),
            o_pvb = mem.add(kind == M_QG ? pl * 8 : 8), o_bref = mem.add(kind == M_BOUSSINESQ ? pl * 8 : 8),
            o_part = mem.add(8 * RED_MAX_BLOCKS * 8);
+    const bool mixed = d->precision != 0;
+    size_t o_f[6] = {0, 0, 0, 0, 0, 0}, o_advf = 0, o_dtf = 0;
+    if (mixed) {
+        for (int k = 0; k < 6; k++) o_f[k] = mem.add(nvar * pl * 4);
+        o_advf = mem.add(sizeof(SplitT<float>));
+        o_dtf = mem.add(16);
+    }
     TRY(mem.alloc());
+    if (mixed) {
+        Xf = mem.at<float>(o_f[0]);
+        S1f = mem.at<float>(o_f[1]);
+        S2f = mem.at<float>(o_f[2]);
+        for (int k = 0; k < 3; k++) Df[k] = mem.at<float>(o_f[3 + k]);
+        advf = mem.at<void>(o_advf);
+        dtf = mem.at<float>(o_dtf);
+    }
     msk = mem.at<int8_t>(o_msk);
     mskp = mem.at<int8_t>(o_mskp);
     ones = mem.at<int8_t>(o_ones);
@@ -933,6 +969,86 @@ int Model::stage(int k, cudaStream_t s) {
     return stage_ortho(o, s);
 }
 
+// One RK3_SSP stage of the mixed form (see kernels_mixed.cu)
+int Model::stage_mixed(int k, cudaStream_t s) {
+    float *xs = k == 0 ? Xf : (k == 1 ? S1f : S2f);
+    float *outf = k == 0 ? S1f : S2f;
+    float *dk = Df[k];
+    const char *tracers[2] = {kind == M_QG ? "pv" : "vorticity", "buoyancy"};
+    const int ntr = kind == M_BOUSSINESQ ? 2 : 1;
+    for (int t = 0; t < ntr; t++) {
+        AdvMixed a;
+        memset(&a, 0, sizeof(a));
+        a.msk = msk;
+        a.q = planef(xs, tracers[t]);
+        a.u = planef(xs, "u");
+        a.v = planef(xs, "v");
+        a.advf = (const SplitT<float> *)advf;
+        a.dtf = dtf;
+        a.dq = planef(dk, tracers[t]);
+        if (kind == M_BOUSSINESQ && t == 0) {
+            a.buoy = planef(xs, "buoyancy");
+            a.torque_coef = (float)(0.5 * desc.gravity / dx);
+        }
+        a.rk = k + 1;
+        a.sbase = planef(Xf, tracers[t]);
+        a.d0 = k >= 1 ? planef(Df[0], tracers[t]) : nullptr;
+        a.d1 = k >= 2 ? planef(Df[1], tracers[t]) : nullptr;
+        a.sout = k < 2 ? planef(outf, tracers[t]) : nullptr;
+        a.xout = k == 2 ? plane(X, tracers[t]) : nullptr;
+        a.kind = (desc.order % 2 == 0) ? 1 : 0;
+        a.method = desc.flux_method;
+        a.order = desc.order;
+        a.mv = mv;
+        a.nv = nv;
+        TRY(stage_advection_mixed(a, s));
+    }
+    const bool inv = (kind == M_BOUSSINESQ) || k < 2;
+    if (!inv) return OK;
+    double *psik = plane(D[k], "psi");
+    if (kind == M_QG) TRY(cuda_status(cudaMemsetAsync(psik, 0, pl * 8, s), "qg warm start"));
+    TRY(c2c_f32(planef(dk, tracers[0]), B, mv, nv, s));
+    TRY(two_vcycle_mixed(gmg, psik, B, s));
+    OrthoMixed o;
+    memset(&o, 0, sizeof(o));
+    o.msk = msk;
+    o.mskp = mskp;
+    o.psi = psik;
+    o.du = planef(dk, "u");
+    o.dv = planef(dk, "v");
+    o.zdx = 1. / dx;
+    o.zdy = 1. / dy;
+    o.rk = k + 1;
+    o.ubase = planef(Xf, "u");
+    o.vbase = planef(Xf, "v");
+    o.u0 = k >= 1 ? planef(Df[0], "u") : nullptr;
+    o.v0 = k >= 1 ? planef(Df[0], "v") : nullptr;
+    o.u1 = k >= 2 ? planef(Df[1], "u") : nullptr;
+    o.v1 = k >= 2 ? planef(Df[1], "v") : nullptr;
+    o.su = k < 2 ? planef(outf, "u") : nullptr;
+    o.sv = k < 2 ? planef(outf, "v") : nullptr;
+    o.xu = k == 2 ? plane(X, "u") : nullptr;
+    o.xv = k == 2 ? plane(X, "v") : nullptr;
+    if (kind != M_BOUSSINESQ && k == 1) {
+        o.psi_rk = 1;
+        o.psibase = plane(X, "psi");
+        o.psi0 = plane(D[0], "psi");
+        o.psi1 = nullptr;
+        o.psiout = plane(X, "psi");
+    } else if (kind == M_BOUSSINESQ && k == 2) {
+        o.psi_rk = 1;
+        o.psibase = plane(X, "psi");
+        o.psi0 = plane(D[0], "psi");
+        o.psi1 = plane(D[1], "psi");
+        o.psiout = plane(X, "psi");
+    }
+    o.dt = dt;
+    o.dtf = dtf;
+    o.mv = mv;
+    o.nv = nv;
+    return stage_ortho_mixed(o, s);
+}
+
 int Model::set_psi(cudaStream_t s) {
     if (kind == M_QG) {
         k_qg_post<<<blocks_for(pl), 256, 0, s>>>(X, pl, pvback, 0., 0);  // pvanom = pv - pvback
@@ -975,7 +1091,13 @@ int Model::step(cudaStream_t s) {
     k_set_dt<<<1, 1, 0, s>>>(dt, cst, (SplitConst *)advc, diag, desc.adaptable_dt, desc.dt,
                              desc.cfl, dx < dy ? dx : dy, desc.dtmax);
     TRY(launch_status("set_dt"));
-    for (int k = 0; k < 3; k++) TRY(stage(k, s));
+    if (desc.precision != 0) {
+        TRY(split_f32(advc, dt, advf, dtf, s));
+        TRY(vec_to_f32(X, Xf, nvar * pl, s));
+        for (int k = 0; k < 3; k++) TRY(stage_mixed(k, s));
+    } else {
+        for (int k = 0; k < 3; k++) TRY(stage(k, s));
+    }
     if (kind == M_BOUSSINESQ) {
         k_banom<<<blocks_for(pl), 256, 0, s>>>(X, pl, bref);
         TRY(launch_status("banom"));
@@ -1037,6 +1159,13 @@ int f2d_model_info(void *model, int *nvar, int *mv, int *nv, int *nlev, int *coa
     if (coarse_level) *coarse_level = M->gmg.cs;
     if (state) *state = M->X;
     if (diag) *diag = M->diag;
+    return OK;
+}
+
+int f2d_model_bytes(void *model, size_t *bytes) {
+    Model *M = (Model *)model;
+    if (!M || !bytes) return ERR_ARG;
+    *bytes = M->mem.total + M->gmg.mem.total;
     return OK;
 }
 

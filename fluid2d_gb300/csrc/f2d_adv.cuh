@@ -126,6 +126,22 @@ F2D_DEV T edge_flux_t(const int8_t *msk, const double *x, const double *vel, siz
     return centered_flux<T>(q, mk, w, order, KIND == 1);
 }
 
+// float32 edge flux from float32 arrays (mixed form)
+F2D_DEV float edge_flux_f32(int kind, const int8_t *msk, const float *x, const float *vel,
+                            size_t p0, ptrdiff_t s, int method, int order,
+                            const SplitT<float> &c) {
+    float q[6];
+    int mk[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) mk[k] = msk[(ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s];
+    if (mk[2] + mk[3] != 2) return 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) q[k] = __ldg(x + (ptrdiff_t)p0 + (ptrdiff_t)(k - 2) * s);
+    const float w = __ldg(vel + p0);
+    if (kind == 0) return upwind_flux<float>(q, mk, w, method, order, c);
+    return centered_flux<float>(q, mk, w, order, kind == 1);
+}
+
 template <int KIND>
 F2D_DEV double edge_flux(const int8_t *msk, const double *x, const double *vel, size_t p0,
                          ptrdiff_t s, int method, int order, const SplitConst &c) {

@@ -25,11 +25,13 @@ struct LevelView {
 // Analytic finest-level operator: A_k(J,I) = sc[k] where msk(J',I') and
 // msk(J'+dj_k, I'+di_k) are fluid, (J',I') the periodic image of (J,I)
 // (the reference fills the halo of A periodically, core/gmg/level.py:297).
-struct Analytic {
-    double sc[5];  // stencil*coef of planes SW, S, SE, W, C
-    double a5;     // A5 on fluid points, after the Helmholtz shift (QG)
-    double c3;     // omega / |a5|
+template <typename T>
+struct AnalyticT {
+    T sc[5];  // stencil*coef of planes SW, S, SE, W, C
+    T a5;     // A5 on fluid points, after the Helmholtz shift (QG)
+    T c3;     // omega / |a5|
 };
+using Analytic = AnalyticT<double>;
 
 enum CycleMode { CYCLE_V = 0, CYCLE_F = 1 };
 
@@ -46,13 +48,13 @@ struct CoarseArgs {
 
 // launchers (kernels_fused.cu)
 template <typename T>
-int mg_sweep1(const LevelView<T> &L, const Analytic *an, T c1, T c2, bool zero_x,
+int mg_sweep1(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, bool zero_x,
               const int *active, cudaStream_t s);
 template <typename T>
-int mg_sweep2(const LevelView<T> &L, const Analytic *an, T c1, T c2, const int *active,
+int mg_sweep2(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, const int *active,
               cudaStream_t s);
 template <typename T>
-int mg_residual(const LevelView<T> &L, const Analytic *an, const T *x, const T *b, T *r,
+int mg_residual(const LevelView<T> &L, const AnalyticT<T> *an, const T *x, const T *b, T *r,
                 const int *active, cudaStream_t s);
 template <typename T>
 int mg_restrict(const LevelView<T> &fine, const T *src, const LevelView<T> &coarse, T *dst,

@@ -27,19 +27,33 @@ __constant__ int c_dj[5] = {-1, -1, -1, 0, 0};
 __constant__ int c_di[5] = {-1, 0, 1, -1, 0};
 
 template <typename T>
-F2D_DEV T analytic_coef(const LevelView<T> &L, const Analytic &an, int k, int J, int I) {
+F2D_DEV T analytic_coef(const LevelView<T> &L, const AnalyticT<T> &an, int k, int J, int I) {
     const int Jw = wrap(J, L.mv, NH), Iw = wrap(I, L.nv, NH);
     const size_t pc = off(Jw, Iw, L.nv);
     if (L.msk[pc] == 0) return (T)0;
     if (L.msk[off(Jw + c_dj[k], Iw + c_di[k], L.nv)] == 0) return (T)0;
-    return (T)(k == 4 ? an.a5 : an.sc[k]);
+    return k == 4 ? an.a5 : an.sc[k];
 }
 
 // the 8 off-diagonal coefficients of point (j, i) in the reference's order
 // A1(j,i) A2(j,i) A3(j,i) A4(j,i) A4(j,i+1) A3(j+1,i-1) A2(j+1,i) A1(j+1,i+1)
+// For the analytic finest level, the caller guarantees msk(j,i) != 0.  Away
+// from the halo no coefficient position needs its periodic image, and each
+// coefficient is sc[k] where its neighbour cell is fluid.
 template <typename T, bool L0>
-F2D_DEV void offdiag(const LevelView<T> &L, const Analytic *an, int j, int i, T (&a)[8]) {
-    if (L0) {
+F2D_DEV void offdiag(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T (&a)[8]) {
+    if (L0 && j >= NH && j <= L.mv - NH - 2 && i >= NH + 1 && i <= L.nv - NH - 2) {
+        const int nv = L.nv;
+        const int8_t *m = L.msk + off(j, i, nv);
+        a[0] = m[-nv - 1] ? an->sc[0] : (T)0;
+        a[1] = m[-nv] ? an->sc[1] : (T)0;
+        a[2] = m[-nv + 1] ? an->sc[2] : (T)0;
+        a[3] = m[-1] ? an->sc[3] : (T)0;
+        a[4] = m[1] ? an->sc[3] : (T)0;
+        a[5] = m[nv - 1] ? an->sc[2] : (T)0;
+        a[6] = m[nv] ? an->sc[1] : (T)0;
+        a[7] = m[nv + 1] ? an->sc[0] : (T)0;
+    } else if (L0) {
         a[0] = analytic_coef(L, *an, 0, j, i);
         a[1] = analytic_coef(L, *an, 1, j, i);
         a[2] = analytic_coef(L, *an, 2, j, i);
@@ -64,23 +78,23 @@ F2D_DEV void offdiag(const LevelView<T> &L, const Analytic *an, int j, int i, T 
 }
 
 template <typename T, bool L0>
-F2D_DEV T diag_coef(const LevelView<T> &L, const Analytic *an, int j, int i) {
+F2D_DEV T diag_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i) {
     if (L0) return analytic_coef(L, *an, 4, j, i);
     return L.A[4 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
 }
 
 template <typename T, bool L0>
-F2D_DEV T c3_coef(const LevelView<T> &L, const Analytic *an, int j, int i, T c1) {
+F2D_DEV T c3_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T c1) {
     if (L0) {
         T a5 = analytic_coef(L, *an, 4, j, i);
-        return a5 != (T)0 ? (T)an->c3 : c1 / fabs(a5);
+        return a5 != (T)0 ? an->c3 : c1 / fabs(a5);
     }
     return L.A[5 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
 }
 
 // damped Jacobi (core/gmg/fortran_multigrid.f90:66-85); q == null: x = 0
 template <typename T, bool L0>
-F2D_DEV T jacobi(const LevelView<T> &L, const Analytic *an, const T *q, const T *b, int j,
+F2D_DEV T jacobi(const LevelView<T> &L, const AnalyticT<T> *an, const T *q, const T *b, int j,
                  int i, T c1, T c2) {
     const int nv = L.nv;
     const size_t p = off(j, i, nv);
@@ -102,7 +116,7 @@ F2D_DEV T jacobi(const LevelView<T> &L, const Analytic *an, const T *q, const T 
 
 // r = b - A x (core/gmg/fortran_multigrid.f90:340-357)
 template <typename T, bool L0>
-F2D_DEV T residual(const LevelView<T> &L, const Analytic *an, const T *x, const T *b, int j,
+F2D_DEV T residual(const LevelView<T> &L, const AnalyticT<T> *an, const T *x, const T *b, int j,
                    int i) {
     const int nv = L.nv;
     const size_t p = off(j, i, nv);
@@ -177,7 +191,7 @@ static inline dim3 lv_grid(int rows, int cols) {
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY)
-k_sweep1(LevelView<T> L, Analytic an, T c1, T c2, int zero_x, const int *active) {
+k_sweep1(LevelView<T> L, AnalyticT<T> an, T c1, T c2, int zero_x, const int *active) {
     if (inactive(active)) return;
     const int i = 2 + blockIdx.x * LV_TX + threadIdx.x;
     const int j = 2 + blockIdx.y * LV_TY + threadIdx.y;
@@ -187,7 +201,7 @@ k_sweep1(LevelView<T> L, Analytic an, T c1, T c2, int zero_x, const int *active)
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY)
-k_sweep2(LevelView<T> L, Analytic an, T c1, T c2, const int *active) {
+k_sweep2(LevelView<T> L, AnalyticT<T> an, T c1, T c2, const int *active) {
     if (inactive(active)) return;
     const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
     const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
@@ -198,7 +212,7 @@ k_sweep2(LevelView<T> L, Analytic an, T c1, T c2, const int *active) {
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY)
-k_residual(LevelView<T> L, Analytic an, const T *x, const T *b, T *r, const int *active) {
+k_residual(LevelView<T> L, AnalyticT<T> an, const T *x, const T *b, T *r, const int *active) {
     if (inactive(active)) return;
     const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
     const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
@@ -267,35 +281,35 @@ k_interp(const int8_t *msk1, int mv1, int nv1, const int8_t *msk2, const T *x2, 
 }
 
 template <typename T>
-int mg_sweep1(const LevelView<T> &L, const Analytic *an, T c1, T c2, bool zero_x,
+int mg_sweep1(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, bool zero_x,
               const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 4, L.nv - 4), b(LV_TX, LV_TY);
     if (an)
         k_sweep1<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, zero_x, active);
     else
-        k_sweep1<T, false><<<g, b, 0, s>>>(L, Analytic{}, c1, c2, zero_x, active);
+        k_sweep1<T, false><<<g, b, 0, s>>>(L, AnalyticT<T>{}, c1, c2, zero_x, active);
     return launch_status("mg_sweep1");
 }
 
 template <typename T>
-int mg_sweep2(const LevelView<T> &L, const Analytic *an, T c1, T c2, const int *active,
+int mg_sweep2(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, const int *active,
               cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), b(LV_TX, LV_TY);
     if (an)
         k_sweep2<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, active);
     else
-        k_sweep2<T, false><<<g, b, 0, s>>>(L, Analytic{}, c1, c2, active);
+        k_sweep2<T, false><<<g, b, 0, s>>>(L, AnalyticT<T>{}, c1, c2, active);
     return launch_status("mg_sweep2");
 }
 
 template <typename T>
-int mg_residual(const LevelView<T> &L, const Analytic *an, const T *x, const T *b, T *r,
+int mg_residual(const LevelView<T> &L, const AnalyticT<T> *an, const T *x, const T *b, T *r,
                 const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
     if (an)
         k_residual<T, true><<<g, bl, 0, s>>>(L, *an, x, b, r, active);
     else
-        k_residual<T, false><<<g, bl, 0, s>>>(L, Analytic{}, x, b, r, active);
+        k_residual<T, false><<<g, bl, 0, s>>>(L, AnalyticT<T>{}, x, b, r, active);
     return launch_status("mg_residual");
 }
 
@@ -319,8 +333,13 @@ int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine
 // ------------------------------------------------------------ coarse CTA
 // All levels below a size threshold are processed by one CTA out of shared
 // memory: the recursion of core/gmg/hierarchy.py:98-151 runs as a sequence
-// of block-wide phases separated by __syncthreads().
-constexpr int CO_THREADS = 1024;
+// of block-wide phases separated by __syncthreads().  Each level's arrays
+// are addressed from a descriptor table in shared memory, so every access
+// compiles to a shared-memory access; threads cover a level in 32 x 32
+// blocks of (row, column).
+constexpr int CO_TX = 32, CO_TY = 32;
+constexpr int COARSE_SMEM_MAX = 220 * 1024;
+constexpr int CO_THREADS = CO_TX * CO_TY;
 
 F2D_HD size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
 
@@ -334,67 +353,83 @@ size_t coarse_smem_bytes(const int *mv, const int *nv, int nlev) {
     return tot;
 }
 
+struct CoLv {
+    int mv, nv;
+    unsigned o_msk, o_A, o_x, o_b, o_r, o_t;
+};
+
 template <typename T>
-F2D_DEV void co_smooth(const LevelView<T> &L, T c1, T c2, bool zero_x) {
-    const int w1 = L.nv - 4, h1 = L.mv - 4;
-    for (int q = threadIdx.x; q < w1 * h1; q += blockDim.x) {
-        int j = 2 + q / w1, i = 2 + q % w1;
-        L.t[off(j, i, L.nv)] = jacobi<T, false>(L, nullptr, zero_x ? nullptr : L.x, L.b, j, i,
-                                                c1, c2);
-    }
+F2D_DEV LevelView<T> co_view(unsigned char *sm, const CoLv &d) {
+    LevelView<T> L;
+    L.mv = d.mv;
+    L.nv = d.nv;
+    L.msk = (const int8_t *)(sm + d.o_msk);
+    L.A = (const T *)(sm + d.o_A);
+    L.x = (T *)(sm + d.o_x);
+    L.b = (T *)(sm + d.o_b);
+    L.r = (T *)(sm + d.o_r);
+    L.t = (T *)(sm + d.o_t);
+    return L;
+}
+
+template <typename T>
+F2D_DEV void co_smooth(unsigned char *sm, const CoLv &d, T c1, T c2, bool zero_x) {
+    const LevelView<T> L = co_view<T>(sm, d);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int j = 2 + ty; j <= L.mv - 3; j += CO_TY)
+        for (int i = 2 + tx; i <= L.nv - 3; i += CO_TX)
+            L.t[off(j, i, L.nv)] = jacobi<T, false>(L, nullptr, zero_x ? nullptr : L.x, L.b, j, i,
+                                                    c1, c2);
     __syncthreads();
-    const int w2 = L.nv - 2 * NH, h2 = L.mv - 2 * NH;
-    for (int q = threadIdx.x; q < w2 * h2; q += blockDim.x) {
-        int j = NH + q / w2, i = NH + q % w2;
-        store_images(L.x, j, i, L.mv, L.nv, jacobi<T, false>(L, nullptr, L.t, L.b, j, i, c1, c2));
-    }
+    for (int j = NH + ty; j <= L.mv - NH - 1; j += CO_TY)
+        for (int i = NH + tx; i <= L.nv - NH - 1; i += CO_TX)
+            store_images(L.x, j, i, L.mv, L.nv, jacobi<T, false>(L, nullptr, L.t, L.b, j, i, c1, c2));
     __syncthreads();
 }
 
 template <typename T>
-F2D_DEV void co_residual(const LevelView<T> &L) {
-    const int w = L.nv - 2 * NH, h = L.mv - 2 * NH;
-    for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
-        int j = NH + q / w, i = NH + q % w;
-        store_images(L.r, j, i, L.mv, L.nv, residual<T, false>(L, nullptr, L.x, L.b, j, i));
-    }
+F2D_DEV void co_residual(unsigned char *sm, const CoLv &d) {
+    const LevelView<T> L = co_view<T>(sm, d);
+    for (int j = NH + threadIdx.y; j <= L.mv - NH - 1; j += CO_TY)
+        for (int i = NH + threadIdx.x; i <= L.nv - NH - 1; i += CO_TX)
+            store_images(L.r, j, i, L.mv, L.nv, residual<T, false>(L, nullptr, L.x, L.b, j, i));
     __syncthreads();
 }
 
 template <typename T>
-F2D_DEV void co_restrict(const LevelView<T> &F, const T *src, const LevelView<T> &Cl, T *dst) {
-    const int w = Cl.nv - 2 * NH, h = Cl.mv - 2 * NH;
-    for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
-        int j = NH + q / w, i = NH + q % w;
-        store_images(dst, j, i, Cl.mv, Cl.nv, restrict_value(Cl.msk, Cl.nv, src, F.nv, j, i));
-    }
+F2D_DEV void co_restrict(unsigned char *sm, const CoLv &df, bool from_b, const CoLv &dc) {
+    const LevelView<T> F = co_view<T>(sm, df), Cl = co_view<T>(sm, dc);
+    const T *src = from_b ? F.b : F.r;
+    for (int j = NH + threadIdx.y; j <= Cl.mv - NH - 1; j += CO_TY)
+        for (int i = NH + threadIdx.x; i <= Cl.nv - NH - 1; i += CO_TX)
+            store_images(Cl.b, j, i, Cl.mv, Cl.nv, restrict_value(Cl.msk, Cl.nv, src, F.nv, j, i));
     __syncthreads();
 }
 
 template <typename T>
-F2D_DEV void co_interp(const LevelView<T> &Cl, const LevelView<T> &F, bool assign) {
-    const int w = F.nv - 2, h = F.mv - 2;
-    for (int q = threadIdx.x; q < w * h; q += blockDim.x) {
-        int j = 1 + q / w, i = 1 + q % w;
-        T v = interp_value(F.msk, F.nv, Cl.msk, Cl.x, Cl.nv, j, i);
-        size_t p = off(j, i, F.nv);
-        F.x[p] = assign ? v : F.x[p] + v;
-    }
+F2D_DEV void co_interp(unsigned char *sm, const CoLv &dc, const CoLv &df, bool assign) {
+    const LevelView<T> Cl = co_view<T>(sm, dc), F = co_view<T>(sm, df);
+    for (int j = 1 + threadIdx.y; j <= F.mv - 2; j += CO_TY)
+        for (int i = 1 + threadIdx.x; i <= F.nv - 2; i += CO_TX) {
+            T v = interp_value(F.msk, F.nv, Cl.msk, Cl.x, Cl.nv, j, i);
+            size_t p = off(j, i, F.nv);
+            F.x[p] = assign ? v : F.x[p] + v;
+        }
     __syncthreads();
 }
 
 template <typename T>
-F2D_DEV void co_vcycle(const LevelView<T> *lev, int l1, int deep, bool zero_first, T c1, T c2,
-                       int ndeepest) {
+F2D_DEV void co_vcycle(unsigned char *sm, const CoLv *lv, int l1, int deep, bool zero_first,
+                       T c1, T c2, int ndeepest) {
     for (int l = l1; l < deep; l++) {
-        co_smooth(lev[l], c1, c2, zero_first || l > l1);
-        co_residual(lev[l]);
-        co_restrict(lev[l], lev[l].r, lev[l + 1], lev[l + 1].b);
+        co_smooth<T>(sm, lv[l], c1, c2, zero_first || l > l1);
+        co_residual<T>(sm, lv[l]);
+        co_restrict<T>(sm, lv[l], false, lv[l + 1]);
     }
-    for (int k = 0; k < ndeepest; k++) co_smooth(lev[deep], c1, c2, k == 0);
+    for (int k = 0; k < ndeepest; k++) co_smooth<T>(sm, lv[deep], c1, c2, k == 0);
     for (int l = deep - 1; l >= l1; l--) {
-        co_interp(lev[l + 1], lev[l], false);
-        co_smooth(lev[l], c1, c2, false);
+        co_interp<T>(sm, lv[l + 1], lv[l], false);
+        co_smooth<T>(sm, lv[l], c1, c2, false);
     }
 }
 
@@ -402,46 +437,54 @@ template <typename T>
 __global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
     if (inactive(a.active)) return;
     extern __shared__ __align__(16) unsigned char sm[];
-    LevelView<T> lev[MAX_LEVELS];
-    size_t o = 0;
+    __shared__ CoLv lv[MAX_LEVELS];
+    const int tid = threadIdx.y * CO_TX + threadIdx.x;
+    if (tid == 0) {
+        unsigned o = 0;
+        for (int l = 0; l < a.nlev; l++) {
+            const unsigned pts = (unsigned)(a.lev[l].mv * a.lev[l].nv);
+            CoLv d;
+            d.mv = a.lev[l].mv;
+            d.nv = a.lev[l].nv;
+            d.o_msk = o;
+            o += (unsigned)align16(pts);
+            d.o_A = o;
+            d.o_x = o + 6 * pts * sizeof(T);
+            d.o_b = o + 7 * pts * sizeof(T);
+            d.o_r = o + 8 * pts * sizeof(T);
+            d.o_t = o + 9 * pts * sizeof(T);
+            o += (unsigned)align16(sizeof(T) * pts * 10);
+            lv[l] = d;
+        }
+    }
+    __syncthreads();
     for (int l = 0; l < a.nlev; l++) {
         const LevelView<T> &g = a.lev[l];
-        const size_t pts = (size_t)g.mv * g.nv;
-        LevelView<T> s = g;
-        int8_t *msk = (int8_t *)(sm + o);
-        o += align16(pts);
-        T *base = (T *)(sm + o);
-        o += align16(sizeof(T) * pts * 10);
-        s.msk = msk;
-        s.A = base;
-        s.x = base + 6 * pts;
-        s.b = base + 7 * pts;
-        s.r = base + 8 * pts;
-        s.t = base + 9 * pts;
-        for (size_t q = threadIdx.x; q < pts; q += blockDim.x) msk[q] = g.msk[q];
-        for (size_t q = threadIdx.x; q < 6 * pts; q += blockDim.x) ((T *)s.A)[q] = g.A[q];
-        if (l == 0) {
-            for (size_t q = threadIdx.x; q < pts; q += blockDim.x) {
+        const LevelView<T> s = co_view<T>(sm, lv[l]);
+        const int pts = g.mv * g.nv;
+        for (int q = tid; q < pts; q += CO_THREADS) ((int8_t *)s.msk)[q] = g.msk[q];
+        for (int q = tid; q < 6 * pts; q += CO_THREADS) ((T *)s.A)[q] = g.A[q];
+        if (l == 0)
+            for (int q = tid; q < pts; q += CO_THREADS) {
                 s.b[q] = g.b[q];
                 s.x[q] = (a.mode == CYCLE_V && !a.zero_first) ? g.x[q] : (T)0;
             }
-        }
-        lev[l] = s;
     }
     __syncthreads();
     const int deep = a.nlev - 1;
     if (a.mode == CYCLE_V) {
-        co_vcycle(lev, 0, deep, a.zero_first != 0, a.c1, a.c2, a.ndeepest);
+        co_vcycle<T>(sm, lv, 0, deep, a.zero_first != 0, a.c1, a.c2, a.ndeepest);
     } else {
-        for (int l = 0; l < deep; l++) co_restrict(lev[l], lev[l].b, lev[l + 1], lev[l + 1].b);
-        for (int k = 0; k < a.ndeepest; k++) co_smooth(lev[deep], a.c1, a.c2, k == 0);
+        for (int l = 0; l < deep; l++) co_restrict<T>(sm, lv[l], true, lv[l + 1]);
+        for (int k = 0; k < a.ndeepest; k++) co_smooth<T>(sm, lv[deep], a.c1, a.c2, k == 0);
         for (int l = deep - 1; l >= 0; l--) {
-            co_interp(lev[l + 1], lev[l], true);
-            co_vcycle(lev, l, deep, false, a.c1, a.c2, a.ndeepest);
+            co_interp<T>(sm, lv[l + 1], lv[l], true);
+            co_vcycle<T>(sm, lv, l, deep, false, a.c1, a.c2, a.ndeepest);
         }
     }
-    const size_t pts0 = (size_t)lev[0].mv * lev[0].nv;
-    for (size_t q = threadIdx.x; q < pts0; q += blockDim.x) a.lev[0].x[q] = lev[0].x[q];
+    const LevelView<T> s0 = co_view<T>(sm, lv[0]);
+    const int pts0 = a.lev[0].mv * a.lev[0].nv;
+    for (int q = tid; q < pts0; q += CO_THREADS) a.lev[0].x[q] = s0.x[q];
 }
 
 namespace {
@@ -455,14 +498,15 @@ int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s) {
     int st = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
     if (st) return st;
     if (dev < 0 || dev >= 64 || !g_coarse_configured[idx][dev]) {
+        // 227 KB per CTA minus the kernel's static shared memory (the level table)
         st = cuda_status(cudaFuncSetAttribute(k_coarse<T>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              227 * 1024),
+                                              COARSE_SMEM_MAX),
                          "coarse smem attribute");
         if (st) return st;
         if (dev >= 0 && dev < 64) g_coarse_configured[idx][dev] = true;
     }
-    k_coarse<T><<<1, CO_THREADS, smem, s>>>(args);
+    k_coarse<T><<<1, dim3(CO_TX, CO_TY), smem, s>>>(args);
     return launch_status("mg_coarse");
 }
 
@@ -609,11 +653,11 @@ int vec_axpy_const(double *x, double area, const double *sum, size_t count, cuda
 
 // explicit instantiations
 #define F2D_INST(T)                                                                              \
-    template int mg_sweep1<T>(const LevelView<T> &, const Analytic *, T, T, bool, const int *,   \
+    template int mg_sweep1<T>(const LevelView<T> &, const AnalyticT<T> *, T, T, bool,            \
+                              const int *, cudaStream_t);                                        \
+    template int mg_sweep2<T>(const LevelView<T> &, const AnalyticT<T> *, T, T, const int *,     \
                               cudaStream_t);                                                     \
-    template int mg_sweep2<T>(const LevelView<T> &, const Analytic *, T, T, const int *,         \
-                              cudaStream_t);                                                     \
-    template int mg_residual<T>(const LevelView<T> &, const Analytic *, const T *, const T *,    \
+    template int mg_residual<T>(const LevelView<T> &, const AnalyticT<T> *, const T *, const T *, \
                                 T *, const int *, cudaStream_t);                                 \
     template int mg_restrict<T>(const LevelView<T> &, const T *, const LevelView<T> &, T *,      \
                                 const int *, cudaStream_t);                                      \

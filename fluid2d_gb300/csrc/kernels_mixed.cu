@@ -1,0 +1,169 @@
+// kernels_mixed.cu -- stage kernels of the mixed-precision form.
+//
+// The mixed form keeps the state, the psi tendencies (the multigrid warm
+// starts), the RK accumulation of the state and the diagnostics in float64,
+// and everything else in float32: the stage states read by the advection,
+// the tracer and velocity tendencies, the fluxes.  On GB300 a conversion
+// between float64 and float32 runs on the same narrow pipe as float64
+// arithmetic, so these kernels read and write float32 wherever the value is
+// consumed in float32 and convert once per value, not once per use.
+//
+// Same update formulas as core/timescheme.py:167-180 (RK3_SSP),
+// core/operators.py:214-236, 303-314, 421-498; only the precision differs.
+#include "f2d_adv.cuh"
+#include "f2d_common.cuh"
+#include "f2d_fused.cuh"
+#include "f2d_kernels.cuh"
+#include "f2d_mixed.cuh"
+
+namespace f2d {
+
+// float copies of the planes the advection reads (tracers, u, v)
+__global__ void k_to_f32(const double *x, float *y, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        y[q] = (float)x[q];
+}
+
+int vec_to_f32(const double *x, float *y, size_t n, cudaStream_t s) {
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    k_to_f32<<<blocks, 256, 0, s>>>(x, y, n);
+    return launch_status("to_f32");
+}
+
+// celltocorner of a float tendency into the float64 right-hand side
+// (core/fortran_operators.f90:58-62, rows/cols 0..m-2)
+__global__ void k_c2c_f32(const float *xr, double *xp, int m, int n) {
+    int i = blockIdx.x * 32 + threadIdx.x;
+    int j = blockIdx.y * 8 + threadIdx.y;
+    if (i > n - 2 || j > m - 2) return;
+    size_t p = off(j, i, n);
+    xp[p] = (double)(0.25f * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]));
+}
+
+int c2c_f32(const float *xr, double *xp, int m, int n, cudaStream_t s) {
+    dim3 b(32, 8);
+    k_c2c_f32<<<grid2d(m - 1, n - 1, b), b, 0, s>>>(xr, xp, m, n);
+    return launch_status("c2c_f32");
+}
+
+// float RK combinations of the stage states (core/timescheme.py:172-176)
+F2D_DEV float rk_stage_f32(int rk, float base, float d0, float dq, float dt) {
+    if (rk == 1) return base + dt * dq;
+    return base + (0.25f * dt) * (d0 + dq);
+}
+
+// Advection of one tracer, float32 fluxes from float32 stage states.
+// rk 1, 2: next stage state (float); rk 3: final float64 accumulation
+// x += (dt/6)*(dx0 + dx1 + 4*dx2) of the state.
+__global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
+    __shared__ float sfx[8][33];
+    __shared__ float sfy[9][32];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int nv = a.nv, mv = a.mv;
+    const int I = NH + blockIdx.x * 32 + tx;
+    const int J = NH + blockIdx.y * 8 + ty;
+    const bool in = (I <= nv - NH - 1) && (J <= mv - NH - 1);
+    const SplitT<float> c = *a.advf;
+    if (in) {
+        const size_t p = off(J, I, nv);
+        sfx[ty][tx + 1] = edge_flux_f32(a.kind, a.msk, a.q, a.u, p, 1, a.method, a.order, c);
+        sfy[ty + 1][tx] = edge_flux_f32(a.kind, a.msk, a.q, a.v, p, nv, a.method, a.order, c);
+        if (tx == 0)
+            sfx[ty][0] = edge_flux_f32(a.kind, a.msk, a.q, a.u, p - 1, 1, a.method, a.order, c);
+        if (ty == 0)
+            sfy[0][tx] = edge_flux_f32(a.kind, a.msk, a.q, a.v, p - nv, nv, a.method, a.order, c);
+    }
+    __syncthreads();
+    if (!in) return;
+    const size_t p = off(J, I, nv);
+    float y = -(c.zdx * (sfx[ty][tx + 1] - sfx[ty][tx])) - c.zdy * (sfy[ty + 1][tx] - sfy[ty][tx]);
+    if (a.buoy) {  // rhs_torque (core/operators.py:311-312)
+        const int mc = a.msk[p];
+        y = mc ? y : 0.f;
+        const int sl = mc + a.msk[p - 1], sr = a.msk[p + 1] + mc;
+        const int ml = sl > 1 ? sl : 1, mr = sr > 1 ? sr : 1;
+        if (ml + mr == 4) y = y + (a.buoy[p + 1] - a.buoy[p - 1]) * a.torque_coef;
+    }
+    const float dt = a.dtf[0];
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    int rows[3], cols[3], nr = 0, nc = 0;
+    rows[nr++] = J;
+    if (J >= m2 && J < m2 + NH) rows[nr++] = J - m2;
+    if (J >= NH && J < 2 * NH) rows[nr++] = J + m2;
+    cols[nc++] = I;
+    if (I >= n2 && I < n2 + NH) cols[nc++] = I - n2;
+    if (I >= NH && I < 2 * NH) cols[nc++] = I + n2;
+    for (int r = 0; r < nr; r++)
+        for (int k = 0; k < nc; k++) {
+            const size_t q = off(rows[r], cols[k], nv);
+            a.dq[q] = y;
+            if (a.rk < 3) {
+                a.sout[q] = rk_stage_f32(a.rk, a.sbase[q], a.d0 ? a.d0[q] : 0.f, y, dt);
+            } else {
+                const float inc = (dt / 6.f) * (a.d0[q] + a.d1[q] + 4.f * y);
+                a.xout[q] = a.xout[q] + (double)inc;
+            }
+        }
+}
+
+int stage_advection_mixed(const AdvMixed &a, cudaStream_t s) {
+    dim3 b(32, 8);
+    k_stage_adv_mixed<<<grid2d(a.mv - 2 * NH, a.nv - 2 * NH, b), b, 0, s>>>(a);
+    return launch_status("stage_advection_mixed");
+}
+
+// psi <- psi*mskp (float64, whole array), u, v = orthogradient(psi) in float64
+// (the differences of psi need it) stored as float tendencies, and the
+// stage-state / final combinations.
+__global__ void __launch_bounds__(256) k_stage_ortho_mixed(OrthoMixed a) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int nv = a.nv, mv = a.mv;
+    if (i >= nv || j >= mv) return;
+    const size_t p = off(j, i, nv);
+    const double pc = a.mskp[p] ? a.psi[p] : 0.;
+    a.psi[p] = pc;
+    if (a.psi_rk) {
+        const double dt = *a.dt;
+        const double d1 = a.psi1 ? a.psi1[p] : pc;
+        const double d2 = a.psi1 ? pc : 0.;
+        a.psiout[p] = a.psibase[p] + (dt / 6.) * (a.psi0[p] + d1 + 4 * d2);
+    }
+    if (i < 1 || j < 1 || i > nv - 2 || j > mv - 2) return;
+    const double ps = a.mskp[p - nv] ? a.psi[p - nv] : 0.;
+    const double pw = a.mskp[p - 1] ? a.psi[p - 1] : 0.;
+    const int mc = a.msk[p];
+    const float u = (mc + a.msk[p + 1] == 2) ? (float)(a.zdy * (ps - pc)) : 0.f;
+    const float v = (mc + a.msk[p + nv] == 2) ? (float)(a.zdx * (pc - pw)) : 0.f;
+    a.du[p] = u;
+    a.dv[p] = v;
+    const float dt = a.dtf[0];
+    if (a.rk == 1 || a.rk == 2) {
+        a.su[p] = rk_stage_f32(a.rk, a.ubase[p], a.u0 ? a.u0[p] : 0.f, u, dt);
+        a.sv[p] = rk_stage_f32(a.rk, a.vbase[p], a.v0 ? a.v0[p] : 0.f, v, dt);
+    } else if (a.rk == 3) {
+        a.xu[p] = a.xu[p] + (double)((dt / 6.f) * (a.u0[p] + a.u1[p] + 4.f * u));
+        a.xv[p] = a.xv[p] + (double)((dt / 6.f) * (a.v0[p] + a.v1[p] + 4.f * v));
+    }
+}
+
+int stage_ortho_mixed(const OrthoMixed &a, cudaStream_t s) {
+    dim3 b(32, 8);
+    k_stage_ortho_mixed<<<grid2d(a.mv, a.nv, b), b, 0, s>>>(a);
+    return launch_status("stage_ortho_mixed");
+}
+
+// float32 split constants and dt (set once per step, after set_dt)
+__global__ void k_split_f32(const SplitConst *c, const double *dt, SplitT<float> *cf, float *dtf) {
+    *cf = split_cast<float>(*c);
+    *dtf = (float)*dt;
+}
+
+int split_f32(const double *advc, const double *dt, void *advf, float *dtf, cudaStream_t s) {
+    k_split_f32<<<1, 1, 0, s>>>((const SplitConst *)advc, dt, (SplitT<float> *)advf, dtf);
+    return launch_status("split_f32");
+}
+
+}  // namespace f2d

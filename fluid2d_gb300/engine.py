@@ -225,6 +225,16 @@ class Model(object):
         self._call("f2d_model_graph_kernels", self.h, ctypes.byref(n))
         return n.value
 
+    def nbytes(self):
+        """Device memory held by the model."""
+        b = ctypes.c_size_t()
+        self._call("f2d_model_bytes", self.h, ctypes.byref(b))
+        return b.value
+
+    @property
+    def cells(self):
+        return self.desc.nx * self.desc.ny
+
     def solve_stats(self):
         nite, res, st = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
         self._call("f2d_model_solve_stats", self.h, ctypes.byref(nite), ctypes.byref(res),
@@ -247,3 +257,58 @@ def from_workload(wl, variant="product", precision="fp64", **kw):
     for name, f in wl["fields"].items():
         m.get(name).copy_(torch.from_numpy(np.ascontiguousarray(f)).cuda())
     return m
+
+
+class Ensemble(object):
+    """Independent simulations advanced together on one GPU.
+
+    Every instance keeps its own device state and captured step graph; the
+    graphs are replayed on `nstreams` CUDA streams (instance i on stream
+    i mod nstreams), so the many small, latency-bound kernels of different
+    instances overlap on the device.  Instances never share data, so each one
+    evolves exactly as it would alone.  For more than 8 concurrent streams set
+    CUDA_DEVICE_MAX_CONNECTIONS (up to 32) before CUDA is initialised.
+    """
+
+    def __init__(self, models, nstreams=32):
+        self.models = list(models)
+        self.streams = [torch.cuda.Stream() for _ in range(max(1, nstreams))]
+
+    @property
+    def cells(self):
+        return sum(m.cells for m in self.models)
+
+    def run(self, nsteps, lockstep=False):
+        """Advance every instance by nsteps (asynchronous)."""
+        cur = torch.cuda.current_stream()
+        for s in self.streams:
+            s.wait_stream(cur)
+        if lockstep:
+            for _ in range(nsteps):
+                for i, m in enumerate(self.models):
+                    with torch.cuda.stream(self.streams[i % len(self.streams)]):
+                        m.run(1, graph=True)
+        else:
+            for i, m in enumerate(self.models):
+                with torch.cuda.stream(self.streams[i % len(self.streams)]):
+                    m.run(nsteps, graph=True)
+        for s in self.streams:
+            cur.wait_stream(s)
+
+    def capture(self):
+        """Capture every instance's step graph (one step each)."""
+        self.run(1)
+
+
+def ensemble_from_workloads(wls, precision="fp64", variant="product", nstreams=32, **kw):
+    """An Ensemble of initialised models (psi set, diagnostics, fixed dt from
+    CFL 0.8 on each instance's initial max|u|)."""
+    models = []
+    for wl in wls:
+        m = from_workload(wl, precision=precision, variant=variant, **kw)
+        m.set_psi_from_vorticity()
+        d = m.diagnostics()
+        if d["maxspeed"] > 0:
+            m.set_dt(0.8 * min(m.dx, m.dy) / d["maxspeed"])
+        models.append(m)
+    return Ensemble(models, nstreams=nstreams)

@@ -124,3 +124,81 @@ def ensemble_member(rng, nmin=64, nmax=768, step=64):
 def ensemble(count=96, seed=4, **kw):
     rng = np.random.default_rng(seed)
     return [ensemble_member(rng, **kw) for _ in range(count)]
+
+
+def served_request(rng, euler_fraction=0.7, side_min=128, side_max=2048, step=128,
+                   steps_min=50, steps_max=500):
+    """One request of the served stream: 70 % Euler / 30 % Boussinesq, sides
+    log-uniform in [side_min, side_max] rounded to multiples of `step`
+    (dx = dy), island masks and initial fields from the request's own seed
+    as in the ensemble (Euler, closed) and shear-layer (Boussinesq,
+    'xchannel') workloads, a step count uniform in [steps_min, steps_max]."""
+    seed = int(rng.integers(2 ** 31))
+    r = np.random.default_rng(seed)
+
+    def side():
+        v = np.exp(r.uniform(np.log(side_min), np.log(side_max)))
+        return int(max(side_min, min(side_max, step * round(v / step))))
+    nx, ny = side(), side()
+    steps = int(r.integers(steps_min, steps_max + 1))
+    if r.random() < euler_fraction:
+        wl = _euler_with_islands(r, nx, ny)
+    else:
+        wl = _shear_with_islands(r, nx, ny)
+    wl["seed"] = seed
+    return wl, steps
+
+
+def _euler_with_islands(r, nx, ny):
+    Lx, Ly = 1., ny / nx
+    xr, yr = cell_coords(nx, ny, Lx, Ly)
+    msk = base_mask(nx, ny, 'closed')
+    L = min(Lx, Ly)
+    for _ in range(r.integers(0, 5)):
+        rad = r.uniform(0.03, 0.1) * L
+        cx, cy = r.uniform(rad, Lx - rad), r.uniform(rad, Ly - rad)
+        msk[(xr - cx) ** 2 + (yr - cy) ** 2 < rad * rad] = 0
+    w = np.zeros_like(xr)
+    fluid = np.argwhere(msk[3:-3, 3:-3] == 1)
+    for _ in range(r.integers(3, 13)):
+        a = r.standard_normal()
+        sig = r.uniform(0.02, 0.08)
+        j, i = fluid[r.integers(len(fluid))]
+        cx, cy = xr[3, 3 + i], yr[3 + j, 3]
+        w += a * np.exp(-((xr - cx) ** 2 + (yr - cy) ** 2) / sig ** 2)
+    return {'model': 'euler', 'geometry': 'closed', 'nx': nx, 'ny': ny, 'Lx': Lx, 'Ly': Ly,
+            'msk': msk, 'fields': {'vorticity': w * msk}}
+
+
+def _shear_with_islands(r, nx, ny, delta=0.02, gravity=5.):
+    """Boussinesq shear layer (Ri = 0.1) in a periodic channel with islands
+    kept away from the periodic ends (the halo of the mask is not filled)."""
+    Ly = 1.
+    Lx = nx / ny * Ly
+    xr, yr = cell_coords(nx, ny, Lx, Ly)
+    msk = base_mask(nx, ny, 'xchannel')
+    dx = Lx / nx
+    for _ in range(r.integers(0, 5)):
+        rad = r.uniform(0.03, 0.1) * min(Lx, Ly)
+        cx = r.uniform(rad + 4 * dx, Lx - rad - 4 * dx)
+        cy = r.uniform(rad, Ly - rad)
+        msk[(xr - cx) ** 2 + (yr - cy) ** 2 < rad * rad] = 0
+    s = (yr - 0.5) / delta
+    w = -(1. / delta) / np.cosh(s) ** 2
+    b = np.tanh(s) + 1e-3 * r.standard_normal(w.shape)
+    return {'model': 'boussinesq', 'geometry': 'xchannel', 'nx': nx, 'ny': ny, 'Lx': Lx,
+            'Ly': Ly, 'gravity': gravity, 'msk': msk,
+            'fields': {'vorticity': w * msk, 'buoyancy': b * msk}}
+
+
+def served_stream(count=2000, rate=40., seed=5, **kw):
+    """(arrival time, workload, steps) of `count` requests with Poisson
+    arrivals at `rate` per second."""
+    rng = np.random.default_rng(seed)
+    t = 0.
+    out = []
+    for _ in range(count):
+        t += rng.exponential(1. / rate)
+        wl, steps = served_request(rng, **kw)
+        out.append((t, wl, steps))
+    return out

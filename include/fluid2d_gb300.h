@@ -221,6 +221,8 @@ int f2d_model_destroy(void *model);
  * diag: DEVICE array of the model's diagnostics (f2d_model_diagname) */
 int f2d_model_info(void *model, int *nvar, int *mv, int *nv, int *nlev, int *coarse_level,
                    double **state, double **diag);
+/* device bytes the model holds (state, tendencies, hierarchy) */
+int f2d_model_bytes(void *model, size_t *bytes);
 const char *f2d_model_varname(void *model, int k);
 const char *f2d_model_diagname(void *model, int k);
 /* internal buffers: "state", "dx0", "dx1", "dx2" (RK tendencies, whose psi

@@ -1,0 +1,84 @@
+"""Host logic of the serving loop (no GPU): admission against the HBM
+budget, continuous batching (requests join and leave between ticks), FIFO
+order, retirement freeing memory, rejection of what can never fit."""
+import numpy as np
+
+from fluid2d_gb300 import serve, workloads as W
+
+
+class FakeModel(object):
+    def __init__(self, wl, precision):
+        self.wl = wl
+
+    def nbytes(self):
+        return serve.estimate_bytes(self.wl, "fp64")
+
+
+def fake_step(models):
+    return 1e-3 * len(models)
+
+
+def wl(n):
+    return {"nx": n, "ny": n, "model": "euler"}
+
+
+def test_admission_respects_the_budget_and_fifo():
+    budget = serve.estimate_bytes(wl(256), "fp64") * 2 + 1
+    s = serve.Server(budget, precision="fp64", make_model=FakeModel, step_models=fake_step)
+    reqs = [serve.Request(k, 0., wl(256), 3) for k in range(5)]
+    for r in reqs:
+        s.submit(r)
+    s.admit(0.)
+    assert [r.rid for r in s.active] == [0, 1]
+    assert s.used <= budget
+    s.tick(0.)
+    s.tick(0.)
+    s.tick(0.)  # 0 and 1 finish, memory freed
+    assert [r.rid for r in s.finished] == [0, 1]
+    s.admit(0.)
+    assert [r.rid for r in s.active] == [2, 3]
+
+
+def test_continuous_batching_requests_join_and_leave():
+    budget = serve.estimate_bytes(wl(128), "fp64") * 3 + 1
+    s = serve.Server(budget, precision="fp64", make_model=FakeModel, step_models=fake_step)
+    s.submit(serve.Request(0, 0., wl(128), 1))
+    s.submit(serve.Request(1, 0., wl(128), 4))
+    s.admit(0.)
+    s.tick(0.)                     # request 0 leaves after one step
+    s.submit(serve.Request(2, 0., wl(128), 2))
+    s.admit(0.)                    # request 2 joins while 1 is running
+    assert sorted(r.rid for r in s.active) == [1, 2]
+    while s.active:
+        s.tick(0.)
+    assert sorted(r.rid for r in s.finished) == [0, 1, 2]
+    assert all(len(r.latencies) == r.steps for r in s.finished)
+
+
+def test_too_large_requests_are_rejected():
+    s = serve.Server(1000, make_model=FakeModel, step_models=fake_step)
+    assert not s.submit(serve.Request(0, 0., wl(512), 1))
+    assert len(s.rejected) == 1
+
+
+def test_run_and_metrics_with_fakes():
+    stream = [(0.001 * k, wl(128), 2 + k % 3) for k in range(10)]
+    budget = serve.estimate_bytes(wl(128), "fp64") * 4
+    s = serve.Server(budget, precision="fp64", make_model=FakeModel, step_models=fake_step)
+    m = s.run(stream, time_scale=100.)
+    assert m["requests"] == 10 and m["rejected"] == 0
+    assert m["cell_steps"] == sum(128 * 128 * st for _, _, st in stream)
+    assert m["p99_step_ms"] >= m["p50_step_ms"] > 0
+
+
+def test_served_stream_generator():
+    st = W.served_stream(count=20, seed=5, side_min=128, side_max=512)
+    ts = [t for t, _, _ in st]
+    assert ts == sorted(ts)
+    kinds = {w["model"] for _, w, _ in st}
+    assert kinds <= {"euler", "boussinesq"}
+    for _, w, steps in st:
+        assert w["nx"] % 128 == 0 and w["ny"] % 128 == 0
+        assert 50 <= steps <= 500
+        assert w["msk"].shape == (w["ny"] + 6, w["nx"] + 6)
+        assert abs(w["Lx"] / w["nx"] - w["Ly"] / w["ny"]) < 1e-15

@@ -214,13 +214,20 @@ struct Gmg {
 
     int setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, double hydroeps,
               double om, bool qg, double Rd, bool f32, cudaStream_t s);
+    // level l is smoothed by the fused one-kernel smoother (output into the
+    // level's other buffer, the views' x/t pointers swapped afterwards):
+    // every level but a float64 finest level, which is FP64-ALU bound and
+    // gains nothing from recomputing a ring of first-sweep values
     template <typename T>
-    int smooth(LevelView<T> *L, int l, bool zero, const int *active, cudaStream_t s);
+    bool fused(int l) const { return l > 0 || sizeof(T) == 4; }
+    template <typename T>
+    int smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream_t s);
     template <typename T>
     int coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int *active,
                cudaStream_t s);
     template <typename T>
-    int vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s);
+    int vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s,
+               int first_mode = 0);
     template <typename T>
     int fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s);
 };
@@ -386,7 +393,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
 }
 
 template <typename T>
-int Gmg::smooth(LevelView<T> *L, int l, bool zero, const int *active, cudaStream_t s) {
+int Gmg::smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream_t s) {
     const AnalyticT<T> *a0 = l == 0 ? analytic<T>() : nullptr;
     T c1 = (T)omega, c2 = (T)(1. - omega);
     const bool pr = probe && l == 0 && nprobe < MAX_PROBES;
@@ -397,8 +404,18 @@ int Gmg::smooth(LevelView<T> *L, int l, bool zero, const int *active, cudaStream
         TRY(cuda_status(cudaEventRecordWithFlags(ev[nprobe][0], s, cudaEventRecordExternal),
                         "probe record"));
     }
-    TRY(mg_sweep1<T>(L[l], a0, c1, c2, zero, active, s));
-    TRY(mg_sweep2<T>(L[l], a0, c1, c2, active, s));
+    if (fused<T>(l)) {
+        TRY(mg_smooth_fused<T>(L[l], a0, c1, c2, xmode, xmode >= X_PLUS_INTERP ? &L[l + 1] : nullptr,
+                               L[l].t, active, s));
+        T *tmp = L[l].x;
+        L[l].x = L[l].t;
+        L[l].t = tmp;
+    } else {
+        if (xmode == X_PLUS_INTERP || xmode == X_INTERP)
+            TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, xmode == X_INTERP, active, s));
+        TRY(mg_sweep1<T>(L[l], a0, c1, c2, xmode == X_ZERO, active, s));
+        TRY(mg_sweep2<T>(L[l], a0, c1, c2, active, s));
+    }
     if (pr) {
         TRY(cuda_status(cudaEventRecordWithFlags(ev[nprobe][1], s, cudaEventRecordExternal),
                         "probe record"));
@@ -424,27 +441,32 @@ int Gmg::coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int
     return mg_coarse<T>(a, smem, s);
 }
 
-// core/gmg/hierarchy.py:98-126
+// core/gmg/hierarchy.py:98-126.  first_mode: the first level's input is x
+// (X_IN) or the prolongation of the next coarser level (X_INTERP, the
+// F-cycle's coarsetofine into x followed by this V-cycle).
 template <typename T>
-int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s) {
+int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s,
+                int first_mode) {
     const int deep = nlev - 1;
     if (l1 >= cs) return coarse(L, l1, CYCLE_V, zero_first, active, s);
     const int stop = cs < deep ? cs : deep;
     for (int l = l1; l < stop; l++) {
-        TRY(smooth(L, l, zero_first || l > l1, active, s));
-        TRY(mg_residual<T>(L[l], l == 0 ? analytic<T>() : nullptr, L[l].x, L[l].b, L[l].r, active,
-                           s));
-        TRY(mg_restrict<T>(L[l], L[l].r, L[l + 1], L[l + 1].b, active, s));
+        const int xm = (zero_first || l > l1) ? X_ZERO : (l == l1 ? first_mode : X_IN);
+        TRY(smooth(L, l, xm, active, s));
+        const AnalyticT<T> *a0 = l == 0 ? analytic<T>() : nullptr;
+        if (fused<T>(l)) {
+            TRY(mg_resres<T>(L[l], a0, L[l + 1], L[l + 1].b, active, s));
+        } else {
+            TRY(mg_residual<T>(L[l], a0, L[l].x, L[l].b, L[l].r, active, s));
+            TRY(mg_restrict<T>(L[l], L[l].r, L[l + 1], L[l + 1].b, active, s));
+        }
     }
     if (cs <= deep) {
         TRY(coarse(L, cs, CYCLE_V, true, active, s));
     } else {
-        for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0, active, s));
+        for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0 ? X_ZERO : X_IN, active, s));
     }
-    for (int l = stop - 1; l >= l1; l--) {
-        TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, false, active, s));
-        TRY(smooth(L, l, false, active, s));
-    }
+    for (int l = stop - 1; l >= l1; l--) TRY(smooth(L, l, X_PLUS_INTERP, active, s));
     return OK;
 }
 
@@ -458,12 +480,9 @@ int Gmg::fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s) {
     if (cs <= deep) {
         TRY(coarse(L, cs, CYCLE_F, false, active, s));
     } else {
-        for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0, active, s));
+        for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0 ? X_ZERO : X_IN, active, s));
     }
-    for (int l = stop - 1; l >= l1; l--) {
-        TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, true, active, s));
-        TRY(vcycle(L, l, false, active, s));
-    }
+    for (int l = stop - 1; l >= l1; l--) TRY(vcycle(L, l, false, active, s, X_INTERP));
     return OK;
 }
 

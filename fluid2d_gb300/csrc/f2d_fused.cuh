@@ -34,6 +34,9 @@ struct AnalyticT {
 using Analytic = AnalyticT<double>;
 
 enum CycleMode { CYCLE_V = 0, CYCLE_F = 1 };
+// input of a smoothing call: x, zero, x + prolongation of the coarser
+// level's x, or the prolongation alone
+enum XMode { X_IN = 0, X_ZERO = 1, X_PLUS_INTERP = 2, X_INTERP = 3 };
 
 template <typename T>
 struct CoarseArgs {
@@ -64,6 +67,15 @@ int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine
               bool assign, const int *active, cudaStream_t s);
 template <typename T>
 int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s);
+// fused smoothtwicewitha: input per xmode (0 x, 1 zero, 2 x + interp(coarse),
+// 3 interp(coarse)), result into `out` (not x)
+template <typename T>
+int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
+                    const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s);
+// residual of L (x, b) restricted into the coarse b2
+template <typename T>
+int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
+              const int *active, cudaStream_t s);
 template <typename T>
 size_t coarse_smem_bytes(const int *mv, const int *nv, int nlev);
 

@@ -330,6 +330,166 @@ int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine
     return launch_status("mg_interp");
 }
 
+// ------------------------------------------------------------ fused level kernels
+// One smoothtwicewitha call in one kernel.  The CTA's input values (x, or
+// x + prolongation of the coarse correction, or the prolongation alone, or
+// zero) on its tile plus a 2-cell ring go to shared memory, the first sweep
+// on the tile plus a 1-cell ring goes to shared memory, and the second sweep
+// writes the tile (and its periodic halo images) to a separate output array:
+// x is read by neighbouring CTAs while they run, so it is never updated in
+// place.  Same arithmetic, same order as the unfused kernels.
+constexpr int FS_TX = 32, FS_TY = 16;
+
+template <typename T>
+struct CoarseSrc {
+    const int8_t *msk;
+    const T *x;
+    int nv;
+};
+
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(FS_TX *FS_TY)
+k_smooth_fused(LevelView<T> L, AnalyticT<T> an, T c1, T c2, int xmode, CoarseSrc<T> cs, T *out,
+               const int *active) {
+    if (inactive(active)) return;
+    constexpr int XW = FS_TX + 4, XH = FS_TY + 4, TW = FS_TX + 2, TH = FS_TY + 2;
+    __shared__ T xs[XH * XW];
+    __shared__ T ts[TH * TW];
+    const int mv = L.mv, nv = L.nv;
+    const int i0 = NH + blockIdx.x * FS_TX, j0 = NH + blockIdx.y * FS_TY;
+    const int tid = threadIdx.y * FS_TX + threadIdx.x;
+    // input x on [j0-2, j0+FS_TY+1] x [i0-2, i0+FS_TX+1], inside rows/cols 1..m-2
+    if (xmode != X_ZERO) {
+        for (int q = tid; q < XH * XW; q += FS_TX * FS_TY) {
+            const int j = j0 - 2 + q / XW, i = i0 - 2 + q % XW;
+            if (j < 1 || j > mv - 2 || i < 1 || i > nv - 2) continue;
+            const size_t p = off(j, i, nv);
+            T v;
+            if (xmode == X_IN) {
+                v = L.x[p];
+            } else {
+                const T c = interp_value(L.msk, nv, cs.msk, cs.x, cs.nv, j, i);
+                v = xmode == X_PLUS_INTERP ? L.x[p] + c : c;
+            }
+            xs[q] = v;
+        }
+    }
+    __syncthreads();
+    // first sweep on [j0-1, j0+FS_TY] x [i0-1, i0+FS_TX], inside rows/cols 2..m-3
+    for (int q = tid; q < TH * TW; q += FS_TX * FS_TY) {
+        const int j = j0 - 1 + q / TW, i = i0 - 1 + q % TW;
+        if (j < 2 || j > mv - 3 || i < 2 || i > nv - 3) continue;
+        const size_t p = off(j, i, nv);
+        T v;
+        if (L.msk[p] == 0) {
+            v = (T)0;
+        } else {
+            const T c3 = c3_coef<T, L0>(L, &an, j, i, c1);
+            if (xmode == X_ZERO) {
+                v = c3 * (-L.b[p]);
+            } else {
+                T a[8];
+                offdiag<T, L0>(L, &an, j, i, a);
+                const T *x = xs + (j - (j0 - 2)) * XW + (i - (i0 - 2));
+                v = x[0] * c2 + c3 * (+a[0] * x[-XW - 1]
+                                      + a[1] * x[-XW]
+                                      + a[2] * x[-XW + 1]
+                                      + a[3] * x[-1]
+                                      + a[4] * x[1]
+                                      + a[5] * x[XW - 1]
+                                      + a[6] * x[XW]
+                                      + a[7] * x[XW + 1]
+                                      - L.b[p]);
+            }
+        }
+        ts[q] = v;
+    }
+    __syncthreads();
+    // second sweep on the tile's interior points
+    const int j = j0 + threadIdx.y, i = i0 + threadIdx.x;
+    if (j > mv - NH - 1 || i > nv - NH - 1) return;
+    const size_t p = off(j, i, nv);
+    T v = (T)0;
+    if (L.msk[p] != 0) {
+        const T c3 = c3_coef<T, L0>(L, &an, j, i, c1);
+        T a[8];
+        offdiag<T, L0>(L, &an, j, i, a);
+        const T *t = ts + (j - (j0 - 1)) * TW + (i - (i0 - 1));
+        v = t[0] * c2 + c3 * (+a[0] * t[-TW - 1]
+                              + a[1] * t[-TW]
+                              + a[2] * t[-TW + 1]
+                              + a[3] * t[-1]
+                              + a[4] * t[1]
+                              + a[5] * t[TW - 1]
+                              + a[6] * t[TW]
+                              + a[7] * t[TW + 1]
+                              - L.b[p]);
+    }
+    store_images(out, j, i, mv, nv, v);
+}
+
+template <typename T>
+int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
+                    const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s) {
+    dim3 b(FS_TX, FS_TY);
+    dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, b);
+    CoarseSrc<T> cs{nullptr, nullptr, 0};
+    if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
+    if (an)
+        k_smooth_fused<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, xmode, cs, out, active);
+    else
+        k_smooth_fused<T, false><<<g, b, 0, s>>>(L, AnalyticT<T>{}, c1, c2, xmode, cs, out, active);
+    return launch_status("mg_smooth_fused");
+}
+
+// residual + full-weighting restriction: the fine residuals a coarse tile
+// needs (fine halo positions through their periodic images, as the
+// reference's halo fill of r makes them) are computed once into shared
+// memory, then restricted.
+constexpr int RR_TX = 16, RR_TY = 8;
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(RR_TX *RR_TY)
+k_resres(LevelView<T> F, AnalyticT<T> an, const int8_t *msk2, int mv2, int nv2, T *b2,
+         const int *active) {
+    if (inactive(active)) return;
+    constexpr int RW = 2 * RR_TX + 1, RH = 2 * RR_TY + 1;
+    __shared__ T rs[RH * RW];
+    const int I2a = NH + blockIdx.x * RR_TX, J2a = NH + blockIdx.y * RR_TY;
+    const int jf0 = 2 * J2a - 3, if0 = 2 * I2a - 3;
+    const int tid = threadIdx.y * RR_TX + threadIdx.x;
+    const int mv = F.mv, nv = F.nv;
+    for (int q = tid; q < RH * RW; q += RR_TX * RR_TY) {
+        const int jf = jf0 + q / RW, iff = if0 + q % RW;
+        if (jf > mv - 3 || iff > nv - 3) continue;  // beyond the last coarse point's stencil
+        rs[q] = residual<T, L0>(F, &an, F.x, F.b, wrap(jf, mv, NH), wrap(iff, nv, NH));
+    }
+    __syncthreads();
+    const int J2 = J2a + threadIdx.y, I2 = I2a + threadIdx.x;
+    if (J2 > mv2 - NH - 1 || I2 > nv2 - NH - 1) return;
+    T v = (T)0;
+    if (msk2[off(J2, I2, nv2)] != 0) {
+        const T *r = rs + (2 * J2 - 2 - jf0) * RW + (2 * I2 - 2 - if0);
+        v = (T)0.25 * r[0]
+            + (T)0.125 * (r[-1] + r[1] + r[-RW] + r[RW])
+            + (T)0.0625 * (r[-RW - 1] + r[-RW + 1] + r[RW - 1] + r[RW + 1]);
+    }
+    store_images(b2, J2, I2, mv2, nv2, v);
+}
+
+template <typename T>
+int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
+              const int *active, cudaStream_t s) {
+    dim3 b(RR_TX, RR_TY);
+    dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, b);
+    if (an)
+        k_resres<T, true><<<g, b, 0, s>>>(F, *an, C.msk, C.mv, C.nv, b2, active);
+    else
+        k_resres<T, false><<<g, b, 0, s>>>(F, AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active);
+    return launch_status("mg_resres");
+}
+
 // ------------------------------------------------------------ coarse CTA
 // All levels below a size threshold are processed by one CTA out of shared
 // memory: the recursion of core/gmg/hierarchy.py:98-151 runs as a sequence
@@ -372,64 +532,108 @@ F2D_DEV LevelView<T> co_view(unsigned char *sm, const CoLv &d) {
     return L;
 }
 
+// Phases on small levels (at most CO_SMALL_PTS points, halo included) run on
+// the first CO_GROUP threads only -- one warp per SM sub-partition, so that
+// float64 work still reaches every FP64 unit -- and synchronise with a named
+// barrier; the other warps skip them.  A block-wide barrier is placed only
+// where a large-level phase follows small-level ones.
+constexpr int CO_GROUP = 128;
+constexpr int CO_SMALL_PTS = 256;
+
+struct CoSched {
+    bool prev_small;
+};
+
+// enter a phase on a level of `pts` points: returns whether this thread works
+F2D_DEV bool co_enter(CoSched &sc, int pts, int &nthreads) {
+    const bool small = pts <= CO_SMALL_PTS;
+    if (!small && sc.prev_small) __syncthreads();
+    sc.prev_small = small;
+    nthreads = small ? CO_GROUP : CO_THREADS;
+    const int tid = threadIdx.y * CO_TX + threadIdx.x;
+    return tid < nthreads;
+}
+
+F2D_DEV void co_leave(int nthreads) {
+    if (nthreads == CO_THREADS)
+        __syncthreads();
+    else
+        asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
+// rows [j0, j1] x cols [i0, i1] strided over the phase's threads
+#define CO_FOR(j0, j1, i0, i1, nthreads)                                               \
+    for (int _q = threadIdx.y * CO_TX + threadIdx.x,                                   \
+             _w = (i1) - (i0) + 1, _n = _w * ((j1) - (j0) + 1);                        \
+         _q < _n; _q += (nthreads))                                                    \
+        for (int j = (j0) + _q / _w, i = (i0) + _q % _w, _once = 1; _once; _once = 0)
+
 template <typename T>
-F2D_DEV void co_smooth(unsigned char *sm, const CoLv &d, T c1, T c2, bool zero_x) {
+F2D_DEV void co_smooth(unsigned char *sm, const CoLv &d, T c1, T c2, bool zero_x, CoSched &sc) {
     const LevelView<T> L = co_view<T>(sm, d);
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    for (int j = 2 + ty; j <= L.mv - 3; j += CO_TY)
-        for (int i = 2 + tx; i <= L.nv - 3; i += CO_TX)
-            L.t[off(j, i, L.nv)] = jacobi<T, false>(L, nullptr, zero_x ? nullptr : L.x, L.b, j, i,
-                                                    c1, c2);
-    __syncthreads();
-    for (int j = NH + ty; j <= L.mv - NH - 1; j += CO_TY)
-        for (int i = NH + tx; i <= L.nv - NH - 1; i += CO_TX)
-            store_images(L.x, j, i, L.mv, L.nv, jacobi<T, false>(L, nullptr, L.t, L.b, j, i, c1, c2));
-    __syncthreads();
+    int nt;
+    if (co_enter(sc, L.mv * L.nv, nt)) {
+        CO_FOR(2, L.mv - 3, 2, L.nv - 3, nt)
+        L.t[off(j, i, L.nv)] = jacobi<T, false>(L, nullptr, zero_x ? nullptr : L.x, L.b, j, i,
+                                                c1, c2);
+        co_leave(nt);
+        CO_FOR(NH, L.mv - NH - 1, NH, L.nv - NH - 1, nt)
+        store_images(L.x, j, i, L.mv, L.nv, jacobi<T, false>(L, nullptr, L.t, L.b, j, i, c1, c2));
+        co_leave(nt);
+    }
 }
 
 template <typename T>
-F2D_DEV void co_residual(unsigned char *sm, const CoLv &d) {
+F2D_DEV void co_residual(unsigned char *sm, const CoLv &d, CoSched &sc) {
     const LevelView<T> L = co_view<T>(sm, d);
-    for (int j = NH + threadIdx.y; j <= L.mv - NH - 1; j += CO_TY)
-        for (int i = NH + threadIdx.x; i <= L.nv - NH - 1; i += CO_TX)
-            store_images(L.r, j, i, L.mv, L.nv, residual<T, false>(L, nullptr, L.x, L.b, j, i));
-    __syncthreads();
+    int nt;
+    if (co_enter(sc, L.mv * L.nv, nt)) {
+        CO_FOR(NH, L.mv - NH - 1, NH, L.nv - NH - 1, nt)
+        store_images(L.r, j, i, L.mv, L.nv, residual<T, false>(L, nullptr, L.x, L.b, j, i));
+        co_leave(nt);
+    }
 }
 
 template <typename T>
-F2D_DEV void co_restrict(unsigned char *sm, const CoLv &df, bool from_b, const CoLv &dc) {
+F2D_DEV void co_restrict(unsigned char *sm, const CoLv &df, bool from_b, const CoLv &dc,
+                         CoSched &sc) {
     const LevelView<T> F = co_view<T>(sm, df), Cl = co_view<T>(sm, dc);
     const T *src = from_b ? F.b : F.r;
-    for (int j = NH + threadIdx.y; j <= Cl.mv - NH - 1; j += CO_TY)
-        for (int i = NH + threadIdx.x; i <= Cl.nv - NH - 1; i += CO_TX)
-            store_images(Cl.b, j, i, Cl.mv, Cl.nv, restrict_value(Cl.msk, Cl.nv, src, F.nv, j, i));
-    __syncthreads();
+    int nt;
+    if (co_enter(sc, F.mv * F.nv, nt)) {
+        CO_FOR(NH, Cl.mv - NH - 1, NH, Cl.nv - NH - 1, nt)
+        store_images(Cl.b, j, i, Cl.mv, Cl.nv, restrict_value(Cl.msk, Cl.nv, src, F.nv, j, i));
+        co_leave(nt);
+    }
 }
 
 template <typename T>
-F2D_DEV void co_interp(unsigned char *sm, const CoLv &dc, const CoLv &df, bool assign) {
+F2D_DEV void co_interp(unsigned char *sm, const CoLv &dc, const CoLv &df, bool assign,
+                       CoSched &sc) {
     const LevelView<T> Cl = co_view<T>(sm, dc), F = co_view<T>(sm, df);
-    for (int j = 1 + threadIdx.y; j <= F.mv - 2; j += CO_TY)
-        for (int i = 1 + threadIdx.x; i <= F.nv - 2; i += CO_TX) {
+    int nt;
+    if (co_enter(sc, F.mv * F.nv, nt)) {
+        CO_FOR(1, F.mv - 2, 1, F.nv - 2, nt) {
             T v = interp_value(F.msk, F.nv, Cl.msk, Cl.x, Cl.nv, j, i);
             size_t p = off(j, i, F.nv);
             F.x[p] = assign ? v : F.x[p] + v;
         }
-    __syncthreads();
+        co_leave(nt);
+    }
 }
 
 template <typename T>
 F2D_DEV void co_vcycle(unsigned char *sm, const CoLv *lv, int l1, int deep, bool zero_first,
-                       T c1, T c2, int ndeepest) {
+                       T c1, T c2, int ndeepest, CoSched &sc) {
     for (int l = l1; l < deep; l++) {
-        co_smooth<T>(sm, lv[l], c1, c2, zero_first || l > l1);
-        co_residual<T>(sm, lv[l]);
-        co_restrict<T>(sm, lv[l], false, lv[l + 1]);
+        co_smooth<T>(sm, lv[l], c1, c2, zero_first || l > l1, sc);
+        co_residual<T>(sm, lv[l], sc);
+        co_restrict<T>(sm, lv[l], false, lv[l + 1], sc);
     }
-    for (int k = 0; k < ndeepest; k++) co_smooth<T>(sm, lv[deep], c1, c2, k == 0);
+    for (int k = 0; k < ndeepest; k++) co_smooth<T>(sm, lv[deep], c1, c2, k == 0, sc);
     for (int l = deep - 1; l >= l1; l--) {
-        co_interp<T>(sm, lv[l + 1], lv[l], false);
-        co_smooth<T>(sm, lv[l], c1, c2, false);
+        co_interp<T>(sm, lv[l + 1], lv[l], false, sc);
+        co_smooth<T>(sm, lv[l], c1, c2, false, sc);
     }
 }
 
@@ -472,16 +676,18 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
     }
     __syncthreads();
     const int deep = a.nlev - 1;
+    CoSched sc{false};
     if (a.mode == CYCLE_V) {
-        co_vcycle<T>(sm, lv, 0, deep, a.zero_first != 0, a.c1, a.c2, a.ndeepest);
+        co_vcycle<T>(sm, lv, 0, deep, a.zero_first != 0, a.c1, a.c2, a.ndeepest, sc);
     } else {
-        for (int l = 0; l < deep; l++) co_restrict<T>(sm, lv[l], true, lv[l + 1]);
-        for (int k = 0; k < a.ndeepest; k++) co_smooth<T>(sm, lv[deep], a.c1, a.c2, k == 0);
+        for (int l = 0; l < deep; l++) co_restrict<T>(sm, lv[l], true, lv[l + 1], sc);
+        for (int k = 0; k < a.ndeepest; k++) co_smooth<T>(sm, lv[deep], a.c1, a.c2, k == 0, sc);
         for (int l = deep - 1; l >= 0; l--) {
-            co_interp<T>(sm, lv[l + 1], lv[l], true);
-            co_vcycle<T>(sm, lv, l, deep, false, a.c1, a.c2, a.ndeepest);
+            co_interp<T>(sm, lv[l + 1], lv[l], true, sc);
+            co_vcycle<T>(sm, lv, l, deep, false, a.c1, a.c2, a.ndeepest, sc);
         }
     }
+    __syncthreads();
     const LevelView<T> s0 = co_view<T>(sm, lv[0]);
     const int pts0 = a.lev[0].mv * a.lev[0].nv;
     for (int q = tid; q < pts0; q += CO_THREADS) a.lev[0].x[q] = s0.x[q];
@@ -664,6 +870,10 @@ int vec_axpy_const(double *x, double area, const double *sum, size_t count, cuda
     template int mg_interp<T>(const LevelView<T> &, const T *, const LevelView<T> &, T *, bool,  \
                               const int *, cudaStream_t);                                        \
     template int mg_coarse<T>(const CoarseArgs<T> &, size_t, cudaStream_t);                     \
+    template int mg_smooth_fused<T>(const LevelView<T> &, const AnalyticT<T> *, T, T, int,       \
+                                    const LevelView<T> *, T *, const int *, cudaStream_t);       \
+    template int mg_resres<T>(const LevelView<T> &, const AnalyticT<T> *, const LevelView<T> &,  \
+                              T *, const int *, cudaStream_t);                                   \
     template size_t coarse_smem_bytes<T>(const int *, const int *, int);
 F2D_INST(double)
 F2D_INST(float)

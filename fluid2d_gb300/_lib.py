@@ -21,8 +21,9 @@ CSRC = os.path.join(_HERE, "csrc")
 BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
-           "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu"]
-HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh"]
+           "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu", "timeloop.cu"]
+HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh",
+           "f2d_loop.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-fvisibility=hidden"]
@@ -168,6 +169,23 @@ class ModelDesc(ctypes.Structure):
                 ("precision", ctypes.c_int)]
 
 
+class LoopDesc(ctypes.Structure):
+    """f2d_loop_desc of include/fluid2d_gb300.h"""
+    _fields_ = [("tend", ctypes.c_double), ("freq_his", ctypes.c_double),
+                ("freq_diag", ctypes.c_double), ("exacthistime", ctypes.c_int),
+                ("rescaledtime", ctypes.c_int), ("nsave", ctypes.c_int),
+                ("save", ctypes.c_int * 8), ("his_cap", ctypes.c_int), ("diag_cap", ctypes.c_int),
+                ("t", ctypes.c_double), ("tnexthis", ctypes.c_double),
+                ("tnextdiag", ctypes.c_double), ("kt", ctypes.c_int)]
+
+
+class LoopState(ctypes.Structure):
+    """f2d_loop_state of include/fluid2d_gb300.h"""
+    _fields_ = [("t", ctypes.c_double), ("dt", ctypes.c_double), ("tnexthis", ctypes.c_double),
+                ("tnextdiag", ctypes.c_double), ("kt", ctypes.c_int), ("status", ctypes.c_int),
+                ("nhis", ctypes.c_int), ("ndiag", ctypes.c_int)]
+
+
 SIGNATURES.update({
     "f2d_gmg_create": [_P, _I, _I, _D, _D, _D, _I, _D, _PP],
     "f2d_gmg_destroy": [_P],
@@ -189,6 +207,11 @@ SIGNATURES.update({
     "f2d_model_probe": [_P, _I, _PI, _PDd],
     "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],
+    "f2d_model_loop_setup": [_P, ctypes.POINTER(LoopDesc), _P],
+    "f2d_model_loop_start": [_P, _P],
+    "f2d_model_loop_run": [_P, _I, _P],
+    "f2d_model_loop_state": [_P, ctypes.POINTER(LoopState), _P],
+    "f2d_model_loop_drain": [_P, _P, _P, _P, _P, _PI, _PI, _P],
 })
 
 EXTRA = {

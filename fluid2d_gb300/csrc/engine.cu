@@ -21,6 +21,7 @@
 #include "f2d_kernels.cuh"
 #include "f2d_adv.cuh"
 #include "f2d_mixed.cuh"
+#include "f2d_loop.cuh"
 
 namespace f2d {
 
@@ -757,6 +758,23 @@ struct Model {
         return nullptr;
     }
     int stage_mixed(int k, cudaStream_t s);
+    // device time loop (core/fluid2d.py:235-314): clock, rings, WHILE graph
+    struct Loop {
+        Arena mem;
+        LoopClock *clock = nullptr;
+        LoopConst k{};
+        LoopRings r{};
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaGraphConditionalHandle h = 0;
+        ~Loop() {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+        }
+    };
+    Loop *loop = nullptr;
+    int loop_body(cudaStream_t s);
+    int loop_build(cudaStream_t s);
     int last_nite = 0;
     int probe_per_step = -1;
     cudaGraph_t graph = nullptr;
@@ -771,6 +789,7 @@ struct Model {
     int invert(double *xs, const char *who, bool full, cudaStream_t s, double *ubase_out = nullptr);
     int stage(int k, cudaStream_t s);
     int step(cudaStream_t s);
+    int advance(cudaStream_t s);
     int diagnostics(cudaStream_t s);
     int set_psi(cudaStream_t s);
 };
@@ -1110,6 +1129,12 @@ int Model::step(cudaStream_t s) {
     k_set_dt<<<1, 1, 0, s>>>(dt, cst, (SplitConst *)advc, diag, desc.adaptable_dt, desc.dt,
                              desc.cfl, dx < dy ? dx : dy, desc.dtmax);
     TRY(launch_status("set_dt"));
+    TRY(advance(s));
+    return diagnostics(s);
+}
+
+// model.step after set_dt: the three stages and the post-step fields
+int Model::advance(cudaStream_t s) {
     if (desc.precision != 0) {
         TRY(split_f32(advc, dt, advf, dtf, s));
         TRY(vec_to_f32(X, Xf, nvar * pl, s));
@@ -1127,7 +1152,62 @@ int Model::step(cudaStream_t s) {
             TRY(launch_status("qg post"));
         }
     }
-    return diagnostics(s);
+    return OK;
+}
+
+// One iteration of core/fluid2d.py:235-311 on the device: set_dt with the
+// exact-history-time adjustment, model.step, t += dt, diagnostics, Output.do
+// into the rings, blow-up check.
+int Model::loop_body(cudaStream_t s) {
+    gmg.nprobe = 0;
+    TRY(loop_pre(loop->clock, loop->k, dt, cst, advc, diag, s));
+    TRY(advance(s));
+    TRY(diagnostics(s));
+    TRY(loop_post(loop->clock, loop->k, diag, loop->r, loop->h, s));
+    return loop_snapshot(loop->clock, loop->r, s);
+}
+
+// Graph: gate kernel -> WHILE node { loop_body }.  The gate and the last
+// kernel of the body set the condition; steps_left bounds every launch.
+int Model::loop_build(cudaStream_t s) {
+    cudaGraph_t g = nullptr;
+    TRY(cuda_status(cudaGraphCreate(&g, 0), "loop graph"));
+    loop->graph = g;
+    TRY(cuda_status(cudaGraphConditionalHandleCreate(&loop->h, g, 0, cudaGraphCondAssignDefault),
+                    "loop condition"));
+    TRY(cuda_status(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal),
+                    "loop gate capture"));
+    int st = loop_gate(loop->clock, loop->k, loop->h, s);
+    cudaGraph_t gc = nullptr;
+    int st2 = cuda_status(cudaStreamEndCapture(s, &gc), "loop gate capture end");
+    TRY(st);
+    TRY(st2);
+    size_t n = 0;
+    TRY(cuda_status(cudaGraphGetNodes(g, nullptr, &n), "loop graph nodes"));
+    if (n != 1) {
+        set_error("loop graph: expected one gate node, found %zu", n);
+        return ERR_CUDA;
+    }
+    cudaGraphNode_t gate = nullptr;
+    TRY(cuda_status(cudaGraphGetNodes(g, &gate, &n), "loop graph nodes"));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = loop->h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t wn = nullptr;
+    TRY(cuda_status(cudaGraphAddNode(&wn, g, &gate, nullptr, 1, &p), "loop while node"));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    TRY(cuda_status(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal),
+                    "loop body capture"));
+    st = loop_body(s);
+    cudaGraph_t bc = nullptr;
+    st2 = cuda_status(cudaStreamEndCapture(s, &bc), "loop body capture end");
+    TRY(st);
+    TRY(st2);
+    return cuda_status(cudaGraphInstantiate(&loop->exec, g, 0), "loop graph instantiate");
 }
 
 }  // namespace f2d
@@ -1163,6 +1243,7 @@ int f2d_model_destroy(void *model) {
     if (!M) return OK;
     if (M->gexec) cudaGraphExecDestroy(M->gexec);
     if (M->graph) cudaGraphDestroy(M->graph);
+    delete M->loop;
     delete M;
     return OK;
 }
@@ -1244,6 +1325,13 @@ int f2d_model_set_dt(void *model, double dt) {
         M->gexec = nullptr;
         M->graph = nullptr;
     }
+    if (M->loop) {
+        M->loop->k.dt0 = dt;
+        if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
+        if (M->loop->graph) cudaGraphDestroy(M->loop->graph);
+        M->loop->exec = nullptr;
+        M->loop->graph = nullptr;
+    }
     return OK;
 }
 
@@ -1271,6 +1359,184 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
         TRY(cuda_status(cudaGraphInstantiate(&M->gexec, g, 0), "graph instantiate"));
     }
     for (int k = 0; k < nsteps; k++) TRY(cuda_status(cudaGraphLaunch(M->gexec, s), "graph launch"));
+    return OK;
+}
+
+// ---- device time loop (core/fluid2d.py:235-314, core/output.py:62-94)
+int f2d_model_loop_setup(void *model, const f2d_loop_desc *ld, void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || !ld) {
+        set_error("f2d_model_loop_setup: null argument");
+        return ERR_ARG;
+    }
+    if (ld->nsave < 0 || ld->nsave > LOOP_MAX_SAVE || ld->his_cap < 1 || ld->diag_cap < 1 ||
+        !(ld->freq_his > 0) || !(ld->freq_diag > 0) || ld->rescaledtime < 0 ||
+        ld->rescaledtime > 1) {
+        set_error("f2d_model_loop_setup: bad loop description");
+        return ERR_ARG;
+    }
+    for (int q = 0; q < ld->nsave; q++)
+        if (ld->save[q] < 0 || ld->save[q] >= M->nvar) {
+            set_error("f2d_model_loop_setup: saved plane %d out of range", ld->save[q]);
+            return ERR_ARG;
+        }
+    // rescaledtime reads 'enstrophy' (core/fluid2d.py:258), which QG lacks
+    if (ld->rescaledtime && M->kind == M_QG) {
+        set_error("f2d_model_loop_setup: rescaledtime 'enstrophy' needs an enstrophy diagnostic");
+        return ERR_ARG;
+    }
+    delete M->loop;
+    M->loop = new (std::nothrow) Model::Loop();
+    if (!M->loop) return ERR_CUDA;
+    Model::Loop &L = *M->loop;
+    const int nd = NDIAG[M->kind];
+    const size_t per = (size_t)M->desc.ny * M->desc.nx * (ld->nsave > 0 ? ld->nsave : 1);
+    size_t o_clock = L.mem.add(sizeof(LoopClock));
+    size_t o_his = L.mem.add(sizeof(float) * per * ld->his_cap);
+    size_t o_ht = L.mem.add(sizeof(double) * ld->his_cap);
+    size_t o_hk = L.mem.add(sizeof(int) * ld->his_cap);
+    size_t o_diag = L.mem.add(sizeof(double) * (size_t)(nd + 4) * ld->diag_cap);
+    TRY(L.mem.alloc());
+    L.clock = L.mem.at<LoopClock>(o_clock);
+    L.k.adaptable = M->desc.adaptable_dt;
+    L.k.exacthistime = ld->exacthistime;
+    L.k.rescale = ld->rescaledtime;
+    L.k.ike = 1;
+    L.k.iens = M->kind == M_EULER ? 3 : (M->kind == M_BOUSSINESQ ? 5 : 3);
+    L.k.ndiag = nd;
+    L.k.his_cap = ld->his_cap;
+    L.k.diag_cap = ld->diag_cap;
+    L.k.dt0 = M->desc.dt;
+    L.k.cfl = M->desc.cfl;
+    L.k.hmin = M->dx < M->dy ? M->dx : M->dy;
+    L.k.dtmax = M->desc.dtmax;
+    L.r.his = L.mem.at<float>(o_his);
+    L.r.his_t = L.mem.at<double>(o_ht);
+    L.r.his_kt = L.mem.at<int>(o_hk);
+    L.r.diag = L.mem.at<double>(o_diag);
+    L.r.X = M->X;
+    L.r.pl = M->pl;
+    L.r.mv = M->mv;
+    L.r.nv = M->nv;
+    L.r.nsave = ld->nsave;
+    for (int q = 0; q < ld->nsave; q++) L.r.planes[q] = ld->save[q];
+    LoopClock c;
+    memset(&c, 0, sizeof(c));
+    c.t = ld->t;
+    c.dt = M->desc.dt;
+    c.tend = ld->tend;
+    c.tnexthis = ld->tnexthis;
+    c.tnextdiag = ld->tnextdiag;
+    c.freq_his = ld->freq_his;
+    c.freq_diag = ld->freq_diag;
+    c.kt = ld->kt;
+    c.his_slot = -1;
+    c.status = LOOP_RUNNING;
+    TRY(cuda_status(cudaMemcpyAsync(L.clock, &c, sizeof(c), cudaMemcpyHostToDevice, s),
+                    "loop clock"));
+    return cuda_status(cudaStreamSynchronize(s), "loop setup");
+}
+
+// the loop's start (core/fluid2d.py:199-214): diagnostics and Output.do at t
+int f2d_model_loop_start(void *model, void *stream) {
+    Model *M = (Model *)model;
+    if (!M || !M->loop) {
+        set_error("f2d_model_loop_start: no loop set up");
+        return ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    TRY(M->diagnostics(s));
+    TRY(loop_record(M->loop->clock, M->loop->k, M->diag, M->loop->r, s));
+    return loop_snapshot(M->loop->clock, M->loop->r, s);
+}
+
+// Run steps until t >= tend, a blow-up, a full ring or max_steps steps,
+// whichever comes first, as one graph launch (no host synchronisation).
+int f2d_model_loop_run(void *model, int max_steps, void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || !M->loop || max_steps < 0 || !s) {
+        set_error("f2d_model_loop_run: needs a loop, max_steps >= 0 and a non-default stream");
+        return ERR_ARG;
+    }
+    if (M->gmg.probe) {
+        set_error("f2d_model_loop_run: disable the smoother probe first");
+        return ERR_ARG;
+    }
+    Model::Loop &L = *M->loop;
+    if (!L.exec) {
+        int st = M->loop_build(s);
+        if (st) {
+            if (L.exec) cudaGraphExecDestroy(L.exec);
+            if (L.graph) cudaGraphDestroy(L.graph);
+            L.exec = nullptr;
+            L.graph = nullptr;
+            return st;
+        }
+    }
+    TRY(cuda_status(cudaMemcpyAsync(&L.clock->steps_left, &max_steps, sizeof(int),
+                                    cudaMemcpyHostToDevice, s),
+                    "loop steps"));
+    return cuda_status(cudaGraphLaunch(L.exec, s), "loop graph launch");
+}
+
+int f2d_model_loop_state(void *model, f2d_loop_state *out, void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || !M->loop || !out) return ERR_ARG;
+    LoopClock c;
+    TRY(cuda_status(cudaMemcpyAsync(&c, M->loop->clock, sizeof(c), cudaMemcpyDeviceToHost, s),
+                    "loop state"));
+    TRY(cuda_status(cudaStreamSynchronize(s), "loop state sync"));
+    out->t = c.t;
+    out->dt = c.dt;
+    out->tnexthis = c.tnexthis;
+    out->tnextdiag = c.tnextdiag;
+    out->kt = c.kt;
+    out->status = c.status;
+    out->nhis = c.nhis;
+    out->ndiag = c.ndiag;
+    return OK;
+}
+
+// Copy the records waiting in the rings to host memory and empty the rings.
+// his: nhis x nsave x ny x nx float32; his_t, his_kt: nhis; diag_rows:
+// ndiag x (ndiag_values + 4) float64.  Null outputs are skipped.
+int f2d_model_loop_drain(void *model, float *his, double *his_t, int *his_kt, double *diag_rows,
+                         int *nhis, int *ndiag, void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || !M->loop) return ERR_ARG;
+    Model::Loop &L = *M->loop;
+    LoopClock c;
+    TRY(cuda_status(cudaMemcpyAsync(&c, L.clock, sizeof(c), cudaMemcpyDeviceToHost, s),
+                    "loop drain"));
+    TRY(cuda_status(cudaStreamSynchronize(s), "loop drain sync"));
+    const size_t per = (size_t)M->desc.ny * M->desc.nx * L.r.nsave;
+    if (his && c.nhis && per)
+        TRY(cuda_status(cudaMemcpyAsync(his, L.r.his, sizeof(float) * per * c.nhis,
+                                        cudaMemcpyDeviceToHost, s),
+                        "loop drain his"));
+    if (his_t && c.nhis)
+        TRY(cuda_status(cudaMemcpyAsync(his_t, L.r.his_t, sizeof(double) * c.nhis,
+                                        cudaMemcpyDeviceToHost, s),
+                        "loop drain his_t"));
+    if (his_kt && c.nhis)
+        TRY(cuda_status(cudaMemcpyAsync(his_kt, L.r.his_kt, sizeof(int) * c.nhis,
+                                        cudaMemcpyDeviceToHost, s),
+                        "loop drain his_kt"));
+    if (diag_rows && c.ndiag)
+        TRY(cuda_status(cudaMemcpyAsync(diag_rows, L.r.diag,
+                                        sizeof(double) * (size_t)(L.k.ndiag + 4) * c.ndiag,
+                                        cudaMemcpyDeviceToHost, s),
+                        "loop drain diag"));
+    const int zero[2] = {0, 0};
+    TRY(cuda_status(cudaMemcpyAsync(&L.clock->nhis, zero, sizeof(zero), cudaMemcpyHostToDevice, s),
+                    "loop drain reset"));
+    TRY(cuda_status(cudaStreamSynchronize(s), "loop drain sync"));
+    if (nhis) *nhis = c.nhis;
+    if (ndiag) *ndiag = c.ndiag;
     return OK;
 }
 

@@ -241,6 +241,129 @@ class Model(object):
                    ctypes.byref(st))
         return nite.value, res.value, st.value
 
+    # ---- device time loop: core/fluid2d.py:190-330 with core/output.py:62-94
+    LOOP_STATUS = {0: "running", 1: "tend", 2: "blowup", 3: "bad_dt"}
+
+    def loop_setup(self, tend, freq_his=1., freq_diag=1., var_to_save=("vorticity",),
+                   exacthistime=True, rescaledtime="none", his_cap=8, diag_cap=1024, t=0.,
+                   kt=0, tnexthis=0., tnextdiag=0.):
+        """Set the device clock and the record rings.  t, kt, tnexthis and
+        tnextdiag are a restart's values (0 for a new run)."""
+        if isinstance(var_to_save, str):
+            var_to_save = (list(self.var.varname_list) if var_to_save == "all"
+                           else [var_to_save])
+        for v in var_to_save:
+            if v not in self.var.varname_list:
+                raise ValueError("%s is not a model variable => modify param.var_to_save" % v)
+        if rescaledtime not in ("none", "enstrophy"):
+            raise ValueError("rescaledtime must be 'none' or 'enstrophy'")
+        d = _lib.LoopDesc()
+        d.tend, d.freq_his, d.freq_diag = float(tend), float(freq_his), float(freq_diag)
+        d.exacthistime = int(bool(exacthistime))
+        d.rescaledtime = int(rescaledtime == "enstrophy")
+        d.nsave = len(var_to_save)
+        for q, v in enumerate(var_to_save):
+            d.save[q] = self.var.varname_list.index(v)
+        d.his_cap, d.diag_cap = int(his_cap), int(diag_cap)
+        d.t, d.tnexthis, d.tnextdiag, d.kt = float(t), float(tnexthis), float(tnextdiag), int(kt)
+        self._call("f2d_model_loop_setup", self.h, ctypes.byref(d), _stream())
+        self._loop = d
+        self.var_to_save = list(var_to_save)
+
+    def loop_start(self):
+        """Diagnostics and Output.do at the clock's time (the loop's start)."""
+        self._call("f2d_model_loop_start", self.h, _stream())
+
+    def loop_run(self, max_steps):
+        """Launch the loop graph: steps until tend, a blow-up, a full ring or
+        max_steps steps (asynchronous)."""
+        self._call("f2d_model_loop_run", self.h, int(max_steps), _stream())
+
+    def loop_state(self):
+        s = _lib.LoopState()
+        self._call("f2d_model_loop_state", self.h, ctypes.byref(s), _stream())
+        return {"t": s.t, "dt": s.dt, "kt": s.kt, "tnexthis": s.tnexthis,
+                "tnextdiag": s.tnextdiag, "status": self.LOOP_STATUS.get(s.status, s.status),
+                "nhis": s.nhis, "ndiag": s.ndiag}
+
+    def loop_drain(self):
+        """The records waiting in the rings, as (t, kt, {var: float32 array})
+        history records and (t, kt, {diag: value}) diagnostic rows; empties
+        the rings."""
+        d = self._loop
+        ny, nx = self.desc.ny, self.desc.nx
+        his = np.empty((d.his_cap, max(1, d.nsave), ny, nx), np.float32)
+        ht = np.empty(d.his_cap, np.float64)
+        hk = np.empty(d.his_cap, np.int32)
+        names = self.diag_names + ["dkedt", "dvdt"]
+        rows = np.empty((d.diag_cap, len(names) + 2), np.float64)
+        nh, nd = ctypes.c_int(), ctypes.c_int()
+        self._call("f2d_model_loop_drain", self.h, his.ctypes.data, ht.ctypes.data,
+                   hk.ctypes.data, rows.ctypes.data, ctypes.byref(nh), ctypes.byref(nd),
+                   _stream())
+        recs = [(float(ht[k]), int(hk[k]),
+                 {v: his[k, q].copy() for q, v in enumerate(self.var_to_save)})
+                for k in range(nh.value)]
+        diag = [(float(rows[k, 0]), int(rows[k, 1]),
+                 {n: float(rows[k, 2 + q]) for q, n in enumerate(names)})
+                for k in range(nd.value)]
+        return recs, diag
+
+    def loop(self, tend, output=None, max_steps=None, start=True, **setup):
+        """Fluid2d.loop on the device: run to tend (or max_steps steps),
+        handing history records and diagnostic rows to ``output``
+        (``write_his(t, kt, fields)``, ``write_diag(t, kt, diags)``) each
+        time the rings are drained, or collecting them when output is None.
+        Returns the final clock (loop_state) with the collected records."""
+        self.loop_setup(tend, **setup)
+        his, diag = [], []
+
+        def hand(recs, rows):
+            if output is None:
+                his.extend(recs)
+                diag.extend(rows)
+                return
+            for t, kt, f in recs:
+                output.write_his(t, kt, f)
+            for t, kt, dg in rows:
+                output.write_diag(t, kt, dg)
+
+        kt0 = self._loop.kt
+        if start:
+            self.loop_start()
+        while True:
+            left = 2 ** 31 - 1
+            if max_steps is not None:
+                left = int(max_steps) - (self.loop_state()["kt"] - kt0)
+                if left <= 0:
+                    break
+            self.loop_run(left)
+            st = self.loop_state()
+            hand(*self.loop_drain())
+            if st["status"] != "running":
+                break
+        st = self.loop_state()
+        hand(*self.loop_drain())
+        self.read_diags()
+        st["his"], st["diag"] = his, diag
+        return st
+
+    def write_restart(self, path, tend):
+        """core/restart.py:120-143: the clock and the float64 state with halo."""
+        from .output import Restart
+        st = self.loop_state()
+        Restart.write(path, tend, st["t"], st["dt"], st["kt"], st["tnextdiag"], st["tnexthis"],
+                      self.var.state.cpu().numpy(), self.var.varname_list)
+
+    def read_restart(self, path):
+        """core/restart.py:145-163 and Fluid2d.relaunch (core/fluid2d.py:356-368):
+        loads the state, returns the clock to pass to ``loop`` (t, kt,
+        tnexthis, tnextdiag) and the stored tend."""
+        from .output import Restart
+        clock, state = Restart.read(path, self.var.varname_list)
+        self.var.state.copy_(torch.from_numpy(state).to(self.var.state.device))
+        return clock
+
     def __del__(self):
         try:
             if getattr(self, "h", None):

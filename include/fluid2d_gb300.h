@@ -245,6 +245,47 @@ int f2d_model_probe(void *model, int enable, int *count, double *avg_ms);
 /* number of kernel nodes in the captured step graph */
 int f2d_model_graph_kernels(void *model, int *nkernels);
 
+/* ---- device time loop.  Replaces the host loop of Fluid2d.loop
+ * (core/fluid2d.py:235-314) with its set_dt (:376-397), exact-history-time
+ * adjustment (:245-254), blow-up stop (:306-311) and the decisions of
+ * Output.do (core/output.py:62-94).  The clock stays on the device; a run is
+ * one graph launch (a conditional WHILE node over one step) that stops at
+ * tend, on a blow-up, when a record ring is full or after max_steps steps.
+ * History records (the interior of the saved planes, float32, the layout of
+ * core/output.py:234-243) and diagnostic rows wait in device rings until
+ * f2d_model_loop_drain copies them out. */
+#define F2D_LOOP_RUNNING 0
+#define F2D_LOOP_TEND 1
+#define F2D_LOOP_BLOWUP 2
+#define F2D_LOOP_BAD_DT 3
+typedef struct f2d_loop_desc {
+    double tend;                  /* param.tend */
+    double freq_his, freq_diag;   /* param.freq_his, param.freq_diag */
+    int exacthistime;             /* param.exacthistime (acts with adaptable_dt) */
+    int rescaledtime;             /* 0: 'none', 1: 'enstrophy' */
+    int nsave;                    /* planes in a history record (<= 8) */
+    int save[8];                  /* their state indices (param.var_to_save) */
+    int his_cap, diag_cap;        /* ring capacities, in records */
+    double t, tnexthis, tnextdiag; /* clock at the start: 0, 0, 0, or a restart's */
+    int kt;
+} f2d_loop_desc;
+typedef struct f2d_loop_state {
+    double t, dt, tnexthis, tnextdiag;
+    int kt, status, nhis, ndiag;
+} f2d_loop_state;
+int f2d_model_loop_setup(void *model, const f2d_loop_desc *ld, void *stream);
+/* diagnostics and Output.do at the current time (core/fluid2d.py:199-214) */
+int f2d_model_loop_start(void *model, void *stream);
+/* asynchronous; stream must not be the legacy default stream */
+int f2d_model_loop_run(void *model, int max_steps, void *stream);
+/* synchronous read of the clock */
+int f2d_model_loop_state(void *model, f2d_loop_state *st, void *stream);
+/* HOST outputs: his nhis x nsave x ny x nx float32, his_t/his_kt nhis,
+ * diag_rows ndiag x (ndiag_values + 4) float64 = t, kt, the model's
+ * diagnostics (f2d_model_diagname order), dkedt, dvdt.  Empties the rings. */
+int f2d_model_loop_drain(void *model, float *his, double *his_t, int *his_kt, double *diag_rows,
+                         int *nhis, int *ndiag, void *stream);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

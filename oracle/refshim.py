@@ -123,3 +123,84 @@ def reference_param(core_dir, **overrides):
     for k, v in overrides.items():
         setattr(p, k, v)
     return p
+
+
+# ------------------------------------------------------------ netCDF recorder
+class _RecVar(object):
+    """A netCDF variable kept in memory: numpy array, first axis growing when
+    it is the unlimited dimension, values cast to the declared type on write
+    ('f' float32, 'd' float64, 'i' int32) as netCDF4 does."""
+
+    TYPES = {'f': np.float32, 'd': np.float64, 'i': np.int32}
+
+    def __init__(self, typ, shape, unlimited):
+        self.unlimited = unlimited
+        self.a = np.zeros(((0,) if unlimited else ()) + tuple(shape), dtype=self.TYPES[typ])
+
+    def __setitem__(self, idx, val):
+        if self.unlimited:
+            first = idx[0] if isinstance(idx, tuple) else idx
+            if isinstance(first, (range, list, np.ndarray)):
+                need = max(first) + 1 if len(first) else 0
+            elif isinstance(first, slice):
+                need = first.stop if first.stop is not None else self.a.shape[0]
+            else:
+                need = int(first) + 1
+            if need > self.a.shape[0]:
+                grown = np.zeros((need,) + self.a.shape[1:], dtype=self.a.dtype)
+                grown[:self.a.shape[0]] = self.a
+                self.a = grown
+        if isinstance(idx, range):
+            idx = np.asarray(idx)
+        self.a[idx] = val
+
+    def __getitem__(self, idx):
+        return self.a[idx]
+
+
+class RecordingDataset(object):
+    """Stand-in for netCDF4.Dataset that keeps every file in ``FILES``
+    (path -> {'attrs', 'dims', 'variables'}), so that the reference's own
+    Output/NcfileIO/Restart code can run and its writes be compared."""
+
+    FILES = {}
+
+    def __init__(self, path, mode='r', format=None):
+        if mode == 'w':
+            RecordingDataset.FILES[path] = {'attrs': {}, 'dims': {}, 'variables': {}}
+        self._f = RecordingDataset.FILES[path]
+        self.variables = self._f['variables']
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+    def close(self):
+        pass
+
+    def setncattr(self, k, v):
+        self._f['attrs'][k] = v
+
+    def getncattr(self, k):
+        return self._f['attrs'][k]
+
+    def createDimension(self, name, size):
+        self._f['dims'][name] = size
+
+    def createVariable(self, name, typ, dims):
+        if isinstance(dims, str):
+            dims = (dims,)
+        sizes = [self._f['dims'][d] for d in dims]
+        unlimited = bool(dims) and sizes[0] is None
+        shape = sizes[1:] if unlimited else sizes
+        v = _RecVar(typ, shape, unlimited)
+        self._f['variables'][name] = v
+        return v
+
+
+def install_recording_netcdf():
+    """Route the reference's ``from netCDF4 import Dataset`` to the recorder."""
+    sys.modules['netCDF4'] = _module('netCDF4', Dataset=RecordingDataset)
+    return RecordingDataset

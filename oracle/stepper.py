@@ -757,6 +757,77 @@ def run(model, param, nsteps, dt0, t=0., callback=None):
     return t
 
 
+class History(object):
+    """What Output.do (core/output.py:62-94) writes, kept in memory: history
+    records (t, kt and the interior of each saved plane in float32, as the
+    netCDF 'f' variables of core/output.py:227-243 store them) and diagnostic
+    rows (t, kt and every model diagnostic, incl. dkedt and dvdt)."""
+
+    def __init__(self, var_to_save, freq_his, freq_diag, tnexthis=0., tnextdiag=0.):
+        self.var_to_save = list(var_to_save)
+        self.freq_his, self.freq_diag = freq_his, freq_diag
+        self.tnexthis, self.tnextdiag = tnexthis, tnextdiag
+        self.his = []
+        self.diag = []
+
+    def do(self, model, t, kt):
+        nh = model.nh
+        if t >= self.tnextdiag:
+            self.tnextdiag += self.freq_diag
+            self.diag.append((t, kt, dict(model.diags)))
+        if t >= self.tnexthis:
+            self.tnexthis += self.freq_his
+            self.his.append((t, kt, {v: model.get(v)[nh:-nh, nh:-nh].astype(np.float32)
+                                     for v in self.var_to_save}))
+
+
+def loop(model, param, tend, dt0, out, t=0., kt=0, exacthistime=True,
+         rescaledtime='none', max_steps=None):
+    """Fluid2d.loop (core/fluid2d.py:190-314): diagnostics and output at the
+    start, then set_dt, the exact-history-time adjustment, step, clock,
+    diagnostics, dkedt/dvdt, output and the blow-up stop.  Returns (t, kt,
+    list of the dt used, stop reason)."""
+    ensname = 'pv2' if isinstance(model, QG) else 'enstrophy'
+    model.diagnostics(t)
+    model.diags['dkedt'] = 0.
+    model.diags['dvdt'] = 0.
+    out.do(model, t, kt)
+    reduce = 0
+    dts = []
+    reason = 'tend'
+    while t < tend:
+        if max_steps is not None and len(dts) >= max_steps:
+            reason = 'max_steps'
+            break
+        dt = set_dt(model, param, dt0)
+        if exacthistime and param.adaptable_dt:
+            if (t + 8 * dt > out.tnexthis) and (reduce == 0):
+                reduce = 8
+            if reduce > 0:
+                dt = (out.tnexthis - t) / (reduce * 0.95)
+                reduce -= 1
+            if t + dt > out.tnexthis:
+                reduce = 0
+                dt = out.tnexthis - t
+        model.step(t, dt)
+        dts.append(dt)
+        if rescaledtime == 'enstrophy':
+            t += dt * np.sqrt(model.diags['enstrophy'])
+        else:
+            t += dt
+        kt += 1
+        ke_old = model.diags['ke']
+        ens_old = model.diags[ensname]
+        model.diagnostics(t)
+        model.diags['dkedt'] = (model.diags['ke'] - ke_old) / dt
+        model.diags['dvdt'] = (model.diags[ensname] - ens_old) / dt
+        out.do(model, t, kt)
+        if model.diags['maxspeed'] > 1e3:
+            reason = 'blowup'
+            break
+    return t, kt, dts, reason
+
+
 def from_workload(wl, **kw):
     """An oracle model for a fluid2d_gb300.workloads dict: mask, fields,
     initial inversion (set_psi_from_vorticity / set_psi_from_pv) and

@@ -49,10 +49,10 @@ def cases():
     }
 
 
-def reference_model(core, wl, kw):
+def reference_model(core, wl, kw, with_param=False):
     over = dict(modelname=wl["model"], nx=wl["nx"], ny=wl["ny"], Lx=wl["Lx"], Ly=wl["Ly"],
-                geometry=wl["geometry"], gravity=wl.get("gravity", 1.), adaptable_dt=False,
-                **kw)
+                geometry=wl["geometry"], gravity=wl.get("gravity", 1.), adaptable_dt=False)
+    over.update(kw)
     p = refshim.reference_param(core, **over)
     import grid as rgrid
     with contextlib.redirect_stdout(io.StringIO()):
@@ -76,7 +76,117 @@ def reference_model(core, wl, kw):
         else:
             M.set_psi_from_vorticity()
         M.diagnostics(M.var, 0.)
+    if with_param:
+        return M, p, g
     return M
+
+
+# ---------------------------------------------------------------- time loop
+LOOP_CASES = {
+    # adaptive dt with the exact-history-time countdown; two saved planes
+    "loop_euler_closed_32": (lambda: W.dipole(32, 32, seed=1),
+                             dict(adaptable_dt=True, cfl=0.8, dt=0.1, dtmax=5.),
+                             dict(tend=0.2, freq_his=0.05, freq_diag=0.02,
+                                  var_to_save=["vorticity", "psi"], exacthistime=True)),
+    # fixed dt (no countdown), Boussinesq, history times crossed between steps
+    "loop_boussinesq_xchannel_64x16": (lambda: W.shear(64, 16, seed=3, delta=0.1),
+                                       dict(adaptable_dt=False, dt=0.004),
+                                       dict(tend=0.1, freq_his=0.03, freq_diag=0.01,
+                                            var_to_save=["vorticity", "buoyancy"],
+                                            exacthistime=True)),
+    # time rescaled by the enstrophy, adaptive dt without the countdown
+    "loop_euler_perio_32_rescaled": (lambda: W.turbulence(32, 32, seed=5, k0=3.),
+                                     dict(adaptable_dt=True, cfl=0.6, dt=0.1, dtmax=5.),
+                                     dict(tend=0.4, freq_his=0.1, freq_diag=0.05,
+                                          var_to_save=["vorticity"], exacthistime=False,
+                                          rescaledtime="enstrophy")),
+}
+
+
+def reference_loop(core, wl, kw, lk, tmpdir):
+    """Fluid2d.loop (core/fluid2d.py:190-330) of the reference, run on an
+    object holding only the attributes the loop reads (the rest of
+    Fluid2d.__init__ copies scripts and redirects stdout), with the
+    reference's own Output writing into the in-memory netCDF recorder."""
+    import types
+    R, p, g = reference_model(core, wl, kw, with_param=True)
+    # the domain area is a size-1 array there (core/grid.py domain_integration
+    # over mpitools), which makes every diagnostic a size-1 array; numpy 2
+    # no longer converts those to the scalars that Output.write_diag stores
+    # (core/output.py:132).  A scalar area gives the same quotients.
+    R.area = float(np.asarray(R.area).ravel()[0])
+    refshim.install_recording_netcdf()
+    import fluid2d as rfluid2d
+    import output as routput
+    routput.Dataset = refshim.RecordingDataset
+    p.expname = "loop"
+    p.expdir = tmpdir
+    p.tend = lk["tend"]
+    p.freq_his = lk["freq_his"]
+    p.freq_diag = lk["freq_diag"]
+    p.var_to_save = list(lk["var_to_save"])
+    p.list_diag = "all"
+    p.nprint = 10 ** 9
+    with contextlib.redirect_stdout(io.StringIO()):
+        out = routput.Output(p, g, R.diags)
+    F = types.SimpleNamespace(
+        myrank=0, decay=False, modelname=wl["model"], model=R, diag_fluxes=False, output=out,
+        plot_interactive=False, nh=3, t=0., kt=0, tend=lk["tend"],
+        exacthistime=lk["exacthistime"], adaptable_dt=kw["adaptable_dt"], dt=kw["dt"],
+        dt0=kw["dt"], cfl=p.cfl, dtmax=p.dtmax, dx=g.dx, dy=g.dy, rescaledtime=lk.get("rescaledtime", "none"),
+        enstrophyname="enstrophy", enforce_momentum=False, nprint=10 ** 9, freq_plot=10 ** 9,
+        npx=1, npy=1, nx=wl["nx"], ny=wl["ny"], nbproc=1)
+    F.set_dt = lambda kt: rfluid2d.Fluid2d.set_dt(F, kt)
+    F.print_config = lambda *a, **k: None
+    with contextlib.redirect_stdout(io.StringIO()):
+        rfluid2d.Fluid2d.loop(F)
+    files = refshim.RecordingDataset.FILES
+    his = files[out.hisfile]["variables"]
+    dia = files[out.diagfile]["variables"]
+    return R, {k: v.a for k, v in his.items()}, {k: v.a for k, v in dia.items()}
+
+
+def main_loop(core):
+    import tempfile
+    refshim.install(core)
+    refshim.install_recording_netcdf()
+    for name, (mk, kw, lk) in LOOP_CASES.items():
+        wl = mk()
+        with tempfile.TemporaryDirectory() as tmp:
+            R, his, dia = reference_loop(core, wl, kw, lk, tmp)
+        p, O = stepper.from_workload(wl, **kw)
+        out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"])
+        t, kt, dts, reason = stepper.loop(O, p, lk["tend"], kw["dt"], out,
+                                          exacthistime=lk["exacthistime"],
+                                          rescaledtime=lk.get("rescaledtime", "none"))
+        assert np.array_equal(R.var.state, O.state), name
+        assert np.array_equal(his["t"], np.array([h[0] for h in out.his], np.float32)), name
+        assert np.array_equal(his["kt"], np.array([h[1] for h in out.his], np.int32)), name
+        for v in lk["var_to_save"]:
+            assert np.array_equal(his[v], np.array([h[2][v] for h in out.his])), (name, v)
+        assert np.array_equal(dia["t"], np.array([d[0] for d in out.diag], np.float32)), name
+        assert np.array_equal(dia["kt"], np.array([d[1] for d in out.diag], np.int32)), name
+        names = [k for k in out.diag[0][2]]
+        for k in names:
+            assert np.array_equal(dia[k], np.array([d[2][k] for d in out.diag], np.float32)), \
+                (name, k)
+        fx = dict(msk=wl["msk"], his_t=his["t"], his_kt=his["kt"],
+                  his_t64=np.array([h[0] for h in out.his]),
+                  diag_t=dia["t"], diag_kt=dia["kt"], diag_names=np.array(names),
+                  diag=np.array([dia[k] for k in names]).T,
+                  diag64=np.array([[d[2][k] for k in names] for d in out.diag]),
+                  dts=np.array(dts), final_state=O.state,
+                  var_to_save=np.array(lk["var_to_save"]),
+                  params=np.array([repr(dict(model=wl["model"], nx=wl["nx"], ny=wl["ny"],
+                                             Lx=wl["Lx"], Ly=wl["Ly"],
+                                             geometry=wl["geometry"],
+                                             gravity=wl.get("gravity", 1.), **kw))]),
+                  loop=np.array([repr(lk)]))
+        for v in lk["var_to_save"]:
+            fx["his_" + v] = his[v]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
+        print("%-28s ok: reference loop == oracle loop, %d steps, %d records, %d rows"
+              % (name, kt, len(out.his), len(out.diag)))
 
 
 def main(core, steps=4):
@@ -111,4 +221,6 @@ def main(core, steps=4):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLUID2D_CORE", DEFAULT_CORE))
+    core = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLUID2D_CORE", DEFAULT_CORE)
+    main(core)
+    main_loop(core)

@@ -19,7 +19,8 @@ import pytest
 from tests import _cases as C
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+GOLDEN = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                if not os.path.basename(p).startswith("loop_"))
 
 
 def K():

@@ -767,9 +767,11 @@ struct Model {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         cudaGraphConditionalHandle h = 0;
+        cudaStream_t capture = nullptr;  // private stream the graph is captured on
         ~Loop() {
             if (exec) cudaGraphExecDestroy(exec);
             if (graph) cudaGraphDestroy(graph);
+            if (capture) cudaStreamDestroy(capture);
         }
     };
     Loop *loop = nullptr;
@@ -1452,12 +1454,13 @@ int f2d_model_loop_start(void *model, void *stream) {
 }
 
 // Run steps until t >= tend, a blow-up, a full ring or max_steps steps,
-// whichever comes first, as one graph launch (no host synchronisation).
+// whichever comes first, as one graph launch (no host synchronisation).  The
+// graph is captured once, on a private stream, and launched on `stream`.
 int f2d_model_loop_run(void *model, int max_steps, void *stream) {
     Model *M = (Model *)model;
     cudaStream_t s = (cudaStream_t)stream;
-    if (!M || !M->loop || max_steps < 0 || !s) {
-        set_error("f2d_model_loop_run: needs a loop, max_steps >= 0 and a non-default stream");
+    if (!M || !M->loop || max_steps < 0) {
+        set_error("f2d_model_loop_run: needs a loop set up and max_steps >= 0");
         return ERR_ARG;
     }
     if (M->gmg.probe) {
@@ -1466,7 +1469,10 @@ int f2d_model_loop_run(void *model, int max_steps, void *stream) {
     }
     Model::Loop &L = *M->loop;
     if (!L.exec) {
-        int st = M->loop_build(s);
+        if (!L.capture)
+            TRY(cuda_status(cudaStreamCreateWithFlags(&L.capture, cudaStreamNonBlocking),
+                            "loop capture stream"));
+        int st = M->loop_build(L.capture);
         if (st) {
             if (L.exec) cudaGraphExecDestroy(L.exec);
             if (L.graph) cudaGraphDestroy(L.graph);

@@ -276,7 +276,7 @@ typedef struct f2d_loop_state {
 int f2d_model_loop_setup(void *model, const f2d_loop_desc *ld, void *stream);
 /* diagnostics and Output.do at the current time (core/fluid2d.py:199-214) */
 int f2d_model_loop_start(void *model, void *stream);
-/* asynchronous; stream must not be the legacy default stream */
+/* asynchronous (the graph is captured once on a private stream) */
 int f2d_model_loop_run(void *model, int max_steps, void *stream);
 /* synchronous read of the clock */
 int f2d_model_loop_state(void *model, f2d_loop_state *st, void *stream);

@@ -110,6 +110,7 @@ def reference_loop(core, wl, kw, lk, tmpdir):
     reference's own Output writing into the in-memory netCDF recorder."""
     import types
     R, p, g = reference_model(core, wl, kw, with_param=True)
+    init_state = R.var.state.copy()
     # the domain area is a size-1 array there (core/grid.py domain_integration
     # over mpitools), which makes every diagnostic a size-1 array; numpy 2
     # no longer converts those to the scalars that Output.write_diag stores
@@ -143,7 +144,7 @@ def reference_loop(core, wl, kw, lk, tmpdir):
     files = refshim.RecordingDataset.FILES
     his = files[out.hisfile]["variables"]
     dia = files[out.diagfile]["variables"]
-    return R, {k: v.a for k, v in his.items()}, {k: v.a for k, v in dia.items()}
+    return R, {k: v.a for k, v in his.items()}, {k: v.a for k, v in dia.items()}, init_state
 
 
 def main_loop(core):
@@ -153,8 +154,13 @@ def main_loop(core):
     for name, (mk, kw, lk) in LOOP_CASES.items():
         wl = mk()
         with tempfile.TemporaryDirectory() as tmp:
-            R, his, dia = reference_loop(core, wl, kw, lk, tmp)
+            R, his, dia, R0_state = reference_loop(core, wl, kw, lk, tmp)
         p, O = stepper.from_workload(wl, **kw)
+        # the initial state is stored: numpy's transcendental ufuncs (exp,
+        # tanh, ...) round differently on other CPU architectures, so the
+        # workload generators are not bit-reproducible across machines
+        init_state = O.state.copy()
+        assert np.array_equal(R0_state, init_state), name
         out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"])
         t, kt, dts, reason = stepper.loop(O, p, lk["tend"], kw["dt"], out,
                                           exacthistime=lk["exacthistime"],
@@ -175,7 +181,7 @@ def main_loop(core):
                   diag_t=dia["t"], diag_kt=dia["kt"], diag_names=np.array(names),
                   diag=np.array([dia[k] for k in names]).T,
                   diag64=np.array([[d[2][k] for k in names] for d in out.diag]),
-                  dts=np.array(dts), final_state=O.state,
+                  dts=np.array(dts), init_state=init_state, final_state=O.state,
                   var_to_save=np.array(lk["var_to_save"]),
                   params=np.array([repr(dict(model=wl["model"], nx=wl["nx"], ny=wl["ny"],
                                              Lx=wl["Lx"], Ly=wl["Ly"],

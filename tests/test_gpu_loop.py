@@ -48,14 +48,38 @@ def _setup_kw(lk, **over):
     return d
 
 
-def _model(wl, kw, variant):
+def _model(wl, kw, variant, init=None):
+    """A device model started from the fixture's initial state (the workload
+    generators use numpy's transcendental ufuncs, whose last-bit rounding
+    differs between CPU architectures) or from the oracle's."""
     import torch
     from fluid2d_gb300 import engine
     from oracle import stepper
-    p, O = stepper.from_workload(wl, **kw)
+    if init is None:
+        p, O = stepper.from_workload(wl, **kw)
+        init = O.state
     G = engine.from_workload(wl, variant=variant, **kw)
-    G.var.state.copy_(torch.from_numpy(O.state).cuda())
+    G.var.state.copy_(torch.from_numpy(np.ascontiguousarray(init)).cuda())
     return G
+
+
+def _oracle(wl, kw, init):
+    from oracle import stepper
+    p, O = stepper.from_workload(wl, **kw)
+    O.state[:] = init
+    O.diagnostics()
+    return p, O
+
+
+def _assert_state_equal(G, ref):
+    st = G.var.state.cpu().numpy()
+    bad = []
+    for k, nm in enumerate(G.var.varname_list):
+        if not np.array_equal(st[k], ref[k]):
+            jj, ii = np.nonzero(st[k] != ref[k])
+            bad.append((nm, len(jj), sorted(set(jj.tolist()))[:8], sorted(set(ii.tolist()))[:8],
+                        float(np.abs(st[k] - ref[k]).max())))
+    assert not bad, bad
 
 
 def _relmax(a, b):
@@ -67,7 +91,7 @@ def _relmax(a, b):
 @pytest.mark.parametrize("name", NAMES)
 def test_device_loop_matches_reference_loop(name, variant):
     z, wl, kw, lk = _fixture(name)
-    G = _model(wl, kw, variant)
+    G = _model(wl, kw, variant, z["init_state"])
     st = G.loop(lk["tend"], **_setup_kw(lk))
     assert st["status"] == "tend"
     his, diag = st["his"], st["diag"]
@@ -80,7 +104,7 @@ def test_device_loop_matches_reference_loop(name, variant):
         assert np.array_equal(np.array([h[1] for h in his], np.int32), z["his_kt"])
         for v in lk["var_to_save"]:
             assert np.array_equal(np.array([h[2][v] for h in his]), z["his_" + v]), v
-        assert np.array_equal(G.var.state.cpu().numpy(), z["final_state"])
+        _assert_state_equal(G, z["final_state"])
     else:
         assert _relmax(t, z["his_t64"]) < 1e-12
         for v in lk["var_to_save"]:
@@ -93,16 +117,18 @@ def test_device_loop_matches_reference_loop(name, variant):
     for q, k in enumerate(names):
         ref = z["diag64"][:, q]
         scale = max(np.abs(ref).max(), 1e-300)
-        # dkedt, dvdt are differences of sums divided by dt: looser
+        # sums: relative 1e-10 of the largest value, or 1e-13 absolute for
+        # the integrals that vanish up to rounding (mean vorticity of a
+        # periodic flow); dkedt, dvdt are differences of sums over dt
         tol = 1e-6 if k in ("dkedt", "dvdt") else 1e-10
-        assert np.abs(rows[:, q] - ref).max() <= tol * scale + 1e-18, k
+        assert np.abs(rows[:, q] - ref).max() <= tol * scale + 1e-13, k
 
 
 def test_ring_pause_and_resume_change_nothing():
     z, wl, kw, lk = _fixture("loop_euler_closed_32")
-    A = _model(wl, kw, "exact")
+    A = _model(wl, kw, "exact", z["init_state"])
     a = A.loop(lk["tend"], **_setup_kw(lk))
-    B = _model(wl, kw, "exact")
+    B = _model(wl, kw, "exact", z["init_state"])
     b = B.loop(lk["tend"], **_setup_kw(lk, his_cap=2, diag_cap=3))
     assert [h[:2] for h in a["his"]] == [h[:2] for h in b["his"]]
     for x, y in zip(a["his"], b["his"]):
@@ -115,7 +141,7 @@ def test_ring_pause_and_resume_change_nothing():
 def test_max_steps_bounds_a_launch_and_the_run_continues():
     import torch
     z, wl, kw, lk = _fixture("loop_euler_closed_32")
-    G = _model(wl, kw, "exact")
+    G = _model(wl, kw, "exact", z["init_state"])
     G.loop_setup(lk["tend"], **_setup_kw(lk, his_cap=16, diag_cap=64))
     G.loop_start()
     G.loop_run(5)
@@ -127,7 +153,7 @@ def test_max_steps_bounds_a_launch_and_the_run_continues():
     assert s["status"] == "tend" and s["kt"] == int(z["his_kt"][-1])
     his, diag = G.loop_drain()
     assert np.array_equal(np.array([h[0] for h in his]), z["his_t64"])
-    assert np.array_equal(G.var.state.cpu().numpy(), z["final_state"])
+    _assert_state_equal(G, z["final_state"])
 
 
 def test_blowup_stops_after_one_step():
@@ -149,7 +175,7 @@ def test_output_files_hold_the_records(tmp_path):
     from scipy.io import netcdf_file
     from fluid2d_gb300.output import Output
     z, wl, kw, lk = _fixture("loop_boussinesq_xchannel_64x16")
-    G = _model(wl, kw, "exact")
+    G = _model(wl, kw, "exact", z["init_state"])
     out = Output.for_model(G, str(tmp_path), "shear", var_to_save=lk["var_to_save"],
                            param=dict(kw, tend=lk["tend"], modelname="boussinesq"))
     st = G.loop(lk["tend"], output=out, **_setup_kw(lk, his_cap=2))

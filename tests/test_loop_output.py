@@ -60,6 +60,7 @@ def test_loop_golden_replay(path):
     assert lk == lk2
     assert np.array_equal(wl["msk"], z["msk"])
     p, O = stepper.from_workload(wl, **kw)
+    O.state[:] = z["init_state"]
     out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"])
     t, kt, dts, reason = stepper.loop(O, p, lk["tend"], kw["dt"], out,
                                       exacthistime=lk["exacthistime"],
@@ -100,7 +101,8 @@ def test_reference_loop_pin():
     z, prm, lk = load_loop(path)
     mk, kw, _ = mg.LOOP_CASES["loop_euler_closed_32"]
     with tempfile.TemporaryDirectory() as tmp:
-        R, his, dia = mg.reference_loop(core, mk(), kw, lk, tmp)
+        R, his, dia, init = mg.reference_loop(core, mk(), kw, lk, tmp)
+    assert np.array_equal(init, z["init_state"])
     assert np.array_equal(his["t"], z["his_t"])
     assert np.array_equal(his["kt"], z["his_kt"])
     for v in lk["var_to_save"]:

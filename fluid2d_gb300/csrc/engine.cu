@@ -22,6 +22,8 @@
 #include "f2d_adv.cuh"
 #include "f2d_mixed.cuh"
 #include "f2d_loop.cuh"
+#include "f2d_flux.cuh"
+#include <string>
 
 namespace f2d {
 
@@ -775,6 +777,23 @@ struct Model {
         }
     };
     Loop *loop = nullptr;
+    // flux diagnostic (core/fluxes.py:6-213): extended state, its own RK
+    // tendencies (persistent, like the reference's Timescheme buffers) and
+    // the rev/irr flux planes
+    struct Flux {
+        Arena mem;
+        int ntr = 0, ns = 0, nflx = 0, next = 0, nfull = 0;
+        int tr[4] = {0, 0, 0, 0};  // plane of each advected quantity
+        double *X = nullptr, *Xe = nullptr, *Xw = nullptr, *S = nullptr, *FLX = nullptr,
+               *fcst = nullptr;
+        double *D[3] = {nullptr, nullptr, nullptr};
+        std::vector<std::string> names;
+    };
+    Flux *flux = nullptr;
+    int flux_setup(cudaStream_t s);
+    int flux_rhs(const double *xs, double *dxdt, cudaStream_t s);
+    int flux_forward(double sgn, cudaStream_t s);
+    int diag_fluxes(cudaStream_t s);
     int loop_body(cudaStream_t s);
     int loop_build(cudaStream_t s);
     int last_nite = 0;
@@ -1157,6 +1176,129 @@ int Model::advance(cudaStream_t s) {
     return OK;
 }
 
+// ---- flux diagnostic (core/fluxes.py)
+int Model::flux_setup(cudaStream_t s) {
+    if (flux) return OK;
+    if (kind == M_QG) {
+        set_error("flux diagnostic: not available for the quasigeostrophic model "
+                  "(core/fluxes.py:14-16)");
+        return ERR_ARG;
+    }
+    Flux *F = new (std::nothrow) Flux();
+    if (!F) return ERR_CUDA;
+    const char *trn[4];
+    F->ntr = 0;
+    trn[F->ntr] = "vorticity";
+    F->tr[F->ntr++] = (int)(plane(X, "vorticity") - X) / (int)pl;
+    if (kind == M_BOUSSINESQ) {
+        trn[F->ntr] = "buoyancy";
+        F->tr[F->ntr++] = (int)((plane(X, "buoyancy") - X) / pl);
+    }
+    trn[F->ntr] = "uc";
+    F->tr[F->ntr++] = nvar;
+    trn[F->ntr] = "vc";
+    F->tr[F->ntr++] = nvar + 1;
+    F->ns = nvar + 2;
+    F->nflx = 2 * F->ntr;
+    F->next = F->ns + F->nflx;
+    F->nfull = 2 * F->nflx;
+    const char *rr[2] = {"rev", "irr"}, *dd[2] = {"x", "y"};
+    for (int r = 0; r < 2; r++)
+        for (int t = 0; t < F->ntr; t++)
+            for (int d = 0; d < 2; d++)
+                F->names.push_back(std::string(rr[r]) + "_" + dd[d] + "_" + trn[t]);
+    const size_t ext = sizeof(double) * pl * F->next;
+    size_t oX = F->mem.add(ext), oXw = F->mem.add(ext), oS = F->mem.add(ext);
+    size_t oD[3] = {F->mem.add(ext), F->mem.add(ext), F->mem.add(ext)};
+    size_t oXe = F->mem.add(sizeof(double) * pl * F->ns);
+    size_t oF = F->mem.add(sizeof(double) * pl * F->nfull);
+    size_t oc = F->mem.add(sizeof(double) * 8);
+    int st = F->mem.alloc();
+    if (st) {
+        delete F;
+        return st;
+    }
+    F->X = F->mem.at<double>(oX);
+    F->Xw = F->mem.at<double>(oXw);
+    F->S = F->mem.at<double>(oS);
+    for (int k = 0; k < 3; k++) F->D[k] = F->mem.at<double>(oD[k]);
+    F->Xe = F->mem.at<double>(oXe);
+    F->FLX = F->mem.at<double>(oF);
+    F->fcst = F->mem.at<double>(oc);
+    flux = F;
+    return cuda_status(cudaStreamSynchronize(s), "flux setup");
+}
+
+// Fluxes.advection (core/fluxes.py:172-213): flux-form advection of every
+// quantity with its edge fluxes, the torque (Boussinesq), the fast inversion
+int Model::flux_rhs(const double *xs, double *dxdt, cudaStream_t s) {
+    Flux &F = *flux;
+    const int iu = (int)((plane(X, "u") - X) / pl), iv = (int)((plane(X, "v") - X) / pl);
+    const int ip = (int)((plane(X, "psi") - X) / pl), iw = F.tr[0];
+    const int akind = (desc.order % 2 == 0) ? 2 : 0;
+    for (int t = 0; t < F.ntr; t++) {
+        const int ik = F.tr[t], ix = F.ns + 2 * t, iy = ix + 1;
+        TRY(launch_advection(akind, msk, xs + ik * pl, dxdt + ik * pl, xs + iu * pl,
+                             xs + iv * pl, dxdt + ix * pl, dxdt + iy * pl, F.fcst, NH,
+                             desc.flux_method, desc.order, mv, nv, s));
+        TRY(launch_fillhalo(dxdt + ik * pl, NH, mv, nv, s));
+        TRY(launch_fillhalo(dxdt + ix * pl, NH, mv, nv, s));
+        TRY(launch_fillhalo(dxdt + iy * pl, NH, mv, nv, s));
+    }
+    if (kind == M_BOUSSINESQ) {  // Operators.rhs_torque (core/operators.py:303-314)
+        const int ib = F.tr[1];
+        TRY(mul_mask(dxdt + iw * pl, msk, pl, s));
+        TRY(launch_add_torque(msk, xs + ib * pl, dx, NH, desc.gravity, dxdt + iw * pl, mv, nv,
+                              s));
+        TRY(launch_fillhalo(dxdt + iw * pl, NH, mv, nv, s));
+    }
+    // Operators.invert_vorticity(dxdt, 'fast') (core/operators.py:421-498)
+    double *psi = dxdt + ip * pl;
+    TRY(launch_celltocorner(dxdt + iw * pl, B, mv, nv, s));
+    TRY(two_vcycle(gmg, psi, B, s));
+    TRY(mul_mask(psi, mskp, pl, s));
+    return launch_orthogradient(msk, psi, dx, dy, mv, nv, dxdt + iu * pl, dxdt + iv * pl, s);
+}
+
+// Timescheme.forward = RK3_SSP (core/timescheme.py:167-180) of the extended
+// state with dt * sgn
+int Model::flux_forward(double sgn, cudaStream_t s) {
+    Flux &F = *flux;
+    const size_t n = pl * F.next;
+    TRY(flux_rhs(F.X, F.D[0], s));
+    TRY(flux_rk(0, n, F.X, F.D[0], F.D[1], F.D[2], F.S, dt, sgn, s));
+    TRY(flux_rhs(F.S, F.D[1], s));
+    TRY(flux_rk(1, n, F.X, F.D[0], F.D[1], F.D[2], F.S, dt, sgn, s));
+    TRY(flux_rhs(F.S, F.D[2], s));
+    return flux_rk(2, n, F.X, F.D[0], F.D[1], F.D[2], F.S, dt, sgn, s);
+}
+
+// Fluxes.diag_fluxes(state, t, dt) (core/fluxes.py:100-170) with the model's
+// current dt and cst[3] (both on the device)
+int Model::diag_fluxes(cudaStream_t s) {
+    Flux &F = *flux;
+    const int iu = (int)((plane(X, "u") - X) / pl), iv = (int)((plane(X, "v") - X) / pl);
+    const int ip = (int)((plane(X, "psi") - X) / pl), iw = F.tr[0];
+    TRY(cuda_status(cudaMemcpyAsync(F.Xe, X, sizeof(double) * pl * nvar,
+                                    cudaMemcpyDeviceToDevice, s),
+                    "flux state copy"));
+    double *uc = F.Xe + (size_t)nvar * pl, *vc = uc + pl;
+    TRY(flux_centre(X + iu * pl, X + iv * pl, uc, vc, mv, nv, s));
+    TRY(launch_fillhalo(uc, NH, mv, nv, s));
+    TRY(launch_fillhalo(vc, NH, mv, nv, s));
+    TRY(flux_cst(F.fcst, cst, dx, dy, desc.aparab, s));
+    TRY(flux_load(F.X, F.Xe, F.ns, F.next, pl, 0u, s));
+    TRY(flux_forward(1., s));
+    TRY(cuda_status(cudaMemcpyAsync(F.Xw, F.X, sizeof(double) * pl * F.next,
+                                    cudaMemcpyDeviceToDevice, s),
+                    "flux forward copy"));
+    const unsigned neg = (1u << iu) | (1u << iv) | (1u << ip) | (1u << iw) | (1u << nvar) |
+                         (1u << (nvar + 1));
+    TRY(flux_load(F.X, F.Xe, F.ns, F.next, pl, neg, s));
+    TRY(flux_forward(-1., s));
+    return flux_final(F.nflx, F.ns, pl, F.Xw, F.X, F.FLX, dt, s);
+}
+
 // One iteration of core/fluid2d.py:235-311 on the device: set_dt with the
 // exact-history-time adjustment, model.step, t += dt, diagnostics, Output.do
 // into the rings, blow-up check.
@@ -1246,6 +1388,7 @@ int f2d_model_destroy(void *model) {
     if (M->gexec) cudaGraphExecDestroy(M->gexec);
     if (M->graph) cudaGraphDestroy(M->graph);
     delete M->loop;
+    delete M->flux;
     delete M;
     return OK;
 }
@@ -1362,6 +1505,36 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
     }
     for (int k = 0; k < nsteps; k++) TRY(cuda_status(cudaGraphLaunch(M->gexec, s), "graph launch"));
     return OK;
+}
+
+// ---- flux diagnostic (core/fluxes.py:100-213)
+int f2d_model_flux_setup(void *model, void *stream) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    return M->flux_setup((cudaStream_t)stream);
+}
+
+int f2d_model_diag_fluxes(void *model, void *stream) {
+    Model *M = (Model *)model;
+    if (!M || !M->flux) {
+        set_error("f2d_model_diag_fluxes: call f2d_model_flux_setup first");
+        return ERR_ARG;
+    }
+    return M->diag_fluxes((cudaStream_t)stream);
+}
+
+int f2d_model_flux_info(void *model, int *nfull, double **flx) {
+    Model *M = (Model *)model;
+    if (!M || !M->flux) return ERR_ARG;
+    if (nfull) *nfull = M->flux->nfull;
+    if (flx) *flx = M->flux->FLX;
+    return OK;
+}
+
+const char *f2d_model_flux_name(void *model, int k) {
+    Model *M = (Model *)model;
+    if (!M || !M->flux || k < 0 || k >= M->flux->nfull) return nullptr;
+    return M->flux->names[k].c_str();
 }
 
 // ---- device time loop (core/fluid2d.py:235-314, core/output.py:62-94)

@@ -241,6 +241,24 @@ class Model(object):
                    ctypes.byref(st))
         return nite.value, res.value, st.value
 
+    # ---- flux diagnostic: core/fluxes.py:100-213
+    def flux_setup(self):
+        self._call("f2d_model_flux_setup", self.h, _stream())
+        n, ptr = ctypes.c_int(), ctypes.POINTER(ctypes.c_double)()
+        self._call("f2d_model_flux_info", self.h, ctypes.byref(n), ctypes.byref(ptr))
+        self.flx = device_view(ctypes.cast(ptr, ctypes.c_void_p).value,
+                               (n.value, self.nyl, self.nxl))
+        self.fullflx_list = [self.L.f2d_model_flux_name(self.h, k).decode()
+                             for k in range(n.value)]
+
+    def diag_fluxes(self, x=None, t=0., dt=None):
+        """Fluxes.diag_fluxes with the model's current dt and umax: the rev/irr
+        flux planes land in ``self.flx`` (device, order ``fullflx_list``)."""
+        if not hasattr(self, "flx"):
+            self.flux_setup()
+        self._call("f2d_model_diag_fluxes", self.h, _stream())
+        return self.flx
+
     # ---- device time loop: core/fluid2d.py:190-330 with core/output.py:62-94
     LOOP_STATUS = {0: "running", 1: "tend", 2: "blowup", 3: "bad_dt"}
 

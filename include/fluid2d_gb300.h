@@ -245,6 +245,19 @@ int f2d_model_probe(void *model, int enable, int *count, double *avg_ms);
 /* number of kernel nodes in the captured step graph */
 int f2d_model_graph_kernels(void *model, int *nkernels);
 
+/* ---- flux diagnostic: Fluxes.diag_fluxes (core/fluxes.py:100-170), the
+ * reversible and irreversible parts of the advective fluxes from one RK3 step
+ * forward and one backward of an extended state (state, cell-centred u and v,
+ * edge fluxes of every advected quantity), with the model's current dt and
+ * umax (the device dt and cst[3] of the last set_dt).  Euler and Boussinesq
+ * (the reference has no flux diagnostic for QG). */
+int f2d_model_flux_setup(void *model, void *stream);
+int f2d_model_diag_fluxes(void *model, void *stream);
+/* flx: DEVICE (nfull, ny+6, nx+6) float64 in the order of f2d_model_flux_name
+ * (the reference's fullflx_list: rev_x_vorticity, rev_y_vorticity, ...) */
+int f2d_model_flux_info(void *model, int *nfull, double **flx);
+const char *f2d_model_flux_name(void *model, int k);
+
 /* ---- device time loop.  Replaces the host loop of Fluid2d.loop
  * (core/fluid2d.py:235-314) with its set_dt (:376-397), exact-history-time
  * adjustment (:245-254), blow-up stop (:306-311) and the decisions of

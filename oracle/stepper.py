@@ -757,6 +757,93 @@ def run(model, param, nsteps, dt0, t=0., callback=None):
     return t
 
 
+class Fluxes(object):
+    """core/fluxes.py:6-213: the reversible and irreversible parts of the
+    advective fluxes, from one step forward and one step back in time of an
+    extended state (the model state, the cell-centred velocities uc, vc and
+    the edge fluxes of every tracer, all advanced by the model's time scheme).
+    It shares the model's Operators (multigrid, work array, cst[3])."""
+
+    def __init__(self, model):
+        p = model.param
+        self.model, self.ope = model, model.ope
+        self.varname_list = list(model.varname_list) + ['uc', 'vc']
+        self.tracer_list = list(model.tracer_list) + ['uc', 'vc']
+        self.nvarstate = len(self.varname_list)
+        self.flx_list = ['flx_%s_%s' % (v, d) for v in self.tracer_list for d in 'xy']
+        self.fullflx_list = ['%s_%s_%s' % (r, d, v) for r in ('rev', 'irr')
+                             for v in self.tracer_list for d in 'xy']
+        nyl, nxl = model.state.shape[1:]
+        size = (self.nvarstate + len(self.flx_list), nyl, nxl)
+        self.x = np.zeros(size)
+        self.xe = np.zeros((self.nvarstate, nyl, nxl))
+        self.xwork = np.zeros(size)
+        self.flx = np.zeros((len(self.fullflx_list), nyl, nxl))
+        self.fortran_adv = K.adv_centered_flux if p.order % 2 == 0 else K.adv_upwind_flux
+        self.cst = np.array([model.grid.dx, model.grid.dy, 0.05, 0., p.aparab])
+        self.order = p.order
+        self.fs_method = self.ope.fs_method
+        self.nh = model.nh
+        self.msk = model.msk
+        self.boussinesq = isinstance(model, Boussinesq)
+        self.tscheme = Timescheme(p.timestepping, self.x)
+        self.tscheme.set(self.advection)
+
+    def diag_fluxes(self, x, t, dt):
+        vl = self.varname_list
+        iu, iv, ip, iw = vl.index('u'), vl.index('v'), vl.index('psi'), vl.index('vorticity')
+        ns = self.nvarstate
+        self.xe[:ns - 2, :, :] = x
+        y = 0.5 * (x[iu] + np.roll(x[iu], 1, axis=1))
+        self.ope.fill_halo(y)
+        self.xe[ns - 2, :, :] = y
+        y = 0.5 * (x[iv] + np.roll(x[iv], 1, axis=0))
+        self.ope.fill_halo(y)
+        self.xe[ns - 1, :, :] = y
+        self.x[:ns, :, :] = self.xe
+        self.x[ns:, :, :] = 0.
+        self.tscheme.forward(self.x, t, dt)
+        self.xwork[:, :, :] = self.x
+        self.x[:ns, :, :] = self.xe
+        for k in (iu, iv, ip, iw, ns - 2, ns - 1):
+            self.x[k] *= -1
+        self.x[ns:, :, :] = 0.
+        self.tscheme.forward(self.x, t + dt, -dt)
+        cff = 0.5 / dt
+        nflx = len(self.flx_list)
+        for k in range(nflx):
+            l = ns + k
+            j = nflx + k
+            sign = -1 if (k < 2 or k >= nflx - 4) else 1
+            self.flx[k, :, :] = cff * (self.xwork[l] + sign * self.x[l])
+            self.flx[j, :, :] = cff * (self.xwork[l] - sign * self.x[l])
+
+    def advection(self, x, t, dxdt):
+        self.rhs_adv(x, t, dxdt)
+        if self.boussinesq:
+            self.ope.rhs_torque(x, t, dxdt)
+        self.ope.invert_vorticity(dxdt, flag='fast')
+
+    def rhs_adv(self, x, t, dxdt):
+        vl = self.varname_list
+        u, v = x[vl.index('u')], x[vl.index('v')]
+        self.cst[3] = self.ope.cst[3]
+        for itrac, trac in enumerate(self.tracer_list):
+            ik = vl.index(trac)
+            y = dxdt[ik]
+            ix = self.nvarstate + itrac * 2
+            iy = ix + 1
+            xf, yf = dxdt[ix], dxdt[iy]
+            self.fortran_adv(self.msk, x[ik], y, u, v, xf, yf, self.cst, self.nh,
+                             self.fs_method, self.order)
+            self.ope.fill_halo(y)
+            self.ope.fill_halo(xf)
+            self.ope.fill_halo(yf)
+            dxdt[ik, :, :] = y
+            dxdt[ix, :, :] = xf
+            dxdt[iy, :, :] = yf
+
+
 class History(object):
     """What Output.do (core/output.py:62-94) writes, kept in memory: history
     records (t, kt and the interior of each saved plane in float32, as the

@@ -226,7 +226,53 @@ def main(core, steps=4):
         print("%-28s ok: reference == oracle stepper, bit for bit, %d steps" % (name, steps))
 
 
+# ------------------------------------------------------ flux diagnostics
+FLUX_CASES = {
+    "fluxes_euler_closed_32": lambda: W.dipole(32, 32, seed=1),
+    "fluxes_boussinesq_xchannel_64x16": lambda: W.shear(64, 16, seed=3, delta=0.1),
+}
+
+
+def main_fluxes(core, steps=2):
+    """Fluxes.diag_fluxes (core/fluxes.py:100-170) of the reference, on the
+    reference model's state after each of `steps` steps, against the oracle's
+    restatement (stepper.Fluxes), bit for bit."""
+    refshim.install(core)
+    for name, mk in FLUX_CASES.items():
+        wl = mk()
+        R, p, g = reference_model(core, wl, {}, with_param=True)
+        import fluxes as rfluxes
+        F = rfluxes.Fluxes(p, g, R.ope)
+        pO, O = stepper.from_workload(wl)
+        init_state = O.state.copy()
+        assert np.array_equal(R.var.state, init_state), name
+        OF = stepper.Fluxes(O)
+        assert OF.fullflx_list == list(F.fullflx_list), name
+        dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
+        t = 0.
+        flx = []
+        for k in range(steps):
+            R.ope.cst[3] = R.diags["maxspeed"]
+            with contextlib.redirect_stdout(io.StringIO()):
+                R.step(t, dt)
+                R.diagnostics(R.var, t + dt)
+            t = stepper.run(O, pO, 1, dt, t=t)
+            assert np.array_equal(R.var.state, O.state), (name, k)
+            F.diag_fluxes(R.var.state, t, dt)
+            OF.diag_fluxes(O.state, t, dt)
+            assert np.array_equal(F.flx, OF.flx), (name, k)
+            assert np.array_equal(R.var.state, O.state), (name, k)
+            flx.append(OF.flx.copy())
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), msk=wl["msk"],
+                            init_state=init_state, dt=dt, flx=np.array(flx),
+                            final_state=O.state, names=np.array(OF.fullflx_list),
+                            model=np.array([wl["model"]]))
+        print("%-34s ok: reference Fluxes == oracle Fluxes, bit for bit, %d calls"
+              % (name, steps))
+
+
 if __name__ == "__main__":
     core = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLUID2D_CORE", DEFAULT_CORE)
     main(core)
     main_loop(core)
+    main_fluxes(core)

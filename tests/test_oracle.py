@@ -20,7 +20,7 @@ from tests import _cases as C
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
-                if not os.path.basename(p).startswith("loop_"))
+                if not os.path.basename(p).startswith(("loop_", "fluxes_")))
 
 
 def K():

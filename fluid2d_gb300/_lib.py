@@ -176,7 +176,8 @@ class LoopDesc(ctypes.Structure):
                 ("rescaledtime", ctypes.c_int), ("nsave", ctypes.c_int),
                 ("save", ctypes.c_int * 8), ("his_cap", ctypes.c_int), ("diag_cap", ctypes.c_int),
                 ("t", ctypes.c_double), ("tnexthis", ctypes.c_double),
-                ("tnextdiag", ctypes.c_double), ("kt", ctypes.c_int)]
+                ("tnextdiag", ctypes.c_double), ("kt", ctypes.c_int),
+                ("diag_fluxes", ctypes.c_int)]
 
 
 class LoopState(ctypes.Structure):
@@ -214,7 +215,7 @@ SIGNATURES.update({
     "f2d_model_loop_start": [_P, _P],
     "f2d_model_loop_run": [_P, _I, _P],
     "f2d_model_loop_state": [_P, ctypes.POINTER(LoopState), _P],
-    "f2d_model_loop_drain": [_P, _P, _P, _P, _P, _PI, _PI, _P],
+    "f2d_model_loop_drain": [_P, _P, _P, _P, _P, _P, _PI, _PI, _P],
 })
 
 EXTRA = {

@@ -768,7 +768,8 @@ struct Model {
         LoopRings r{};
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
-        cudaGraphConditionalHandle h = 0;
+        cudaGraphConditionalHandle h = 0;      // WHILE: run another step
+        cudaGraphConditionalHandle hflux = 0;  // IF: flux diagnostic this step
         cudaStream_t capture = nullptr;  // private stream the graph is captured on
         ~Loop() {
             if (exec) cudaGraphExecDestroy(exec);
@@ -1307,50 +1308,88 @@ int Model::loop_body(cudaStream_t s) {
     TRY(loop_pre(loop->clock, loop->k, dt, cst, advc, diag, s));
     TRY(advance(s));
     TRY(diagnostics(s));
-    TRY(loop_post(loop->clock, loop->k, diag, loop->r, loop->h, s));
+    TRY(loop_post(loop->clock, loop->k, diag, loop->r, loop->h, loop->hflux, s));
     return loop_snapshot(loop->clock, loop->r, s);
 }
 
-// Graph: gate kernel -> WHILE node { loop_body }.  The gate and the last
-// kernel of the body set the condition; steps_left bounds every launch.
+// capture `body` into graph g after its current leaf nodes (none: at the root)
+template <typename F>
+static int capture_into(cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps, cudaStream_t s,
+                        F body) {
+    TRY(cuda_status(cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(),
+                                                  nullptr, deps.size(),
+                                                  cudaStreamCaptureModeThreadLocal),
+                    "capture begin"));
+    int st = body();
+    cudaGraph_t out = nullptr;
+    int st2 = cuda_status(cudaStreamEndCapture(s, &out), "capture end");
+    TRY(st);
+    return st2;
+}
+
+// nodes of g without dependents
+static int graph_leaves(cudaGraph_t g, std::vector<cudaGraphNode_t> &leaves) {
+    size_t n = 0;
+    TRY(cuda_status(cudaGraphGetNodes(g, nullptr, &n), "graph nodes"));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) TRY(cuda_status(cudaGraphGetNodes(g, nodes.data(), &n), "graph nodes"));
+    leaves.clear();
+    for (size_t q = 0; q < n; q++) {
+        size_t nd = 0;
+        TRY(cuda_status(cudaGraphNodeGetDependentNodes(nodes[q], nullptr, nullptr, &nd),
+                        "graph dependents"));
+        if (nd == 0) leaves.push_back(nodes[q]);
+    }
+    return OK;
+}
+
+static int add_conditional(cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps,
+                           cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                           cudaGraph_t *body) {
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    TRY(cuda_status(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr,
+                                     deps.size(), &p),
+                    "conditional node"));
+    *body = p.conditional.phGraph_out[0];
+    return OK;
+}
+
+// Graph: gate kernel -> WHILE node { loop_body [-> IF node { flux diagnostic }] }.
+// The gate and the last kernel of the body set the WHILE condition, which
+// steps_left bounds in every launch; k_loop_post sets the IF condition when
+// the step writes a history record.
 int Model::loop_build(cudaStream_t s) {
     cudaGraph_t g = nullptr;
     TRY(cuda_status(cudaGraphCreate(&g, 0), "loop graph"));
     loop->graph = g;
     TRY(cuda_status(cudaGraphConditionalHandleCreate(&loop->h, g, 0, cudaGraphCondAssignDefault),
                     "loop condition"));
-    TRY(cuda_status(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0,
-                                                  cudaStreamCaptureModeThreadLocal),
-                    "loop gate capture"));
-    int st = loop_gate(loop->clock, loop->k, loop->h, s);
-    cudaGraph_t gc = nullptr;
-    int st2 = cuda_status(cudaStreamEndCapture(s, &gc), "loop gate capture end");
-    TRY(st);
-    TRY(st2);
-    size_t n = 0;
-    TRY(cuda_status(cudaGraphGetNodes(g, nullptr, &n), "loop graph nodes"));
-    if (n != 1) {
-        set_error("loop graph: expected one gate node, found %zu", n);
-        return ERR_CUDA;
+    std::vector<cudaGraphNode_t> deps;
+    TRY(capture_into(g, deps, s, [&]() { return loop_gate(loop->clock, loop->k, loop->h, s); }));
+    TRY(graph_leaves(g, deps));
+    cudaGraph_t body = nullptr;
+    TRY(add_conditional(g, deps, loop->h, cudaGraphCondTypeWhile, &body));
+    if (loop->k.fluxes)
+        TRY(cuda_status(cudaGraphConditionalHandleCreate(&loop->hflux, body, 0,
+                                                         cudaGraphCondAssignDefault),
+                        "flux condition"));
+    deps.clear();
+    TRY(capture_into(body, deps, s, [&]() { return loop_body(s); }));
+    if (loop->k.fluxes) {
+        TRY(graph_leaves(body, deps));
+        cudaGraph_t fbody = nullptr;
+        TRY(add_conditional(body, deps, loop->hflux, cudaGraphCondTypeIf, &fbody));
+        deps.clear();
+        TRY(capture_into(fbody, deps, s, [&]() {
+            TRY(diag_fluxes(s));
+            return loop_flux_snapshot(loop->clock, loop->r, s);
+        }));
     }
-    cudaGraphNode_t gate = nullptr;
-    TRY(cuda_status(cudaGraphGetNodes(g, &gate, &n), "loop graph nodes"));
-    cudaGraphNodeParams p = {};
-    p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = loop->h;
-    p.conditional.type = cudaGraphCondTypeWhile;
-    p.conditional.size = 1;
-    cudaGraphNode_t wn = nullptr;
-    TRY(cuda_status(cudaGraphAddNode(&wn, g, &gate, nullptr, 1, &p), "loop while node"));
-    cudaGraph_t body = p.conditional.phGraph_out[0];
-    TRY(cuda_status(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
-                                                  cudaStreamCaptureModeThreadLocal),
-                    "loop body capture"));
-    st = loop_body(s);
-    cudaGraph_t bc = nullptr;
-    st2 = cuda_status(cudaStreamEndCapture(s, &bc), "loop body capture end");
-    TRY(st);
-    TRY(st2);
     return cuda_status(cudaGraphInstantiate(&loop->exec, g, 0), "loop graph instantiate");
 }
 
@@ -1561,10 +1600,12 @@ int f2d_model_loop_setup(void *model, const f2d_loop_desc *ld, void *stream) {
         set_error("f2d_model_loop_setup: rescaledtime 'enstrophy' needs an enstrophy diagnostic");
         return ERR_ARG;
     }
+    if (ld->diag_fluxes) TRY(M->flux_setup(s));
     delete M->loop;
     M->loop = new (std::nothrow) Model::Loop();
     if (!M->loop) return ERR_CUDA;
     Model::Loop &L = *M->loop;
+    const int nfull = ld->diag_fluxes ? M->flux->nfull : 0;
     const int nd = NDIAG[M->kind];
     const size_t per = (size_t)M->desc.ny * M->desc.nx * (ld->nsave > 0 ? ld->nsave : 1);
     size_t o_clock = L.mem.add(sizeof(LoopClock));
@@ -1572,6 +1613,8 @@ int f2d_model_loop_setup(void *model, const f2d_loop_desc *ld, void *stream) {
     size_t o_ht = L.mem.add(sizeof(double) * ld->his_cap);
     size_t o_hk = L.mem.add(sizeof(int) * ld->his_cap);
     size_t o_diag = L.mem.add(sizeof(double) * (size_t)(nd + 4) * ld->diag_cap);
+    size_t o_flx = L.mem.add(sizeof(float) * (size_t)M->desc.ny * M->desc.nx * nfull *
+                             ld->his_cap);
     TRY(L.mem.alloc());
     L.clock = L.mem.at<LoopClock>(o_clock);
     L.k.adaptable = M->desc.adaptable_dt;
@@ -1596,6 +1639,10 @@ int f2d_model_loop_setup(void *model, const f2d_loop_desc *ld, void *stream) {
     L.r.nv = M->nv;
     L.r.nsave = ld->nsave;
     for (int q = 0; q < ld->nsave; q++) L.r.planes[q] = ld->save[q];
+    L.k.fluxes = ld->diag_fluxes ? 1 : 0;
+    L.r.nfull = nfull;
+    L.r.flx = nfull ? L.mem.at<float>(o_flx) : nullptr;
+    L.r.FLX = nfull ? M->flux->FLX : nullptr;
     LoopClock c;
     memset(&c, 0, sizeof(c));
     c.t = ld->t;
@@ -1622,8 +1669,17 @@ int f2d_model_loop_start(void *model, void *stream) {
     }
     cudaStream_t s = (cudaStream_t)stream;
     TRY(M->diagnostics(s));
+    if (M->loop->k.fluxes) {
+        // set_dt then the flux diagnostic (core/fluid2d.py:203-210)
+        k_set_dt<<<1, 1, 0, s>>>(M->dt, M->cst, (SplitConst *)M->advc, M->diag,
+                                 M->desc.adaptable_dt, M->desc.dt, M->desc.cfl,
+                                 M->dx < M->dy ? M->dx : M->dy, M->desc.dtmax);
+        TRY(launch_status("set_dt"));
+        TRY(M->diag_fluxes(s));
+    }
     TRY(loop_record(M->loop->clock, M->loop->k, M->diag, M->loop->r, s));
-    return loop_snapshot(M->loop->clock, M->loop->r, s);
+    TRY(loop_snapshot(M->loop->clock, M->loop->r, s));
+    return loop_flux_snapshot(M->loop->clock, M->loop->r, s);
 }
 
 // Run steps until t >= tend, a blow-up, a full ring or max_steps steps,
@@ -1682,8 +1738,8 @@ int f2d_model_loop_state(void *model, f2d_loop_state *out, void *stream) {
 // Copy the records waiting in the rings to host memory and empty the rings.
 // his: nhis x nsave x ny x nx float32; his_t, his_kt: nhis; diag_rows:
 // ndiag x (ndiag_values + 4) float64.  Null outputs are skipped.
-int f2d_model_loop_drain(void *model, float *his, double *his_t, int *his_kt, double *diag_rows,
-                         int *nhis, int *ndiag, void *stream) {
+int f2d_model_loop_drain(void *model, float *his, float *flx, double *his_t, int *his_kt,
+                         double *diag_rows, int *nhis, int *ndiag, void *stream) {
     Model *M = (Model *)model;
     cudaStream_t s = (cudaStream_t)stream;
     if (!M || !M->loop) return ERR_ARG;
@@ -1697,6 +1753,11 @@ int f2d_model_loop_drain(void *model, float *his, double *his_t, int *his_kt, do
         TRY(cuda_status(cudaMemcpyAsync(his, L.r.his, sizeof(float) * per * c.nhis,
                                         cudaMemcpyDeviceToHost, s),
                         "loop drain his"));
+    const size_t fper = (size_t)M->desc.ny * M->desc.nx * L.r.nfull;
+    if (flx && c.nhis && fper)
+        TRY(cuda_status(cudaMemcpyAsync(flx, L.r.flx, sizeof(float) * fper * c.nhis,
+                                        cudaMemcpyDeviceToHost, s),
+                        "loop drain flx"));
     if (his_t && c.nhis)
         TRY(cuda_status(cudaMemcpyAsync(his_t, L.r.his_t, sizeof(double) * c.nhis,
                                         cudaMemcpyDeviceToHost, s),

@@ -40,6 +40,7 @@ struct LoopConst {
     int adaptable, exacthistime, rescale;
     int ike, iens, ndiag;  // diag indices of ke and enstrophy, diag count
     int his_cap, diag_cap;
+    int fluxes;  // flux diagnostic before each history record
     double dt0, cfl, hmin, dtmax;
 };
 
@@ -55,14 +56,18 @@ struct LoopRings {
     size_t pl;
     int mv, nv, nsave;
     int planes[LOOP_MAX_SAVE];
+    float *flx;        // [his_cap][nfull][ny][nx] flux records, or null
+    const double *FLX; // the flux diagnostic's planes (nfull, mv, nv)
+    int nfull;
 };
 
 int loop_gate(LoopClock *c, LoopConst k, cudaGraphConditionalHandle h, cudaStream_t s);
 int loop_pre(LoopClock *c, LoopConst k, double *dt, double *cst, void *advc, const double *diag,
              cudaStream_t s);
 int loop_post(LoopClock *c, LoopConst k, const double *diag, LoopRings r,
-              cudaGraphConditionalHandle h, cudaStream_t s);
+              cudaGraphConditionalHandle h, cudaGraphConditionalHandle hflux, cudaStream_t s);
 int loop_record(LoopClock *c, LoopConst k, const double *diag, LoopRings r, cudaStream_t s);
 int loop_snapshot(const LoopClock *c, LoopRings r, cudaStream_t s);
+int loop_flux_snapshot(const LoopClock *c, LoopRings r, cudaStream_t s);
 
 }  // namespace f2d

@@ -86,7 +86,7 @@ F2D_DEV void loop_output(LoopClock &C, const LoopConst &k, const double *diag, c
 // blow-up check, and the while-condition of the next iteration
 // (core/fluid2d.py:256-311)
 __global__ void k_loop_post(LoopClock *c, LoopConst k, const double *diag, LoopRings r,
-                            cudaGraphConditionalHandle h) {
+                            cudaGraphConditionalHandle h, cudaGraphConditionalHandle hflux) {
     LoopClock &C = *c;
     const double d = C.dt;
     if (k.rescale)  // rescaledtime == 'enstrophy': the enstrophy before the step
@@ -103,6 +103,9 @@ __global__ void k_loop_post(LoopClock *c, LoopConst k, const double *diag, LoopR
     if (C.status == LOOP_RUNNING && !(C.t < C.tend)) C.status = LOOP_TEND;
     C.steps_left -= 1;
     cudaGraphSetConditional(h, loop_can_step(C, k) ? 1u : 0u);
+    // the flux diagnostic runs before a history record is written
+    // (core/fluid2d.py:291-293)
+    if (k.fluxes) cudaGraphSetConditional(hflux, C.his_slot >= 0 ? 1u : 0u);
 }
 
 // Output.do at the start of the loop (core/fluid2d.py:199-214): dkedt and dvdt
@@ -129,6 +132,23 @@ __global__ void k_loop_snapshot(const LoopClock *c, LoopRings r) {
     }
 }
 
+// flux record of this step: the interior of the flux planes, float32
+__global__ void k_loop_flux_snapshot(const LoopClock *c, LoopRings r) {
+    const int slot = c->his_slot;
+    if (slot < 0) return;
+    const int ny = r.mv - 2 * NH, nx = r.nv - 2 * NH;
+    const size_t per = (size_t)ny * nx;
+    const size_t total = per * r.nfull;
+    float *dst = r.flx + (size_t)slot * total;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int v = (int)(q / per);
+        const size_t rem = q - (size_t)v * per;
+        const int j = (int)(rem / nx), i = (int)(rem - (size_t)j * nx);
+        dst[q] = (float)r.FLX[(size_t)v * r.pl + off(j + NH, i + NH, r.nv)];
+    }
+}
+
 int loop_gate(LoopClock *c, LoopConst k, cudaGraphConditionalHandle h, cudaStream_t s) {
     k_loop_gate<<<1, 1, 0, s>>>(c, k, h);
     return launch_status("loop_gate");
@@ -141,8 +161,8 @@ int loop_pre(LoopClock *c, LoopConst k, double *dt, double *cst, void *advc, con
 }
 
 int loop_post(LoopClock *c, LoopConst k, const double *diag, LoopRings r,
-              cudaGraphConditionalHandle h, cudaStream_t s) {
-    k_loop_post<<<1, 1, 0, s>>>(c, k, diag, r, h);
+              cudaGraphConditionalHandle h, cudaGraphConditionalHandle hflux, cudaStream_t s) {
+    k_loop_post<<<1, 1, 0, s>>>(c, k, diag, r, h, hflux);
     return launch_status("loop_post");
 }
 
@@ -158,6 +178,19 @@ int loop_snapshot(const LoopClock *c, LoopRings r, cudaStream_t s) {
     if (blocks > 2048) blocks = 2048;
     k_loop_snapshot<<<(unsigned)blocks, 256, 0, s>>>(c, r);
     return launch_status("loop_snapshot");
+}
+
+}  // namespace f2d
+
+namespace f2d {
+
+int loop_flux_snapshot(const LoopClock *c, LoopRings r, cudaStream_t s) {
+    const size_t total = (size_t)(r.mv - 2 * NH) * (r.nv - 2 * NH) * r.nfull;
+    if (total == 0 || !r.flx) return OK;
+    size_t blocks = (total + 255) / 256;
+    if (blocks > 2048) blocks = 2048;
+    k_loop_flux_snapshot<<<(unsigned)blocks, 256, 0, s>>>(c, r);
+    return launch_status("loop_flux_snapshot");
 }
 
 }  // namespace f2d

@@ -264,7 +264,7 @@ class Model(object):
 
     def loop_setup(self, tend, freq_his=1., freq_diag=1., var_to_save=("vorticity",),
                    exacthistime=True, rescaledtime="none", his_cap=8, diag_cap=1024, t=0.,
-                   kt=0, tnexthis=0., tnextdiag=0.):
+                   kt=0, tnexthis=0., tnextdiag=0., diag_fluxes=False):
         """Set the device clock and the record rings.  t, kt, tnexthis and
         tnextdiag are a restart's values (0 for a new run)."""
         if isinstance(var_to_save, str):
@@ -284,9 +284,12 @@ class Model(object):
             d.save[q] = self.var.varname_list.index(v)
         d.his_cap, d.diag_cap = int(his_cap), int(diag_cap)
         d.t, d.tnexthis, d.tnextdiag, d.kt = float(t), float(tnexthis), float(tnextdiag), int(kt)
+        d.diag_fluxes = int(bool(diag_fluxes))
         self._call("f2d_model_loop_setup", self.h, ctypes.byref(d), _stream())
         self._loop = d
         self.var_to_save = list(var_to_save)
+        if diag_fluxes:
+            self.flux_setup()
 
     def loop_start(self):
         """Diagnostics and Output.do at the clock's time (the loop's start)."""
@@ -306,22 +309,27 @@ class Model(object):
 
     def loop_drain(self):
         """The records waiting in the rings, as (t, kt, {var: float32 array})
-        history records and (t, kt, {diag: value}) diagnostic rows; empties
-        the rings."""
+        history records (with the flux planes when the loop runs the flux
+        diagnostic) and (t, kt, {diag: value}) diagnostic rows; empties the
+        rings."""
         d = self._loop
         ny, nx = self.desc.ny, self.desc.nx
         his = np.empty((d.his_cap, max(1, d.nsave), ny, nx), np.float32)
+        fl = self.fullflx_list if d.diag_fluxes else []
+        flx = np.empty((d.his_cap, max(1, len(fl)), ny, nx), np.float32)
         ht = np.empty(d.his_cap, np.float64)
         hk = np.empty(d.his_cap, np.int32)
         names = self.diag_names + ["dkedt", "dvdt"]
         rows = np.empty((d.diag_cap, len(names) + 2), np.float64)
         nh, nd = ctypes.c_int(), ctypes.c_int()
-        self._call("f2d_model_loop_drain", self.h, his.ctypes.data, ht.ctypes.data,
-                   hk.ctypes.data, rows.ctypes.data, ctypes.byref(nh), ctypes.byref(nd),
-                   _stream())
-        recs = [(float(ht[k]), int(hk[k]),
-                 {v: his[k, q].copy() for q, v in enumerate(self.var_to_save)})
-                for k in range(nh.value)]
+        self._call("f2d_model_loop_drain", self.h, his.ctypes.data,
+                   flx.ctypes.data if fl else None, ht.ctypes.data, hk.ctypes.data,
+                   rows.ctypes.data, ctypes.byref(nh), ctypes.byref(nd), _stream())
+        recs = []
+        for k in range(nh.value):
+            f = {v: his[k, q].copy() for q, v in enumerate(self.var_to_save)}
+            f.update({"flx:" + v: flx[k, q].copy() for q, v in enumerate(fl)})
+            recs.append((float(ht[k]), int(hk[k]), f))
         diag = [(float(rows[k, 0]), int(rows[k, 1]),
                  {n: float(rows[k, 2 + q]) for q, n in enumerate(names)})
                 for k in range(nd.value)]
@@ -342,7 +350,10 @@ class Model(object):
                 diag.extend(rows)
                 return
             for t, kt, f in recs:
-                output.write_his(t, kt, f)
+                output.write_his(t, kt, {k: v for k, v in f.items() if not k.startswith("flx:")})
+                fl = {k[4:]: v for k, v in f.items() if k.startswith("flx:")}
+                if fl:
+                    output.write_flx(t, kt, fl)
             for t, kt, dg in rows:
                 output.write_diag(t, kt, dg)
 

@@ -115,31 +115,51 @@ class Output(object):
     """The history and diagnostic files of one run (core/output.py:8-152)."""
 
     def __init__(self, expdir, expname, var_to_save, msk, Lx, Ly, param=None,
-                 list_diag="all"):
+                 list_diag="all", flxlist=None):
         self.expdir, self.expname = expdir, expname
         os.makedirs(expdir, exist_ok=True)
         self.hisfile = "%s/%s_his.nc" % (expdir, expname)
         self.diagfile = "%s/%s_diag.nc" % (expdir, expname)
         msk = np.asarray(msk)
         ny, nx = msk.shape[0] - 2 * NH, msk.shape[1] - 2 * NH
-        self.nchis = NcfileIO(self.hisfile, var_to_save, msk, cell_centres(nx, Lx),
-                              cell_centres(ny, Ly), _attrs_of(param or {}))
+        attrs = _attrs_of(param or {})
+        x, y = cell_centres(nx, Lx), cell_centres(ny, Ly)
+        self.nchis = NcfileIO(self.hisfile, var_to_save, msk, x, y, attrs)
+        # the flux records (core/output.py:41-47, 75-77): same layout, one
+        # variable per rev/irr flux
+        self.flxfile = "%s/%s_flx.nc" % (expdir, expname) if flxlist else None
+        self.ncflx = NcfileIO(self.flxfile, flxlist, msk, x, y, attrs) if flxlist else None
         self.list_diag = list_diag
         self._his_created = False
+        self._flx_created = False
         self.kdiag = 0
 
     @classmethod
-    def for_model(cls, model, expdir, expname, var_to_save=None, param=None):
-        """An Output for an engine.Model (mask and domain from the model)."""
+    def for_model(cls, model, expdir, expname, var_to_save=None, param=None, fluxes=False):
+        """An Output for an engine.Model (mask and domain from the model);
+        fluxes: also the flux file (the model's flux diagnostic names)."""
         d = model.desc
+        flxlist = None
+        if fluxes:
+            if not hasattr(model, "fullflx_list"):
+                model.flux_setup()
+            flxlist = model.fullflx_list
         return cls(expdir, expname, var_to_save or getattr(model, "var_to_save", ["vorticity"]),
-                   model.msk, d.Lx, d.Ly, param=param)
+                   model.msk, d.Lx, d.Ly, param=param, flxlist=flxlist)
 
     def write_his(self, t, kt, fields):
         if not self._his_created:
             self.nchis.create()
             self._his_created = True
         self.nchis.write(fields, t, kt)
+
+    def write_flx(self, t, kt, fields):
+        if self.ncflx is None:
+            raise ValueError("this Output has no flux file (flxlist not given)")
+        if not self._flx_created:
+            self.ncflx.create()
+            self._flx_created = True
+        self.ncflx.write(fields, t, kt)
 
     def create_diag(self, names):
         with netcdf_file(self.diagfile, "w", version=2) as nc:

@@ -281,6 +281,7 @@ typedef struct f2d_loop_desc {
     int his_cap, diag_cap;        /* ring capacities, in records */
     double t, tnexthis, tnextdiag; /* clock at the start: 0, 0, 0, or a restart's */
     int kt;
+    int diag_fluxes;              /* param.diag_fluxes: flux records with the history */
 } f2d_loop_desc;
 typedef struct f2d_loop_state {
     double t, dt, tnexthis, tnextdiag;
@@ -293,11 +294,12 @@ int f2d_model_loop_start(void *model, void *stream);
 int f2d_model_loop_run(void *model, int max_steps, void *stream);
 /* synchronous read of the clock */
 int f2d_model_loop_state(void *model, f2d_loop_state *st, void *stream);
-/* HOST outputs: his nhis x nsave x ny x nx float32, his_t/his_kt nhis,
- * diag_rows ndiag x (ndiag_values + 4) float64 = t, kt, the model's
- * diagnostics (f2d_model_diagname order), dkedt, dvdt.  Empties the rings. */
-int f2d_model_loop_drain(void *model, float *his, double *his_t, int *his_kt, double *diag_rows,
-                         int *nhis, int *ndiag, void *stream);
+/* HOST outputs: his nhis x nsave x ny x nx float32, flx nhis x nfull x ny x nx
+ * float32 (flux records, with diag_fluxes), his_t/his_kt nhis, diag_rows
+ * ndiag x (ndiag_values + 4) float64 = t, kt, the model's diagnostics
+ * (f2d_model_diagname order), dkedt, dvdt.  Empties the rings. */
+int f2d_model_loop_drain(void *model, float *his, float *flx, double *his_t, int *his_kt,
+                         double *diag_rows, int *nhis, int *ndiag, void *stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -850,12 +850,15 @@ class History(object):
     netCDF 'f' variables of core/output.py:227-243 store them) and diagnostic
     rows (t, kt and every model diagnostic, incl. dkedt and dvdt)."""
 
-    def __init__(self, var_to_save, freq_his, freq_diag, tnexthis=0., tnextdiag=0.):
+    def __init__(self, var_to_save, freq_his, freq_diag, tnexthis=0., tnextdiag=0.,
+                 fluxes=None):
         self.var_to_save = list(var_to_save)
         self.freq_his, self.freq_diag = freq_his, freq_diag
         self.tnexthis, self.tnextdiag = tnexthis, tnextdiag
+        self.fluxes = fluxes
         self.his = []
         self.diag = []
+        self.flx = []
 
     def do(self, model, t, kt):
         nh = model.nh
@@ -866,6 +869,10 @@ class History(object):
             self.tnexthis += self.freq_his
             self.his.append((t, kt, {v: model.get(v)[nh:-nh, nh:-nh].astype(np.float32)
                                      for v in self.var_to_save}))
+            if self.fluxes is not None:  # the 'flx' file (core/output.py:92-93)
+                F = self.fluxes
+                self.flx.append((t, kt, {v: F.flx[k][nh:-nh, nh:-nh].astype(np.float32)
+                                         for k, v in enumerate(F.fullflx_list)}))
 
 
 def loop(model, param, tend, dt0, out, t=0., kt=0, exacthistime=True,
@@ -878,6 +885,8 @@ def loop(model, param, tend, dt0, out, t=0., kt=0, exacthistime=True,
     model.diagnostics(t)
     model.diags['dkedt'] = 0.
     model.diags['dvdt'] = 0.
+    if out.fluxes is not None:  # core/fluid2d.py:203-210
+        out.fluxes.diag_fluxes(model.state, t, set_dt(model, param, dt0))
     out.do(model, t, kt)
     reduce = 0
     dts = []
@@ -908,6 +917,8 @@ def loop(model, param, tend, dt0, out, t=0., kt=0, exacthistime=True,
         model.diagnostics(t)
         model.diags['dkedt'] = (model.diags['ke'] - ke_old) / dt
         model.diags['dvdt'] = (model.diags[ensname] - ens_old) / dt
+        if out.fluxes is not None and t >= out.tnexthis:  # core/fluid2d.py:291-293
+            out.fluxes.diag_fluxes(model.state, t, dt)
         out.do(model, t, kt)
         if model.diags['maxspeed'] > 1e3:
             reason = 'blowup'

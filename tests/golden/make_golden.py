@@ -94,6 +94,13 @@ LOOP_CASES = {
                                        dict(tend=0.1, freq_his=0.03, freq_diag=0.01,
                                             var_to_save=["vorticity", "buoyancy"],
                                             exacthistime=True)),
+    # flux diagnostic at every history record (adaptive dt, countdown)
+    "loop_boussinesq_xchannel_64x16_fluxes": (lambda: W.shear(64, 16, seed=3, delta=0.1),
+                                              dict(adaptable_dt=True, cfl=0.8, dt=0.1,
+                                                   dtmax=5.),
+                                              dict(tend=0.06, freq_his=0.02, freq_diag=0.01,
+                                                   var_to_save=["vorticity"],
+                                                   exacthistime=True, diag_fluxes=True)),
     # time rescaled by the enstrophy, adaptive dt without the countdown
     "loop_euler_perio_32_rescaled": (lambda: W.turbulence(32, 32, seed=5, k0=3.),
                                      dict(adaptable_dt=True, cfl=0.6, dt=0.1, dtmax=5.),
@@ -128,10 +135,17 @@ def reference_loop(core, wl, kw, lk, tmpdir):
     p.var_to_save = list(lk["var_to_save"])
     p.list_diag = "all"
     p.nprint = 10 ** 9
+    flx = None
+    if lk.get("diag_fluxes"):
+        import fluxes as rfluxes
+        p.diag_fluxes = True
+        flx = rfluxes.Fluxes(p, g, R.ope)
     with contextlib.redirect_stdout(io.StringIO()):
-        out = routput.Output(p, g, R.diags)
+        out = routput.Output(p, g, R.diags,
+                             flxlist=flx.fullflx_list if flx is not None else None)
     F = types.SimpleNamespace(
-        myrank=0, decay=False, modelname=wl["model"], model=R, diag_fluxes=False, output=out,
+        myrank=0, decay=False, modelname=wl["model"], model=R, diag_fluxes=flx is not None,
+        flx=flx, output=out,
         plot_interactive=False, nh=3, t=0., kt=0, tend=lk["tend"],
         exacthistime=lk["exacthistime"], adaptable_dt=kw["adaptable_dt"], dt=kw["dt"],
         dt0=kw["dt"], cfl=p.cfl, dtmax=p.dtmax, dx=g.dx, dy=g.dy, rescaledtime=lk.get("rescaledtime", "none"),
@@ -144,7 +158,10 @@ def reference_loop(core, wl, kw, lk, tmpdir):
     files = refshim.RecordingDataset.FILES
     his = files[out.hisfile]["variables"]
     dia = files[out.diagfile]["variables"]
-    return R, {k: v.a for k, v in his.items()}, {k: v.a for k, v in dia.items()}, init_state
+    his = {k: v.a for k, v in his.items()}
+    if flx is not None:
+        his.update({"flx:" + k: v.a for k, v in files[out.flxfile]["variables"].items()})
+    return R, his, {k: v.a for k, v in dia.items()}, init_state
 
 
 def main_loop(core):
@@ -161,7 +178,8 @@ def main_loop(core):
         # workload generators are not bit-reproducible across machines
         init_state = O.state.copy()
         assert np.array_equal(R0_state, init_state), name
-        out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"])
+        fl = stepper.Fluxes(O) if lk.get("diag_fluxes") else None
+        out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"], fluxes=fl)
         t, kt, dts, reason = stepper.loop(O, p, lk["tend"], kw["dt"], out,
                                           exacthistime=lk["exacthistime"],
                                           rescaledtime=lk.get("rescaledtime", "none"))
@@ -190,6 +208,14 @@ def main_loop(core):
                   loop=np.array([repr(lk)]))
         for v in lk["var_to_save"]:
             fx["his_" + v] = his[v]
+        if fl is not None:
+            assert np.array_equal(his["flx:t"], fx["his_t"]), name
+            assert np.array_equal(his["flx:kt"], fx["his_kt"]), name
+            for v in fl.fullflx_list:
+                assert np.array_equal(his["flx:" + v],
+                                      np.array([f[2][v] for f in out.flx])), (name, v)
+            fx["flx_names"] = np.array(fl.fullflx_list)
+            fx["flx"] = np.array([[f[2][v] for v in fl.fullflx_list] for f in out.flx])
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **fx)
         print("%-28s ok: reference loop == oracle loop, %d steps, %d records, %d rows"
               % (name, kt, len(out.his), len(out.diag)))

@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 NAMES = ["loop_euler_closed_32", "loop_boussinesq_xchannel_64x16",
-         "loop_euler_perio_32_rescaled"]
+         "loop_boussinesq_xchannel_64x16_fluxes", "loop_euler_perio_32_rescaled"]
 
 
 def _mg():
@@ -43,7 +43,8 @@ def _fixture(name):
 def _setup_kw(lk, **over):
     d = dict(freq_his=lk["freq_his"], freq_diag=lk["freq_diag"],
              var_to_save=lk["var_to_save"], exacthistime=lk["exacthistime"],
-             rescaledtime=lk.get("rescaledtime", "none"))
+             rescaledtime=lk.get("rescaledtime", "none"),
+             diag_fluxes=lk.get("diag_fluxes", False))
     d.update(over)
     return d
 
@@ -110,6 +111,13 @@ def test_device_loop_matches_reference_loop(name, variant):
         for v in lk["var_to_save"]:
             assert _relmax(np.array([h[2][v] for h in his]), z["his_" + v]) < 1e-6, v
         assert _relmax(G.var.state.cpu().numpy()[0], z["final_state"][0]) < 1e-9
+    if lk.get("diag_fluxes"):
+        fl = [str(n) for n in z["flx_names"]]
+        got = np.array([[h[2]["flx:" + v] for v in fl] for h in his])
+        if bitexact:
+            assert np.array_equal(got, z["flx"])
+        else:
+            assert _relmax(got, z["flx"]) < 1e-6
     names = [str(n) for n in z["diag_names"]]
     rows = np.array([[d[2][k] for k in names] for d in diag])
     assert rows.shape == z["diag64"].shape
@@ -188,6 +196,23 @@ def test_output_files_hold_the_records(tmp_path):
                                   z["his_" + v])
     with netcdf_file(out.diagfile, "r", mmap=False) as nc:
         assert np.array_equal(np.array(nc.variables["kt"][:]), z["diag_kt"])
+
+
+def test_flux_file_holds_the_flux_records(tmp_path):
+    from scipy.io import netcdf_file
+    from fluid2d_gb300.output import Output
+    z, wl, kw, lk = _fixture("loop_boussinesq_xchannel_64x16_fluxes")
+    G = _model(wl, kw, "exact", z["init_state"])
+    out = Output.for_model(G, str(tmp_path), "shear", var_to_save=lk["var_to_save"],
+                           fluxes=True)
+    st = G.loop(lk["tend"], output=out, **_setup_kw(lk, his_cap=2))
+    assert st["status"] == "tend"
+    names = [str(n) for n in z["flx_names"]]
+    with netcdf_file(out.flxfile, "r", mmap=False) as nc:
+        assert np.array_equal(np.array(nc.variables["kt"][:]), z["his_kt"])
+        for q, v in enumerate(names):
+            assert np.array_equal(np.array(nc.variables[v][:]).astype(np.float32),
+                                  z["flx"][:, q]), v
 
 
 def test_restart_continues_like_the_oracle(tmp_path):

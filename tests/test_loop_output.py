@@ -61,7 +61,8 @@ def test_loop_golden_replay(path):
     assert np.array_equal(wl["msk"], z["msk"])
     p, O = stepper.from_workload(wl, **kw)
     O.state[:] = z["init_state"]
-    out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"])
+    fl = stepper.Fluxes(O) if lk.get("diag_fluxes") else None
+    out = stepper.History(lk["var_to_save"], lk["freq_his"], lk["freq_diag"], fluxes=fl)
     t, kt, dts, reason = stepper.loop(O, p, lk["tend"], kw["dt"], out,
                                       exacthistime=lk["exacthistime"],
                                       rescaledtime=lk.get("rescaledtime", "none"))
@@ -75,10 +76,14 @@ def test_loop_golden_replay(path):
     names = [str(n) for n in z["diag_names"]]
     assert np.array_equal(np.array([[d[2][k] for k in names] for d in out.diag]), z["diag64"])
     assert np.array_equal(O.state, z["final_state"])
+    if fl is not None:
+        assert [str(n) for n in z["flx_names"]] == fl.fullflx_list
+        assert np.array_equal(np.array([[f[2][v] for v in fl.fullflx_list] for f in out.flx]),
+                              z["flx"])
 
 
 def test_loop_fixtures_exist():
-    assert len(LOOPS) >= 3
+    assert len(LOOPS) >= 4
 
 
 def test_exacthistime_lands_on_history_times():

@@ -166,7 +166,8 @@ class ModelDesc(ctypes.Structure):
                 ("Rd", ctypes.c_double), ("beta", ctypes.c_double),
                 ("hydroepsilon", ctypes.c_double), ("adaptable_dt", ctypes.c_int),
                 ("dt", ctypes.c_double), ("cfl", ctypes.c_double), ("dtmax", ctypes.c_double),
-                ("precision", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("diffusion", ctypes.c_int),
+                ("Kdiff", ctypes.c_double * 2)]
 
 
 class LoopDesc(ctypes.Structure):

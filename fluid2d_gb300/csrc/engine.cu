@@ -760,6 +760,19 @@ struct Model {
         return nullptr;
     }
     int stage_mixed(int k, cudaStream_t s);
+    // the forcing stage (the third of RK3_SSP) inverts: Boussinesq always,
+    // Euler when it diffuses (core/euler.py:156-169)
+    bool invert_at_forcing_stage() const {
+        return kind == M_BOUSSINESQ || (kind == M_EULER && desc.diffusion);
+    }
+    // add_diffusion coefficient of tracer t at the forcing stage: Kdiff times
+    // the stage coefficient (1; Boussinesq: the RK3_SSP dtcoef 1.5,
+    // core/boussinesq.py:106-112), over dx*dx (core/fortran_operators.f90:138)
+    double diffusion_coef(int t) const {
+        if (!desc.diffusion) return 0.;
+        const double K = (kind == M_BOUSSINESQ ? 1.5 : 1.) * desc.Kdiff[t];
+        return K / (dx * dx);
+    }
     // device time loop (core/fluid2d.py:235-314): clock, rings, WHILE graph
     struct Loop {
         Arena mem;
@@ -987,12 +1000,13 @@ int Model::stage(int k, cudaStream_t s) {
         a.d0 = k >= 1 ? plane(D[0], tracers[t]) : nullptr;
         a.d1 = k >= 2 ? plane(D[1], tracers[t]) : nullptr;
         a.out = plane(out, tracers[t]);
+        if (k == 2) a.diff_coef = diffusion_coef(t);
         TRY(stage_advection(a, s));
     }
     // Euler and QG do not invert at the forcing stage (kforcing = 2,
-    // core/euler.py:156-169, core/quasigeostrophic.py:160-168); Boussinesq
-    // inverts at every stage (core/boussinesq.py:114)
-    const bool inv = (kind == M_BOUSSINESQ) || k < 2;
+    // core/euler.py:156-169, core/quasigeostrophic.py:160-168) unless Euler
+    // diffuses there; Boussinesq inverts at every stage (core/boussinesq.py:114)
+    const bool inv = (kind == M_BOUSSINESQ) || k < 2 || (kind == M_EULER && desc.diffusion);
     if (!inv) return OK;
     if (kind == M_QG) {
         // dxdt[:] = 0 then dxdt[pvanom] = dxdt[pv]: the warm start is zero
@@ -1011,20 +1025,22 @@ int Model::stage(int k, cudaStream_t s) {
     o.v1 = k >= 2 ? plane(D[1], "v") : nullptr;
     o.uout = plane(out, "u");
     o.vout = plane(out, "v");
-    if (kind != M_BOUSSINESQ && k == 1) {
+    const bool inv2 = invert_at_forcing_stage();
+    if (!inv2 && k == 1) {
         // x[psi] += (dt/6)*(dx0 + dx1 + 4*0): the last stage leaves dx2[psi] = 0
         o.psi_rk = 1;
         o.psibase = plane(X, "psi");
         o.psi0 = plane(D[0], "psi");
         o.psi1 = nullptr;
         o.psiout = plane(X, "psi");
-    } else if (kind == M_BOUSSINESQ && k == 2) {
+    } else if (inv2 && k == 2) {
         o.psi_rk = 1;
         o.psibase = plane(X, "psi");
         o.psi0 = plane(D[0], "psi");
         o.psi1 = plane(D[1], "psi");
         o.psiout = plane(X, "psi");
     }
+    // Euler: u, v of the RK update are overwritten by the full solve
     if (kind != M_BOUSSINESQ && k == 2) o.rk = 0;
     return stage_ortho(o, s);
 }
@@ -1061,9 +1077,10 @@ int Model::stage_mixed(int k, cudaStream_t s) {
         a.order = desc.order;
         a.mv = mv;
         a.nv = nv;
+        if (k == 2) a.diff_coef = (float)diffusion_coef(t);
         TRY(stage_advection_mixed(a, s));
     }
-    const bool inv = (kind == M_BOUSSINESQ) || k < 2;
+    const bool inv = (kind == M_BOUSSINESQ) || k < 2 || (kind == M_EULER && desc.diffusion);
     if (!inv) return OK;
     double *psik = plane(D[k], "psi");
     if (kind == M_QG) TRY(cuda_status(cudaMemsetAsync(psik, 0, pl * 8, s), "qg warm start"));
@@ -1089,13 +1106,13 @@ int Model::stage_mixed(int k, cudaStream_t s) {
     o.sv = k < 2 ? planef(outf, "v") : nullptr;
     o.xu = k == 2 ? plane(X, "u") : nullptr;
     o.xv = k == 2 ? plane(X, "v") : nullptr;
-    if (kind != M_BOUSSINESQ && k == 1) {
+    if (!invert_at_forcing_stage() && k == 1) {
         o.psi_rk = 1;
         o.psibase = plane(X, "psi");
         o.psi0 = plane(D[0], "psi");
         o.psi1 = nullptr;
         o.psiout = plane(X, "psi");
-    } else if (kind == M_BOUSSINESQ && k == 2) {
+    } else if (invert_at_forcing_stage() && k == 2) {
         o.psi_rk = 1;
         o.psibase = plane(X, "psi");
         o.psi0 = plane(D[0], "psi");

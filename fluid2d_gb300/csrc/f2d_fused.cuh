@@ -89,6 +89,9 @@ struct AdvStage {
     // torque (Boussinesq, core/operators.py:303-314): dq = dq*msk + g db/dx
     const double *buoy;       // null: no torque
     double torque_coef;       // 0.5*gravity/dx
+    // diffusion (core/fortran_operators.f90:125-156 add_diffusion), added after
+    // the torque: dq += coef*sum(msk_nb*(q_nb - q)) where msk == 1; 0: none
+    double diff_coef;         // Kdiff/(dx*dx), Kdiff already scaled by the stage coef
     // RK combination written in the same pass: out = base + c*(sum of tendencies)
     int rk;                   // 0 none, 1: out = base + dt*dq, 2: out = base + (dt/4)(d0+dq),
                               // 3: out = base + (dt/6)(d0 + d1 + 4 dq)

@@ -13,6 +13,7 @@ struct AdvMixed {
     float *dq;                  // tendency (float, interior + periodic halo)
     const float *buoy;          // Boussinesq torque: stage buoyancy (null: none)
     float torque_coef;          // 0.5*gravity/dx
+    float diff_coef;            // add_diffusion coefficient Kdiff/(dx*dx), 0: none
     int rk;                     // 1, 2: sout = stage combination; 3: xout += (dt/6)(...)
     const float *sbase, *d0, *d1;
     float *sout;

@@ -759,6 +759,14 @@ __global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
         const int ml = sl > 1 ? sl : 1, mr = sr > 1 ? sr : 1;
         if (ml + mr == 4) y = y + (a.buoy[p + 1] - a.buoy[p - 1]) * a.torque_coef * (double)mc;
     }
+    if (a.diff_coef != 0. && a.msk[p] == 1) {  // add_diffusion, Fortran term order
+        const double t = a.q[p];
+        const double lap = (double)a.msk[p - 1] * (a.q[p - 1] - t) +
+                           (double)a.msk[p + 1] * (a.q[p + 1] - t) +
+                           (double)a.msk[p - nv] * (a.q[p - nv] - t) +
+                           (double)a.msk[p + nv] * (a.q[p + nv] - t);
+        y = y + a.diff_coef * lap;
+    }
     const double dt = a.rk ? *a.dt : 0.;
     const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
     int rows[3], cols[3], nr = 0, nc = 0;

@@ -86,6 +86,14 @@ __global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
         const int ml = sl > 1 ? sl : 1, mr = sr > 1 ? sr : 1;
         if (ml + mr == 4) y = y + (a.buoy[p + 1] - a.buoy[p - 1]) * a.torque_coef;
     }
+    if (a.diff_coef != 0.f && a.msk[p] == 1) {  // add_diffusion
+        const float t = a.q[p];
+        const float lap = (float)a.msk[p - 1] * (a.q[p - 1] - t) +
+                          (float)a.msk[p + 1] * (a.q[p + 1] - t) +
+                          (float)a.msk[p - nv] * (a.q[p - nv] - t) +
+                          (float)a.msk[p + nv] * (a.q[p + nv] - t);
+        y = y + a.diff_coef * lap;
+    }
     const float dt = a.dtf[0];
     const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
     int rows[3], cols[3], nr = 0, nc = 0;

@@ -122,7 +122,8 @@ class Model(object):
     def __init__(self, modelname="euler", nx=128, ny=128, Lx=1., Ly=1., geometry="closed",
                  msk=None, order=5, flux_splitting_method="parabolic", aparab=0.05,
                  gravity=1., Rd=1., beta=0., hydroepsilon=1., adaptable_dt=False, dt=0.1,
-                 cfl=0.5, dtmax=5., precision="fp64", variant="product"):
+                 cfl=0.5, dtmax=5., precision="fp64", variant="product", diffusion=False,
+                 Kdiff=0.):
         self.variant = variant
         self.L = _lib.lib(variant)
         self.modelname = modelname
@@ -140,6 +141,13 @@ class Model(object):
         d.adaptable_dt = int(bool(adaptable_dt))
         d.dt, d.cfl, d.dtmax = float(dt), float(cfl), float(dtmax)
         d.precision = {"fp64": 0, "mixed": 1}[precision]
+        # Kdiff: one value for every tracer, or {tracer: value}
+        # (core/operators.py:146-152)
+        d.diffusion = int(bool(diffusion))
+        tracers = {"euler": ["vorticity"], "boussinesq": ["vorticity", "buoyancy"],
+                   "quasigeostrophic": ["pv"]}[modelname]
+        for q, tr in enumerate(tracers):
+            d.Kdiff[q] = float(Kdiff[tr] if isinstance(Kdiff, dict) else Kdiff)
         self.desc = d
         h = ctypes.c_void_p()
         self._call("f2d_model_create", ctypes.byref(d), self.msk.ctypes.data, ctypes.byref(h))

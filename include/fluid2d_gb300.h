@@ -212,7 +212,10 @@ typedef struct f2d_model_desc {
     double hydroepsilon;
     int adaptable_dt;    /* core/fluid2d.py:378-391 */
     double dt, cfl, dtmax;
-    int precision;       /* 0: float64 */
+    int precision;       /* 0: float64, 1: mixed (float32 fluxes and multigrid) */
+    int diffusion;       /* param.diffusion: add_diffusion at the forcing stage */
+    double Kdiff[2];     /* param.Kdiff of the advected tracers: [0] vorticity / pv,
+                            [1] buoyancy (core/operators.py:146-152) */
 } f2d_model_desc;
 /* msk_host: HOST int8 cell mask (ny+6, nx+6) including the geometry's halo */
 int f2d_model_create(const f2d_model_desc *d, const int8_t *msk_host, void **model);

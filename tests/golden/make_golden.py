@@ -46,6 +46,13 @@ def cases():
         "euler_perio_32": (W.turbulence(32, 32, seed=5, k0=3.), {}),
         "boussinesq_xchannel_64x16": (W.shear(64, 16, seed=3, delta=0.1), {}),
         "qg_closed_32": (qg, {"Rd": 0.3, "beta": 2.0}),
+        # diffusion at the forcing stage (core/operators.py:292-300)
+        "euler_closed_32_diffusion": (W.dipole(32, 32, seed=1),
+                                      {"diffusion": True, "Kdiff": 2e-3}),
+        "boussinesq_xchannel_64x16_diffusion": (W.shear(64, 16, seed=3, delta=0.1),
+                                                {"diffusion": True, "Kdiff": 1e-3}),
+        "qg_closed_32_diffusion": (qg, {"Rd": 0.3, "beta": 2.0, "diffusion": True,
+                                        "Kdiff": 2e-3}),
     }
 
 

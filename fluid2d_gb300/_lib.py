@@ -21,9 +21,10 @@ CSRC = os.path.join(_HERE, "csrc")
 BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
-           "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu", "timeloop.cu", "fluxdiag.cu"]
+           "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu", "timeloop.cu", "fluxdiag.cu",
+           "kernels_walls.cu"]
 HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh",
-           "f2d_loop.cuh", "f2d_flux.cuh"]
+           "f2d_loop.cuh", "f2d_flux.cuh", "f2d_walls.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-fvisibility=hidden"]
@@ -209,6 +210,7 @@ SIGNATURES.update({
     "f2d_model_probe": [_P, _I, _PI, _PDd],
     "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],
+    "f2d_model_noslip": [_P, _P, _P],
     "f2d_model_flux_setup": [_P, _P],
     "f2d_model_diag_fluxes": [_P, _P],
     "f2d_model_flux_info": [_P, _PI, _PPD],

@@ -23,6 +23,7 @@
 #include "f2d_mixed.cuh"
 #include "f2d_loop.cuh"
 #include "f2d_flux.cuh"
+#include "f2d_walls.cuh"
 #include <string>
 
 namespace f2d {
@@ -804,6 +805,17 @@ struct Model {
         std::vector<std::string> names;
     };
     Flux *flux = nullptr;
+    // no-slip walls (core/operators.py:157-184, 245-290): wall mask, boundary
+    // cells, their count, and the source buffer (Euler: the 'source' plane)
+    struct Noslip {
+        Arena mem;
+        int8_t *msk = nullptr, *mskbc = nullptr;
+        double *src = nullptr, *sum = nullptr;
+        double bcarea = 0.;
+    };
+    Noslip *noslip = nullptr;
+    int noslip_setup(const int8_t *msknoslip_host, cudaStream_t s);
+    int add_noslip(cudaStream_t s);
     int flux_setup(cudaStream_t s);
     int flux_rhs(const double *xs, double *dxdt, cudaStream_t s);
     int flux_forward(double sgn, cudaStream_t s);
@@ -1181,6 +1193,7 @@ int Model::advance(cudaStream_t s) {
     } else {
         for (int k = 0; k < 3; k++) TRY(stage(k, s));
     }
+    if (noslip) TRY(add_noslip(s));
     if (kind == M_BOUSSINESQ) {
         k_banom<<<blocks_for(pl), 256, 0, s>>>(X, pl, bref);
         TRY(launch_status("banom"));
@@ -1191,6 +1204,87 @@ int Model::advance(cudaStream_t s) {
             TRY(launch_status("qg post"));
         }
     }
+    return OK;
+}
+
+// ---- no-slip walls
+// core/operators.py:157-184: the boundary cells are the wall-mask cells with
+// a solid neighbour (np.roll over the whole array), then the halo is filled
+int Model::noslip_setup(const int8_t *mh, cudaStream_t s) {
+    std::vector<int8_t> bc(pl, 0);
+    for (int j = 0; j < mv; j++)
+        for (int i = 0; i < nv; i++) {
+            const int c = mh[off(j, i, nv)];
+            const int z = mh[off(j, (i + 1) % nv, nv)] + mh[off((j + 1) % mv, i, nv)] +
+                          mh[off(j, (i + nv - 1) % nv, nv)] + mh[off((j + mv - 1) % mv, i, nv)] -
+                          4 * c;
+            bc[off(j, i, nv)] = (z * c < 0) ? (int8_t)c : 0;
+        }
+    // fillhalo (periodic images of the interior, core/gmg/fortran_multigrid.f90:365-412)
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    for (int j = 0; j < mv; j++)
+        for (int i = 0; i < nv; i++) {
+            int jj = j < NH ? j + m2 : (j >= mv - NH ? j - m2 : j);
+            int ii = i < NH ? i + n2 : (i >= nv - NH ? i - n2 : i);
+            if (jj != j || ii != i) bc[off(j, i, nv)] = bc[off(jj, ii, nv)];
+        }
+    double area = 0.;
+    for (int j = NH; j < mv - NH; j++)
+        for (int i = NH; i < nv - NH; i++) area += bc[off(j, i, nv)];
+    if (!(area > 0)) {
+        set_error("noslip: the wall mask has no boundary cell");
+        return ERR_ARG;
+    }
+    Noslip *N = new (std::nothrow) Noslip();
+    if (!N) return ERR_CUDA;
+    size_t om = N->mem.add(pl), ob = N->mem.add(pl), os = N->mem.add(sizeof(double) * pl),
+           ou = N->mem.add(sizeof(double) * 4);
+    int st = N->mem.alloc();
+    if (st) {
+        delete N;
+        return st;
+    }
+    N->msk = N->mem.at<int8_t>(om);
+    N->mskbc = N->mem.at<int8_t>(ob);
+    N->src = kind == M_EULER ? plane(X, "source") : N->mem.at<double>(os);
+    N->sum = N->mem.at<double>(ou);
+    N->bcarea = area;
+    st = cuda_status(cudaMemcpyAsync(N->msk, mh, pl, cudaMemcpyHostToDevice, s), "noslip msk");
+    if (!st)
+        st = cuda_status(cudaMemcpyAsync(N->mskbc, bc.data(), pl, cudaMemcpyHostToDevice, s),
+                         "noslip mskbc");
+    if (!st) st = cuda_status(cudaStreamSynchronize(s), "noslip setup");
+    if (st) {
+        delete N;
+        return st;
+    }
+    delete noslip;
+    noslip = N;
+    return OK;
+}
+
+// rhs_noslip then invert_vorticity(x, 'fast') on the state
+// (core/euler.py:109-113, 171-179; core/boussinesq.py:93-94, 116-118;
+// core/quasigeostrophic.py:112-114, 171-175); Euler keeps source/dt
+int Model::add_noslip(cudaStream_t s) {
+    Noslip &N = *noslip;
+    const char *who = kind == M_QG ? "pvanom" : "vorticity";
+    if (kind == M_QG) {
+        const bool mixed = desc.precision != 0;
+        TRY(pvanom_rk(plane(X, "pvanom"), mixed ? nullptr : plane(D[0], "pv"),
+                      mixed ? nullptr : plane(D[1], "pv"), mixed ? planef(Df[0], "pv") : nullptr,
+                      mixed ? planef(Df[1], "pv") : nullptr, dt, pl, s));
+    }
+    TRY(noslip_source(N.msk, plane(X, "psi"), N.src, dx, dy, mv, nv, s));
+    // domain_integration(source) / bcarea, an unmasked sum over the interior
+    TRY(launch_reduce(2, ones, N.src, nullptr, NH, mv, nv, N.sum, gmg.work, s));
+    TRY(noslip_mean(N.src, N.sum, N.mskbc, N.bcarea, pl, s));
+    TRY(launch_fillhalo(N.src, NH, mv, nv, s));
+    TRY(plane_sub(plane(X, who), N.src, pl, s));
+    TRY(invert(X, who, false, s));
+    OrthoStage o = ortho_base(*this, X);
+    TRY(stage_ortho(o, s));
+    if (kind == M_EULER) TRY(plane_div(N.src, dt, pl, s));
     return OK;
 }
 
@@ -1445,6 +1539,7 @@ int f2d_model_destroy(void *model) {
     if (M->graph) cudaGraphDestroy(M->graph);
     delete M->loop;
     delete M->flux;
+    delete M->noslip;
     delete M;
     return OK;
 }
@@ -1560,6 +1655,28 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
         TRY(cuda_status(cudaGraphInstantiate(&M->gexec, g, 0), "graph instantiate"));
     }
     for (int k = 0; k < nsteps; k++) TRY(cuda_status(cudaGraphLaunch(M->gexec, s), "graph launch"));
+    return OK;
+}
+
+// ---- no-slip walls (core/operators.py:245-290)
+int f2d_model_noslip(void *model, const int8_t *msknoslip_host, void *stream) {
+    Model *M = (Model *)model;
+    if (!M || !msknoslip_host) {
+        set_error("f2d_model_noslip: null argument");
+        return ERR_ARG;
+    }
+    TRY(M->noslip_setup(msknoslip_host, (cudaStream_t)stream));
+    // captured graphs hold the step without the wall source: capture again
+    if (M->gexec) cudaGraphExecDestroy(M->gexec);
+    if (M->graph) cudaGraphDestroy(M->graph);
+    M->gexec = nullptr;
+    M->graph = nullptr;
+    if (M->loop) {
+        if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
+        if (M->loop->graph) cudaGraphDestroy(M->loop->graph);
+        M->loop->exec = nullptr;
+        M->loop->graph = nullptr;
+    }
     return OK;
 }
 

@@ -123,7 +123,7 @@ class Model(object):
                  msk=None, order=5, flux_splitting_method="parabolic", aparab=0.05,
                  gravity=1., Rd=1., beta=0., hydroepsilon=1., adaptable_dt=False, dt=0.1,
                  cfl=0.5, dtmax=5., precision="fp64", variant="product", diffusion=False,
-                 Kdiff=0.):
+                 Kdiff=0., noslip=False, msknoslip=None):
         self.variant = variant
         self.L = _lib.lib(variant)
         self.modelname = modelname
@@ -173,6 +173,12 @@ class Model(object):
         self._diag = device_view(ctypes.cast(dg, ctypes.c_void_p).value, (8,))
         self.diags = {}
         self.dx, self.dy = d.Lx / d.nx, d.Ly / d.ny
+        if noslip:
+            # the no-slip walls: the geometry's mask before islands are carved
+            # (core/grid.py:101), unless given
+            mns = workloads.base_mask(nx, ny, geometry) if msknoslip is None else msknoslip
+            self.msknoslip = np.ascontiguousarray(mns, dtype=np.int8)
+            self._call("f2d_model_noslip", self.h, self.msknoslip.ctypes.data, _stream())
 
     def _call(self, name, *args):
         _lib.call(name, *args, variant=self.variant)

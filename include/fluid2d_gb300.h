@@ -248,6 +248,14 @@ int f2d_model_probe(void *model, int enable, int *count, double *avg_ms);
 /* number of kernel nodes in the captured step graph */
 int f2d_model_graph_kernels(void *model, int *nkernels);
 
+/* ---- no-slip walls: after each step, the vorticity source along the walls
+ * that cancels the tangential velocity, then a fast inversion (rhs_noslip,
+ * core/operators.py:245-290 with computenoslipsourceterm,
+ * core/fortran_operators.f90:221-277; core/euler.py:109-113).  msknoslip:
+ * HOST int8 (ny+6, nx+6), the walls that are no-slip (the reference's
+ * grid.msknoslip: the geometry's mask before islands are carved). */
+int f2d_model_noslip(void *model, const int8_t *msknoslip_host, void *stream);
+
 /* ---- flux diagnostic: Fluxes.diag_fluxes (core/fluxes.py:100-170), the
  * reversible and irreversible parts of the advective fluxes from one RK3 step
  * forward and one backward of an extended state (state, cell-centred u and v,

@@ -57,6 +57,7 @@ class Param(object):
         self.gravity = 1.
         self.Rd = 1.
         self.beta = 0.
+        self.noslip = False
         self.adaptable_dt = False
         self.dt = 0.1
         self.cfl = 0.5
@@ -97,6 +98,9 @@ class Grid(object):
         if self.geometry == 'disc':
             r = np.sqrt((self.xr / self.Lx - 0.5)**2 + (self.yr / self.Ly - 0.5)**2)
             self.msk[r >= 0.5] = 0
+        # the no-slip walls are those of the geometry, before the user edits
+        # the mask (core/grid.py:101)
+        self.msknoslip = self.msk.copy()
         self.finalize_msk()
 
     def finalize_msk(self):
@@ -373,6 +377,34 @@ class Operators(object):
         self.fs_method = lst.index(param.flux_splitting_method) \
             if param.flux_splitting_method in lst else 1
         self.last_solve = (0, 0.)
+        self.msknoslip = grid.msknoslip
+        self.set_boundary_msk()
+
+    def set_boundary_msk(self):
+        """core/operators.py:157-184: the cells along the solid boundary."""
+        msk = self.msknoslip
+        z = (np.roll(msk, -1, axis=1) + np.roll(msk, -1, axis=0)
+             + np.roll(msk, +1, axis=1) + np.roll(msk, +1, axis=0) - 4 * msk)
+        z = z * msk
+        self.mskbc = self.msk * 0
+        self.mskbc[z < 0] = 1
+        self.mskbc *= self.msknoslip
+        self.fill_halo(self.mskbc)
+        self.bcarea = self.grid.domain_integration(self.mskbc)
+
+    def rhs_noslip(self, x, source):
+        """core/operators.py:245-290 (without enforce_momentum): the vorticity
+        source along the walls that cancels the tangential velocity."""
+        ip = self.varname_list.index('psi')
+        iw = self.varname_list.index(self.whosetspsi)
+        K.cornertocell(x[ip], self.work)
+        K.computenoslipsourceterm(self.msknoslip, x[ip], self.work, self.dx, self.dy,
+                                  self.nh)
+        source[:, :] = self.work
+        meansource = self.grid.domain_integration(source) / self.bcarea
+        source -= meansource * self.mskbc
+        self.fill_halo(source)
+        x[iw] -= source
 
     def rhs_adv(self, x, t, dxdt):
         iu = self.varname_list.index('u')
@@ -582,12 +614,17 @@ class _Model(object):
 
 
 class Euler(_Model):
-    """core/euler.py:12-223 (no forcing, noslip, sponge, dye, islands)."""
+    """core/euler.py:12-223 (no forcing, sponge, dye, islands)."""
     varname_list = ['vorticity', 'psi', 'u', 'v', 'source']
     tracer_list = ['vorticity']
 
     def step(self, t, dt):
         self.tscheme.forward(self.state, t, dt)
+        if self.param.noslip:  # core/euler.py:109-113, 171-179
+            source = self.get('source')
+            self.ope.rhs_noslip(self.state, source)
+            self.ope.invert_vorticity(self.state, flag='fast')
+            source /= dt
         self.set_psi_from_vorticity()
 
     def dynamics(self, x, t, dxdt):
@@ -624,16 +661,20 @@ class Euler(_Model):
 
 
 class Boussinesq(_Model):
-    """core/boussinesq.py:10-153 (no forcing, noslip, islands)."""
+    """core/boussinesq.py:10-153 (no forcing, islands)."""
     varname_list = ['vorticity', 'psi', 'u', 'v', 'buoyancy', 'banom']
     tracer_list = ['vorticity', 'buoyancy']
 
     def __init__(self, param, grid=None):
         _Model.__init__(self, param, grid)
         self.bref = self.get('buoyancy').copy()
+        self.source = np.zeros(self.state.shape[1:])
 
     def step(self, t, dt):
         self.tscheme.forward(self.state, t, dt)
+        if self.param.noslip:  # core/boussinesq.py:93-94, 116-118
+            self.ope.rhs_noslip(self.state, self.source)
+            self.ope.invert_vorticity(self.state, flag='fast')
         banom = self.get('banom')
         banom[:, :] = self.get('buoyancy') - self.bref
 
@@ -686,9 +727,13 @@ class QG(_Model):
         self.ivor = self.varname_list.index('vorticity')
         self.ipsi = self.varname_list.index('psi')
         self.Rd = param.Rd
+        self.source = np.zeros(self.state.shape[1:])
 
     def step(self, t, dt):
         self.tscheme.forward(self.state, t, dt)
+        if self.param.noslip:  # core/quasigeostrophic.py:112-114, 171-175
+            self.ope.rhs_noslip(self.state, self.source)
+            self.ope.invert_vorticity(self.state, flag='fast')
         self.set_psi_from_pv()
         self.state[self.ipva] = self.state[self.ipv] - self.pvback
         self.state[self.ivor] = (self.state[self.ipva]

@@ -53,6 +53,12 @@ def cases():
                                                 {"diffusion": True, "Kdiff": 1e-3}),
         "qg_closed_32_diffusion": (qg, {"Rd": 0.3, "beta": 2.0, "diffusion": True,
                                         "Kdiff": 2e-3}),
+        # no-slip walls (core/operators.py:245-290), with islands in the mask
+        # that keep free slip (core/grid.py:101)
+        "euler_closed_islands_48x32_noslip": (isl, {"noslip": True}),
+        "boussinesq_xchannel_64x16_noslip": (W.shear(64, 16, seed=3, delta=0.1),
+                                             {"noslip": True}),
+        "qg_closed_32_noslip": (qg, {"Rd": 0.3, "beta": 2.0, "noslip": True}),
     }
 
 

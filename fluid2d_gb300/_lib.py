@@ -24,7 +24,8 @@ SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engin
            "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu", "timeloop.cu", "fluxdiag.cu",
            "kernels_walls.cu"]
 HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh",
-           "f2d_loop.cuh", "f2d_flux.cuh", "f2d_walls.cuh"]
+           "f2d_loop.cuh", "f2d_flux.cuh", "f2d_walls.cuh",
+           "f2d_tri.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-fvisibility=hidden"]
@@ -145,6 +146,7 @@ SIGNATURES = {
     "f2d_smoothtwicewitha": [_P, _P, _P, _P, _D, _I, _I, _P],
     "f2d_smoothtwicewitha_noalloc": [_P, _P, _P, _P, _D, _I, _I, _P],
     "f2d_computeresidualwitha": [_P, _P, _P, _P, _P, _I, _I, _P],
+    "f2d_smoothtridiag": [_P, _P, _P, _P, _I, _I, _P],
     "f2d_fillhalo": [_P, _I, _I, _I, _P],
     "f2d_interpolate": [_P, _P, _P, _I, _I, _I, _I, _I, _P, _P],
     "f2d_restrict": [_P, _P, _I, _I, _I, _I, _I, _P, _P],

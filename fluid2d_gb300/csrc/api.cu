@@ -221,6 +221,18 @@ int f2d_smoothtwicewitha(const int8_t *msk, const double *A, double *x, const do
     return launch_smoothtwice(msk, A, x, b, coef, m, n, tmp, STREAM(stream));
 }
 
+int f2d_smoothtridiag(const int8_t *msk, const double *A, double *x, const double *b, int m,
+                      int n, void *stream) {
+    if (!msk || !A || !x || !b) {
+        set_error("smoothtridiag: null pointer");
+        return ERR_ARG;
+    }
+    int st = OK;
+    double *work = (double *)scratch_buffer(2 * sizeof(double) * (size_t)m * n, &st);
+    if (st) return st;
+    return launch_smoothtridiag(msk, A, x, b, m, n, work, STREAM(stream));
+}
+
 int f2d_computeresidualwitha(const int8_t *msk, const double *A, const double *x,
                              const double *b, double *y, int m, int n, void *stream) {
     if (!msk || !A || !x || !b || !y) {

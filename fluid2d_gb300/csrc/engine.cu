@@ -223,7 +223,11 @@ struct Gmg {
     // every level but a float64 finest level, which is FP64-ALU bound and
     // gains nothing from recomputing a ring of first-sweep values
     template <typename T>
-    bool fused(int l) const { return l > 0 || sizeof(T) == 4; }
+    bool fused(int l) const { return !tri && (l > 0 || sizeof(T) == 4); }
+    // line relaxation on every level (hydroepsilon*dy/dx <= 0.2,
+    // core/gmg/level.py:153-163): elimination factors per level
+    bool tri = false;
+    double *gam[MAX_LEVELS] = {}, *bet[MAX_LEVELS] = {};
     template <typename T>
     int smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream_t s);
     template <typename T>
@@ -254,18 +258,26 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
         }
         nv[l] = info[l].n + 2 * NH;
         mv[l] = info[l].m + 2 * NH;
-        if (hydroeps * info[l].dy / info[l].dx <= .2) {
-            set_error("multigrid: aspect ratio %g needs the tridiagonal relaxation "
-                      "(core/gmg/level.py:153-163), not supported on the GPU",
-                      hydroeps * info[l].dy / info[l].dx);
+        const bool t = hydroeps * info[l].dy / info[l].dx <= .2;
+        if (l == 0) tri = t;
+        if (t != tri) {
+            set_error("multigrid: levels with and without the tridiagonal relaxation");
             return ERR_ARG;
         }
+    }
+    if (tri && f32) {
+        set_error("multigrid: the tridiagonal relaxation runs in float64 only");
+        return ERR_ARG;
+    }
+    if (tri && mv[0] > 5632) {
+        set_error("multigrid: %d rows exceed the line relaxation's column buffers", mv[0]);
+        return ERR_LIMIT;
     }
     has_f32 = f32;
     // first level of the coarse CTA: the largest suffix of levels >= 1 that
     // fits in shared memory
     cs = nlev;
-    for (int l = nlev - 1; l >= 1; l--) {
+    for (int l = nlev - 1; l >= 1 && !tri; l--) {
         if (coarse_smem_bytes<double>(mv + l, nv + l, nlev - l) <= 200 * 1024) cs = l;
         else break;
     }
@@ -303,6 +315,12 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
     size_t o_solve = mem.add(sizeof(SolveState));
     size_t o_sc9 = mem.add(16 * sizeof(double));
     size_t o_ones = mem.add(maxpl);
+    size_t o_gam[MAX_LEVELS] = {}, o_bet[MAX_LEVELS] = {};
+    if (tri)
+        for (int l = 0; l < nlev; l++) {
+            o_gam[l] = mem.add(sizeof(double) * (size_t)mv[l] * nv[l]);
+            o_bet[l] = mem.add(sizeof(double) * (size_t)mv[l] * nv[l]);
+        }
     TRY(mem.alloc());
     work = mem.at<double>(o_work);
     sums = mem.at<double>(o_sums);
@@ -393,6 +411,12 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
         size_t pl = (size_t)mv[l] * nv[l];
         TRY(cuda_status(cudaMemsetAsync(d[l].r, 0, pl * sizeof(double), s), "clear"));
     }
+    if (tri)
+        for (int l = 0; l < nlev; l++) {
+            gam[l] = mem.at<double>(o_gam[l]);
+            bet[l] = mem.at<double>(o_bet[l]);
+            TRY(mg_tri_factor(d[l], l == 0 ? &an : nullptr, gam[l], bet[l], s));
+        }
     return OK;
 }
 
@@ -408,7 +432,27 @@ int Gmg::smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream
         TRY(cuda_status(cudaEventRecordWithFlags(ev[nprobe][0], s, cudaEventRecordExternal),
                         "probe record"));
     }
-    if (fused<T>(l)) {
+    if (tri) {
+        // Level.smooth with the line relaxation (core/gmg/level.py:340-368):
+        // three smoothtridiag sweeps per call, each followed by a halo fill
+        if constexpr (sizeof(T) == 8) {
+            const size_t n = (size_t)L[l].mv * L[l].nv;
+            if (xmode == X_ZERO) TRY(mg_zero(L[l].x, n, active, s));
+            if (xmode == X_PLUS_INTERP || xmode == X_INTERP) {
+                // coarsetofine writes the whole fine array (nh = 3, no halo
+                // fill) and the line relaxation reads its outer columns, so
+                // the correction is formed in r and added everywhere
+                // (core/gmg/hierarchy.py:118-126, level.py:447-470)
+                TRY(launch_interpolate(L[l].msk, L[l + 1].msk, L[l + 1].x, NH, L[l + 1].mv,
+                                       L[l + 1].nv, L[l].mv, L[l].nv, L[l].r, s));
+                TRY(mg_add(L[l].x, L[l].r, n, xmode == X_INTERP, active, s));
+            }
+            for (int k = 0; k < 3; k++) {
+                TRY(mg_tri_sweep(L[l], l == 0 ? &an : nullptr, gam[l], bet[l], active, s));
+                TRY(launch_fillhalo(L[l].x, NH, L[l].mv, L[l].nv, s));
+            }
+        }
+    } else if (fused<T>(l)) {
         TRY(mg_smooth_fused<T>(L[l], a0, c1, c2, xmode, xmode >= X_PLUS_INTERP ? &L[l + 1] : nullptr,
                                L[l].t, active, s));
         T *tmp = L[l].x;

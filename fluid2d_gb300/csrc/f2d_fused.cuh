@@ -131,5 +131,17 @@ int mg_residual_mixed(const LevelView<double> &L, const Analytic &an, const doub
                       const double *b, double *r, float *rf, const int *active, cudaStream_t s);
 int vec_axpy_const(double *x, double alpha_sub, const double *dev_scalar, size_t count,
                    cudaStream_t s);
+// line relaxation (core/gmg/fortran_multigrid.f90:215-317) of a level whose
+// operator is analytic (a0, the finest level) or stored: elimination factors
+// once, then one sweep per call (no halo fill)
+int mg_tri_factor(const LevelView<double> &L, const Analytic *a0, double *gam, double *bet,
+                  cudaStream_t s);
+int mg_tri_sweep(const LevelView<double> &L, const Analytic *a0, const double *gam,
+                 const double *bet, const int *active, cudaStream_t s);
+// x = 0 unless *active == 0
+int mg_zero(double *x, size_t n, const int *active, cudaStream_t s);
+// x = r (assign) or x += r over the whole array, unless *active == 0
+int mg_add(double *x, const double *r, size_t n, bool assign, const int *active,
+           cudaStream_t s);
 
 }  // namespace f2d

@@ -19,6 +19,8 @@ int launch_reduce(int kind, const int8_t *msk, const double *x, const double *y,
                   int n, double *out, double *work, cudaStream_t s);
 int launch_smoothtwice(const int8_t *msk, const double *A, double *x, const double *b,
                        double coef, int m, int n, double *tmp, cudaStream_t s);
+int launch_smoothtridiag(const int8_t *msk, const double *A, double *x, const double *b, int m,
+                         int n, double *work, cudaStream_t s);
 int launch_residual(const int8_t *msk, const double *A, const double *x, const double *b,
                     double *r, int m, int n, cudaStream_t s);
 int launch_fillhalo(double *x, int nh, int m, int n, cudaStream_t s);

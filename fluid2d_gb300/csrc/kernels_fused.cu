@@ -19,6 +19,7 @@
 #include "f2d_fused.cuh"
 #include "f2d_kernels.cuh"
 #include "f2d_adv.cuh"
+#include "f2d_tri.cuh"
 
 namespace f2d {
 
@@ -885,5 +886,85 @@ int vec_axpy_const(double *x, double area, const double *sum, size_t count, cuda
     template size_t coarse_smem_bytes<T>(const int *, const int *, int);
 F2D_INST(double)
 F2D_INST(float)
+
+// ------------------------------------------------------------ line relaxation
+// the finest level's analytic operator as a tridiagonal-smoother accessor
+struct AAnalytic {
+    LevelView<double> L;
+    Analytic an;
+    F2D_DEV double operator()(int k, int j, int i) const { return analytic_coef(L, an, k, j, i); }
+};
+
+int mg_tri_factor(const LevelView<double> &L, const Analytic *a0, double *gam, double *bet,
+                  cudaStream_t s) {
+    const unsigned g = (unsigned)((L.nv - 2 + 127) / 128);
+    if (a0)
+        k_tri_factor<AAnalytic><<<g, 128, 0, s>>>(L.msk, AAnalytic{L, *a0}, gam, bet, L.mv, L.nv);
+    else
+        k_tri_factor<AStored><<<g, 128, 0, s>>>(L.msk, AStored{L.A, (size_t)L.mv * L.nv, L.nv},
+                                                gam, bet, L.mv, L.nv);
+    return launch_status("tri_factor");
+}
+
+namespace {
+// per library and device: the opt-in shared memory of the two sweep kernels
+bool g_tri_configured[2][64];
+}
+
+int mg_tri_sweep(const LevelView<double> &L, const Analytic *a0, const double *gam,
+                 const double *bet, const int *active, cudaStream_t s) {
+    const size_t smem = tri_smem_bytes(L.mv);
+    int dev = 0;
+    int st0 = cuda_status(cudaGetDevice(&dev), "tri device");
+    if (st0) return st0;
+    if (smem > 48 * 1024 && dev < 64 && !g_tri_configured[a0 ? 1 : 0][dev]) {
+        int st = a0 ? cuda_status(cudaFuncSetAttribute(k_tri_sweep<AAnalytic>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       220 * 1024),
+                                  "tri smem")
+                    : cuda_status(cudaFuncSetAttribute(k_tri_sweep<AStored>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       220 * 1024),
+                                  "tri smem");
+        if (st) return st;
+        g_tri_configured[a0 ? 1 : 0][dev] = true;
+    }
+    if (a0)
+        k_tri_sweep<AAnalytic><<<1, TRI_THREADS, smem, s>>>(L.msk, AAnalytic{L, *a0}, L.x, L.b,
+                                                            gam, bet, L.mv, L.nv, active);
+    else
+        k_tri_sweep<AStored><<<1, TRI_THREADS, smem, s>>>(
+            L.msk, AStored{L.A, (size_t)L.mv * L.nv, L.nv}, L.x, L.b, gam, bet, L.mv, L.nv,
+            active);
+    return launch_status("tri_sweep");
+}
+
+__global__ void k_zero_active(double *x, size_t n, const int *active) {
+    if (active && *active == 0) return;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = 0.;
+}
+
+__global__ void k_add_active(double *x, const double *r, size_t n, int assign,
+                             const int *active) {
+    if (active && *active == 0) return;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        x[q] = assign ? r[q] : x[q] + r[q];
+}
+
+int mg_add(double *x, const double *r, size_t n, bool assign, const int *active,
+           cudaStream_t s) {
+    size_t b = (n + 255) / 256;
+    k_add_active<<<(unsigned)(b > 4096 ? 4096 : b), 256, 0, s>>>(x, r, n, assign ? 1 : 0, active);
+    return launch_status("mg_add");
+}
+
+int mg_zero(double *x, size_t n, const int *active, cudaStream_t s) {
+    size_t b = (n + 255) / 256;
+    k_zero_active<<<(unsigned)(b > 4096 ? 4096 : b), 256, 0, s>>>(x, n, active);
+    return launch_status("mg_zero");
+}
 
 }  // namespace f2d

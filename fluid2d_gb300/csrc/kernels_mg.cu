@@ -13,6 +13,7 @@
 // arrays of coarsenmatrix are stored the same way with 9 planes.
 #include "f2d_common.cuh"
 #include "f2d_kernels.cuh"
+#include "f2d_tri.cuh"
 
 namespace f2d {
 
@@ -84,6 +85,32 @@ int launch_smoothtwice(const int8_t *msk, const double *A, double *x, const doub
     k_smooth_sweep1<<<g, bl, 0, s>>>(msk, A, x, b, c1, c2, m, n, tmp);
     k_smooth_sweep2<<<g, bl, 0, s>>>(msk, A, tmp, b, c1, c2, m, n, x);
     return launch_status("smoothtwicewitha");
+}
+
+// smoothtridiag (core/gmg/fortran_multigrid.f90:215-317): factors into
+// `work` (2 m n doubles), then one sweep
+int launch_smoothtridiag(const int8_t *msk, const double *A, double *x, const double *b, int m,
+                         int n, double *work, cudaStream_t s) {
+    if (m < 8 || n < 3) return OK;  // no row in 3..m-5
+    const size_t smem = tri_smem_bytes(m);
+    if (smem > 220 * 1024) {
+        set_error("smoothtridiag: %d rows exceed the shared-memory column buffers", m);
+        return ERR_LIMIT;
+    }
+    AStored acc{A, (size_t)m * n, n};
+    double *gam = work, *bet = work + (size_t)m * n;
+    k_tri_factor<AStored><<<(n - 2 + 127) / 128, 128, 0, s>>>(msk, acc, gam, bet, m, n);
+    int st = launch_status("smoothtridiag factor");
+    if (st) return st;
+    if (smem > 48 * 1024) {
+        st = cuda_status(cudaFuncSetAttribute(k_tri_sweep<AStored>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem),
+                         "smoothtridiag smem");
+        if (st) return st;
+    }
+    k_tri_sweep<AStored><<<1, TRI_THREADS, smem, s>>>(msk, acc, x, b, gam, bet, m, n, nullptr);
+    return launch_status("smoothtridiag");
 }
 
 // r = b - A x on rows/cols 1..m-2 (0-based), masked -> 0

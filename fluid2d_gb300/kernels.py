@@ -312,6 +312,16 @@ def smoothtwicewitha(msk, A, x, b, coef, yo=None):
     X.done()
 
 
+def smoothtridiag(msk, A, x, b):
+    """core/gmg/fortran_multigrid.f90:215-317 (one vertical line-relaxation sweep)"""
+    _same(msk, x, b)
+    m, n = _mn(msk)
+    M, X, B = _i8(msk), _f64(x, True), _f64(b)
+    AP = _planes(A, 5)
+    _call("f2d_smoothtridiag", M.ptr, AP.data_ptr(), X.ptr, B.ptr, m, n, stream_handle())
+    X.done()
+
+
 def computeresidualwitha(msk, A, x, b, y):
     """core/gmg/fortran_multigrid.f90:320-362"""
     _same(msk, x, b, y)

@@ -143,6 +143,13 @@ int f2d_smoothtwicewitha(const int8_t *msk, const double *A, double *x, const do
  * buffer, so calls that overlap on the GPU race with each other. */
 int f2d_smoothtwicewitha_noalloc(const int8_t *msk, const double *A, double *x,
                                  const double *b, double coef, int m, int n, void *stream);
+/* core/gmg/fortran_multigrid.f90:215-317 smoothtridiag(msk,A,x,b), called from
+ * core/gmg/level.py:349 when hydroepsilon*dy/dx <= 0.2: one sweep of vertical
+ * line relaxation (Gauss-Seidel across columns, a Thomas solve of rows
+ * 3..m-5 per column).  No halo fill (the caller fills it).  m <= 5632.
+ * (scratch: the elimination factors) */
+int f2d_smoothtridiag(const int8_t *msk, const double *A, double *x, const double *b, int m,
+                      int n, void *stream);
 /* core/gmg/fortran_multigrid.f90:320-362 computeresidualwitha(msk,A,x,b,y),
  * core/gmg/level.py:374 */
 int f2d_computeresidualwitha(const int8_t *msk, const double *A, const double *x,

@@ -59,6 +59,11 @@ def cases():
         "boussinesq_xchannel_64x16_noslip": (W.shear(64, 16, seed=3, delta=0.1),
                                              {"noslip": True}),
         "qg_closed_32_noslip": (qg, {"Rd": 0.3, "beta": 2.0, "noslip": True}),
+        # line relaxation on every level (hydroepsilon*dy/dx <= 0.2,
+        # core/gmg/level.py:153-163): flat cells, and a small hydroepsilon
+        "euler_closed_16x96_tridiag": (W.dipole(16, 96, seed=4), {}),
+        "boussinesq_xchannel_64x16_hydro": (W.shear(64, 16, seed=3, delta=0.1),
+                                            {"hydroepsilon": 0.1}),
     }
 
 

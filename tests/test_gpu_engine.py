@@ -145,3 +145,33 @@ def test_gmg_twovcycle_and_solve(eng):
         assert nite_g == nite_o
         assert abs(res_g - res_o) <= 1e-6 * res_o
         assert np.array_equal(xg.cpu().numpy(), xo), relerr(xg.cpu().numpy(), xo)
+
+
+@pytest.mark.parametrize("geom,hyd,dyfac", [("xchannel", 0.1, 1.), ("closed", 0.1, 1.),
+                                            ("xchannel", 1., 1. / 6), ("perio", 1., 1. / 6)])
+def test_gmg_line_relaxation(eng, geom, hyd, dyfac):
+    """Hierarchies relaxed by smoothtridiag (hydroepsilon*dy/dx <= 0.2): the
+    device twoVcycle and solve equal the oracle's bit for bit (exact build);
+    the periodic solve differs only by the rounding of its norms."""
+    import torch
+    from oracle import stepper
+    m, n = 22, 70
+    msk = C.corner_mask(C.mask(m, n, geom, 0, 1))
+    dx = 4. / (n - 6)
+    dy = dx * dyfac
+    pp = {'nh': 3, 'n': n - 6, 'm': m - 6, 'omega': 8. / 9., 'dx': dx, 'dy': dy,
+          'hydroepsilon': hyd}
+    O = stepper.Gmg(pp, msk * 1.)
+    assert all(L.relaxation == 'tridiagonal' for L in O.grid)
+    G = eng.Gmg(msk, n - 6, m - 6, dx, dy, hydroepsilon=hyd, variant="exact")
+    x, b = C.field(m, n, 1), C.field(m, n, 2)
+    xo = x.copy()
+    O.twoVcycle(xo, b)
+    xg = torch.from_numpy(x).cuda()
+    G.twoVcycle(xg, torch.from_numpy(b).cuda())
+    assert np.array_equal(xg.cpu().numpy(), xo)
+    xo = x.copy()
+    O.solve(xo, b, {'maxite': 4, 'tol': 1e-11})
+    xg = torch.from_numpy(x).cuda()
+    G.solve(xg, torch.from_numpy(b).cuda())
+    assert relerr(xg.cpu().numpy(), xo) <= 1e-13

@@ -249,3 +249,26 @@ def test_multigrid_kernels(gk, variant, m, n, geom, islands, seed):
             ref = K().coarsenmatrix(L.A, L.msk, Lc.msk, 3)
             got = gk.coarsenmatrix(L.A, L.msk, Lc.msk, 3)
             check(np.asarray(got), ref, variant)
+
+
+@pytest.mark.parametrize("m,n,geom,islands,seed", [(102, 22, "closed", 0, 4),
+                                                   (70, 38, "xchannel", 2, 5),
+                                                   (134, 70, "perio", 0, 6)])
+def test_smoothtridiag(gk, variant, m, n, geom, islands, seed):
+    """The vertical line relaxation on the levels of a flat-cell hierarchy
+    (dy = dx/6), whole array compared (no halo fill inside the routine)."""
+    dx = 1. / (n - 6)
+    levs = _hierarchy(m, n, geom, islands, seed, dx=dx, dy=dx / 6)
+    for k, L in enumerate(levs):
+        if L.m + 6 < 8:
+            continue
+        mv, nv = L.mv, L.nv
+        x, b = C.field(mv, nv, 20 * k), C.field(mv, nv, 20 * k + 1)
+        A5 = np.ascontiguousarray(L.A[:, :, :5])
+        ref = x.copy()
+        for _ in range(3):
+            K().smoothtridiag(L.msk, A5, ref, b)
+        g = cuda(x)
+        for _ in range(3):
+            gk.smoothtridiag(cuda(L.msk), A5, g, cuda(b))
+        check(host(g), ref, variant)

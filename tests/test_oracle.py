@@ -37,7 +37,8 @@ def load_golden(path):
 def golden_model(path):
     from oracle import stepper
     z, prm = load_golden(path)
-    kw = {k: prm[k] for k in ("Rd", "beta", "diffusion", "Kdiff", "noslip") if k in prm}
+    kw = {k: prm[k] for k in ("Rd", "beta", "diffusion", "Kdiff", "noslip",
+                                      "hydroepsilon") if k in prm}
     p = stepper.Param(modelname=prm["model"], nx=prm["nx"], ny=prm["ny"], Lx=prm["Lx"],
                       Ly=prm["Ly"], geometry=prm["geometry"], gravity=prm["gravity"], **kw)
     g = stepper.Grid(p)

@@ -64,6 +64,13 @@ def cases():
         "euler_closed_16x96_tridiag": (W.dipole(16, 96, seed=4), {}),
         "boussinesq_xchannel_64x16_hydro": (W.shear(64, 16, seed=3, delta=0.1),
                                             {"hydroepsilon": 0.1}),
+        # centred fluxes (core/fortran_advection.f90:169-284) and the other
+        # upwind orders and flux splitting
+        "euler_closed_32_order4": (W.dipole(32, 32, seed=6), {"order": 4}),
+        "euler_perio_32_order3_minmax": (W.turbulence(32, 32, seed=7, k0=3.),
+                                         {"order": 3, "flux_splitting_method": "minmax"}),
+        "boussinesq_xchannel_64x16_order2": (W.shear(64, 16, seed=8, delta=0.1),
+                                             {"order": 2}),
     }
 
 

@@ -31,7 +31,7 @@ def test_engine_replays_reference_steps(path, variant):
     z = np.load(path, allow_pickle=False)
     prm = ast.literal_eval(str(z["params"][0]))
     kw = {k: prm[k] for k in ("Rd", "beta", "diffusion", "Kdiff", "noslip",
-                                      "hydroepsilon") if k in prm}
+                                      "hydroepsilon", "order", "flux_splitting_method") if k in prm}
     G = engine.Model(prm["model"], prm["nx"], prm["ny"], prm["Lx"], prm["Ly"],
                      prm["geometry"], msk=z["msk"], gravity=prm["gravity"], dt=float(z["dt"]),
                      variant=variant, **kw)

@@ -38,7 +38,7 @@ def golden_model(path):
     from oracle import stepper
     z, prm = load_golden(path)
     kw = {k: prm[k] for k in ("Rd", "beta", "diffusion", "Kdiff", "noslip",
-                                      "hydroepsilon") if k in prm}
+                                      "hydroepsilon", "order", "flux_splitting_method") if k in prm}
     p = stepper.Param(modelname=prm["model"], nx=prm["nx"], ny=prm["ny"], Lx=prm["Lx"],
                       Ly=prm["Ly"], geometry=prm["geometry"], gravity=prm["gravity"], **kw)
     g = stepper.Grid(p)

@@ -213,6 +213,7 @@ SIGNATURES.update({
     "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],
     "f2d_model_noslip": [_P, _P, _P],
+    "f2d_model_islands": [_P, _P, _P, _P],
     "f2d_model_flux_setup": [_P, _P],
     "f2d_model_diag_fluxes": [_P, _P],
     "f2d_model_flux_info": [_P, _PI, _PPD],

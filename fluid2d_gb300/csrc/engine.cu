@@ -877,7 +877,22 @@ struct Model {
         return nullptr;
     }
     int create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t s);
-    int invert(double *xs, const char *who, bool full, cudaStream_t s, double *ubase_out = nullptr);
+    int invert(double *xs, const char *who, bool full, cudaStream_t s, bool island = false);
+    // islands with a prescribed streamfunction (core/island.py, core/operators.py:442-444,
+    // 482-486): the right-hand-side correction and the psi offset
+    struct Islands {
+        Arena mem;
+        double *rhsp = nullptr, *psi = nullptr;
+    };
+    Islands *isl = nullptr;
+    // psi*mskp (+ the islands' psi) and psi -> (u, v) with the RK options of o
+    int ortho(OrthoStage &o, bool island, cudaStream_t s) {
+        if (island && isl) {
+            TRY(psi_island(o.psi, mskp, isl->psi, pl, s));
+            o.premasked = 1;
+        }
+        return stage_ortho(o, s);
+    }
     int stage(int k, cudaStream_t s);
     int step(cudaStream_t s);
     int advance(cudaStream_t s);
@@ -983,10 +998,11 @@ int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t 
 
 // invert_vorticity (core/operators.py:421-498), up to (not including) the
 // psi*mskp + orthogradient pass, which the caller fuses with RK updates
-int Model::invert(double *xs, const char *who, bool full, cudaStream_t s, double *) {
+int Model::invert(double *xs, const char *who, bool full, cudaStream_t s, bool island) {
     double *w = plane(xs, who), *psi = plane(xs, "psi");
     const bool mixed = desc.precision != 0;
     TRY(launch_celltocorner(w, B, mv, nv, s));
+    if (island && isl) TRY(plane_sub(B, isl->rhsp, pl, s));
     if (!full) return mixed ? two_vcycle_mixed(gmg, psi, B, s) : two_vcycle(gmg, psi, B, s);
     if (mixed)
         TRY(solve_mixed(gmg, psi, B, 4, 1e-11, s));
@@ -1067,7 +1083,7 @@ int Model::stage(int k, cudaStream_t s) {
     if (kind == M_QG) {
         // dxdt[:] = 0 then dxdt[pvanom] = dxdt[pv]: the warm start is zero
         TRY(cuda_status(cudaMemsetAsync(plane(dk, "psi"), 0, pl * 8, s), "qg warm start"));
-        TRY(invert(dk, "pv", false, s));
+        TRY(invert(dk, "pv", false, s, true));
     } else {
         TRY(invert(dk, "vorticity", false, s));
     }
@@ -1098,7 +1114,7 @@ int Model::stage(int k, cudaStream_t s) {
     }
     // Euler: u, v of the RK update are overwritten by the full solve
     if (kind != M_BOUSSINESQ && k == 2) o.rk = 0;
-    return stage_ortho(o, s);
+    return ortho(o, kind == M_QG, s);
 }
 
 // One RK3_SSP stage of the mixed form (see kernels_mixed.cu)
@@ -1186,12 +1202,12 @@ int Model::set_psi(cudaStream_t s) {
     if (kind == M_QG) {
         k_qg_post<<<blocks_for(pl), 256, 0, s>>>(X, pl, pvback, 0., 0);  // pvanom = pv - pvback
         TRY(launch_status("pvanom"));
-        TRY(invert(X, "pvanom", true, s));
+        TRY(invert(X, "pvanom", true, s, true));
     } else {
-        TRY(invert(X, "vorticity", true, s));
+        TRY(invert(X, "vorticity", true, s, true));
     }
     OrthoStage o = ortho_base(*this, X);
-    return stage_ortho(o, s);
+    return ortho(o, true, s);
 }
 
 int Model::diagnostics(cudaStream_t s) {
@@ -1325,9 +1341,9 @@ int Model::add_noslip(cudaStream_t s) {
     TRY(noslip_mean(N.src, N.sum, N.mskbc, N.bcarea, pl, s));
     TRY(launch_fillhalo(N.src, NH, mv, nv, s));
     TRY(plane_sub(plane(X, who), N.src, pl, s));
-    TRY(invert(X, who, false, s));
+    TRY(invert(X, who, false, s, true));
     OrthoStage o = ortho_base(*this, X);
-    TRY(stage_ortho(o, s));
+    TRY(ortho(o, true, s));
     if (kind == M_EULER) TRY(plane_div(N.src, dt, pl, s));
     return OK;
 }
@@ -1584,6 +1600,7 @@ int f2d_model_destroy(void *model) {
     delete M->loop;
     delete M->flux;
     delete M->noslip;
+    delete M->isl;
     delete M;
     return OK;
 }
@@ -1699,6 +1716,54 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
         TRY(cuda_status(cudaGraphInstantiate(&M->gexec, g, 0), "graph instantiate"));
     }
     for (int k = 0; k < nsteps; k++) TRY(cuda_status(cudaGraphLaunch(M->gexec, s), "graph launch"));
+    return OK;
+}
+
+// ---- islands (core/island.py, core/fluid2d.py:110-113)
+int f2d_model_islands(void *model, const double *rhsp_host, const double *psi_host,
+                      void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || !rhsp_host || !psi_host) {
+        set_error("f2d_model_islands: null argument");
+        return ERR_ARG;
+    }
+    if (M->kind == M_QG && M->desc.precision != 0) {
+        set_error("f2d_model_islands: the quasigeostrophic islands run in float64 only");
+        return ERR_ARG;
+    }
+    Model::Islands *I = new (std::nothrow) Model::Islands();
+    if (!I) return ERR_CUDA;
+    size_t o1 = I->mem.add(sizeof(double) * M->pl), o2 = I->mem.add(sizeof(double) * M->pl);
+    int st = I->mem.alloc();
+    if (!st) {
+        I->rhsp = I->mem.at<double>(o1);
+        I->psi = I->mem.at<double>(o2);
+        st = cuda_status(cudaMemcpyAsync(I->rhsp, rhsp_host, sizeof(double) * M->pl,
+                                         cudaMemcpyHostToDevice, s),
+                         "islands rhsp");
+    }
+    if (!st)
+        st = cuda_status(cudaMemcpyAsync(I->psi, psi_host, sizeof(double) * M->pl,
+                                         cudaMemcpyHostToDevice, s),
+                         "islands psi");
+    if (!st) st = cuda_status(cudaStreamSynchronize(s), "islands");
+    if (st) {
+        delete I;
+        return st;
+    }
+    delete M->isl;
+    M->isl = I;
+    if (M->gexec) cudaGraphExecDestroy(M->gexec);
+    if (M->graph) cudaGraphDestroy(M->graph);
+    M->gexec = nullptr;
+    M->graph = nullptr;
+    if (M->loop) {
+        if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
+        if (M->loop->graph) cudaGraphDestroy(M->loop->graph);
+        M->loop->exec = nullptr;
+        M->loop->graph = nullptr;
+    }
     return OK;
 }
 

@@ -122,6 +122,9 @@ struct OrthoStage {
     double *psiout;
     const double *dt;
     int mv, nv;
+    // psi is already masked (and carries the islands' streamfunction,
+    // core/operators.py:482-486): read it as it is
+    int premasked;
 };
 int stage_ortho(const OrthoStage &a, cudaStream_t s);
 

@@ -14,6 +14,8 @@ int noslip_mean(double *src, const double *sum, const int8_t *mskbc, double bcar
                 cudaStream_t s);
 int plane_sub(double *x, const double *y, size_t n, cudaStream_t s);
 int plane_div(double *x, const double *dt, size_t n, cudaStream_t s);
+// psi = psi*mskp + psi_island (the islands' streamfunction)
+int psi_island(double *psi, const int8_t *mskp, const double *isl, size_t n, cudaStream_t s);
 // QG: pvanom += (dt/6)(d0 + d1) with the pv tendencies of stages 0 and 1
 // (float64 d0/d1, or float32 f0/f1 in the mixed form)
 int pvanom_rk(double *x, const double *d0, const double *d1, const float *f0, const float *f1,

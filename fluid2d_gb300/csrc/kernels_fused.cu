@@ -808,9 +808,9 @@ __global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
     const size_t p = off(j, i, nv);
     // masking is idempotent, so neighbours read before or after their own
     // thread masks them give the same value
-    const double pc = a.mskp[p] ? a.psi[p] : 0.;
+    const double pc = (a.premasked || a.mskp[p]) ? a.psi[p] : 0.;
     const double dt = (a.rk || a.psi_rk) ? *a.dt : 0.;
-    a.psi[p] = pc;
+    if (!a.premasked) a.psi[p] = pc;
     if (a.psi_rk) {
         // x += (dt/6)*(dx0 + dx1 + 4*dx2) (core/timescheme.py:180)
         const double d1 = a.psi1 ? a.psi1[p] : pc;
@@ -818,8 +818,8 @@ __global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
         a.psiout[p] = a.psibase[p] + (dt / 6.) * (a.psi0[p] + d1 + 4 * d2);
     }
     if (i < 1 || j < 1 || i > nv - 2 || j > mv - 2) return;
-    const double ps = a.mskp[p - nv] ? a.psi[p - nv] : 0.;
-    const double pw = a.mskp[p - 1] ? a.psi[p - 1] : 0.;
+    const double ps = (a.premasked || a.mskp[p - nv]) ? a.psi[p - nv] : 0.;
+    const double pw = (a.premasked || a.mskp[p - 1]) ? a.psi[p - 1] : 0.;
     const int mc = a.msk[p];
     const double u = (mc + a.msk[p + 1] == 2) ? a.zdy * (ps - pc) : 0.;
     const double v = (mc + a.msk[p + nv] == 2) ? a.zdx * (pc - pw) : 0.;

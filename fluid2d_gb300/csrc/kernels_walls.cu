@@ -86,6 +86,19 @@ int plane_div(double *x, const double *dt, size_t n, cudaStream_t s) {
     return launch_status("plane_div");
 }
 
+// psi = psi*mskp + psi_island over the whole array (core/operators.py:481-486)
+__global__ void k_psi_island(double *psi, const int8_t *mskp, const double *isl, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        psi[q] = psi[q] * (double)mskp[q] + isl[q];
+}
+
+int psi_island(double *psi, const int8_t *mskp, const double *isl, size_t n, cudaStream_t s) {
+    size_t b = (n + 255) / 256;
+    k_psi_island<<<(unsigned)(b > 4096 ? 4096 : b), 256, 0, s>>>(psi, mskp, isl, n);
+    return launch_status("psi_island");
+}
+
 // QG: the RK update of the pvanom plane that the wall source reads
 // (core/timescheme.py:180 over dxdt[pvanom] = dxdt[pv] at stages 0, 1 and 0 at
 // the forcing stage, core/quasigeostrophic.py:158-168)

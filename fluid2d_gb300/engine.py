@@ -255,6 +255,15 @@ class Model(object):
                    ctypes.byref(st))
         return nite.value, res.value, st.value
 
+    def set_islands(self, rhsp, psi):
+        """Islands with a prescribed streamfunction: the rhsp and psi arrays of
+        core/island.py (``fluid2d_gb300.island.Island.finalize``)."""
+        r = np.ascontiguousarray(rhsp, dtype=np.float64)
+        p = np.ascontiguousarray(psi, dtype=np.float64)
+        if r.shape != (self.nyl, self.nxl) or p.shape != (self.nyl, self.nxl):
+            raise ValueError("island arrays must be (ny+6, nx+6)")
+        self._call("f2d_model_islands", self.h, r.ctypes.data, p.ctypes.data, _stream())
+
     # ---- flux diagnostic: core/fluxes.py:100-213
     def flux_setup(self):
         self._call("f2d_model_flux_setup", self.h, _stream())

@@ -263,6 +263,14 @@ int f2d_model_graph_kernels(void *model, int *nkernels);
  * grid.msknoslip: the geometry's mask before islands are carved). */
 int f2d_model_noslip(void *model, const int8_t *msknoslip_host, void *stream);
 
+/* ---- islands with a prescribed streamfunction (core/island.py:21-47 gives
+ * the two arrays; core/fluid2d.py:110-113 hands them to the operators): the
+ * full inversions, the no-slip inversion and QG's stage inversions subtract
+ * rhsp from the right-hand side and add psi to the masked solution
+ * (core/operators.py:442-444, 482-486).  HOST float64 (ny+6, nx+6) arrays. */
+int f2d_model_islands(void *model, const double *rhsp_host, const double *psi_host,
+                      void *stream);
+
 /* ---- flux diagnostic: Fluxes.diag_fluxes (core/fluxes.py:100-170), the
  * reversible and irreversible parts of the advective fluxes from one RK3 step
  * forward and one backward of an extended state (state, cell-centred u and v,

@@ -437,7 +437,7 @@ class Operators(object):
         self.fill_halo(y)
         dxdt[iw][:, :] = y
 
-    def invert_vorticity(self, x, flag='full'):
+    def invert_vorticity(self, x, flag='full', island=False):
         iu = self.varname_list.index('u')
         iv = self.varname_list.index('v')
         ip = self.varname_list.index('psi')
@@ -446,6 +446,8 @@ class Operators(object):
         v = x[iv]
         psi = x[ip]
         K.celltocorner(x[iw], self.work)
+        if island:  # core/operators.py:442-444
+            self.work[:, :] -= self.rhsp
         if flag == 'fast':
             self.gmg.twoVcycle(psi, self.work, {'maxite': 1, 'tol': 1e-6})
         else:
@@ -455,6 +457,8 @@ class Operators(object):
                 psim = self.grid.domain_integration(psi) / self.area
                 psi -= psim
         psi = psi * self.mskp
+        if island:  # core/operators.py:482-486
+            psi += self.psi
         K.computeorthogradient(self.msk, psi, self.dx, self.dy, self.nh, u, v)
         x[iu] = u
         x[iv] = v
@@ -608,6 +612,14 @@ class _Model(object):
         self.tscheme = Timescheme(param.timestepping, self.state)
         self.tscheme.set(self.dynamics)
         self.diags = {}
+        # islands with a prescribed streamfunction (core/fluid2d.py:110-113):
+        # set_islands gives the Island's rhsp and psi (core/island.py:21-47)
+        self.isisland = False
+
+    def set_islands(self, rhsp, psi):
+        self.ope.rhsp = np.array(rhsp, dtype=float)
+        self.ope.psi = np.array(psi, dtype=float)
+        self.isisland = True
 
     def get(self, name):
         return self.state[self.varname_list.index(name)]
@@ -623,7 +635,7 @@ class Euler(_Model):
         if self.param.noslip:  # core/euler.py:109-113, 171-179
             source = self.get('source')
             self.ope.rhs_noslip(self.state, source)
-            self.ope.invert_vorticity(self.state, flag='fast')
+            self.ope.invert_vorticity(self.state, flag='fast', island=self.isisland)
             source /= dt
         self.set_psi_from_vorticity()
 
@@ -637,7 +649,7 @@ class Euler(_Model):
             self.ope.invert_vorticity(dxdt, flag='fast')
 
     def set_psi_from_vorticity(self):
-        self.ope.invert_vorticity(self.state)
+        self.ope.invert_vorticity(self.state, island=self.isisland)
 
     def diagnostics(self, t=0.):
         u, v = self.get('u'), self.get('v')
@@ -674,7 +686,7 @@ class Boussinesq(_Model):
         self.tscheme.forward(self.state, t, dt)
         if self.param.noslip:  # core/boussinesq.py:93-94, 116-118
             self.ope.rhs_noslip(self.state, self.source)
-            self.ope.invert_vorticity(self.state, flag='fast')
+            self.ope.invert_vorticity(self.state, flag='fast', island=self.isisland)
         banom = self.get('banom')
         banom[:, :] = self.get('buoyancy') - self.bref
 
@@ -688,7 +700,7 @@ class Boussinesq(_Model):
         self.ope.invert_vorticity(dxdt, flag='fast')
 
     def set_psi_from_vorticity(self):
-        self.ope.invert_vorticity(self.state)
+        self.ope.invert_vorticity(self.state, island=self.isisland)
 
     def diagnostics(self, t=0.):
         nh = self.nh
@@ -733,7 +745,7 @@ class QG(_Model):
         self.tscheme.forward(self.state, t, dt)
         if self.param.noslip:  # core/quasigeostrophic.py:112-114, 171-175
             self.ope.rhs_noslip(self.state, self.source)
-            self.ope.invert_vorticity(self.state, flag='fast')
+            self.ope.invert_vorticity(self.state, flag='fast', island=self.isisland)
         self.set_psi_from_pv()
         self.state[self.ipva] = self.state[self.ipv] - self.pvback
         self.state[self.ivor] = (self.state[self.ipva]
@@ -747,12 +759,12 @@ class QG(_Model):
                 self.ope.rhs_diffusion(x, t, dxdt)
         else:
             dxdt[self.ipva] = dxdt[self.ipv]
-            self.ope.invert_vorticity(dxdt, flag='fast')
+            self.ope.invert_vorticity(dxdt, flag='fast', island=self.isisland)
 
     def set_psi_from_pv(self):
         state = self.state
         state[self.ipva] = state[self.ipv] - self.pvback
-        self.ope.invert_vorticity(self.state, flag='full')
+        self.ope.invert_vorticity(self.state, flag='full', island=self.isisland)
 
     def diagnostics(self, t=0.):
         u, v = self.get('u'), self.get('v')
@@ -979,8 +991,12 @@ def from_workload(wl, **kw):
               geometry=wl["geometry"], gravity=wl.get("gravity", 1.), **kw)
     g = Grid(p)
     g.msk = wl["msk"].copy()
+    if "msknoslip" in wl:  # an experiment's own no-slip walls
+        g.msknoslip = wl["msknoslip"].copy()
     g.finalize_msk()
     M = MODELS[wl["model"]](p, grid=g)
+    if "island_arrays" in wl:  # rhsp, psi of core/island.py
+        M.set_islands(*wl["island_arrays"])
     for name, f in wl["fields"].items():
         M.get(name)[:] = f
     if wl["model"] == "quasigeostrophic":

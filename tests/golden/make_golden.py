@@ -31,6 +31,35 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_CORE = "/root/reference/core"
 
 
+def channel_with_islands(model="euler", nx=64, ny=32, seed=9):
+    """A channel with a disc obstacle held at psi = 0 and the walls held at
+    +-0.1: a through-flow, as experiments/VonKarman/karman_street.py sets it
+    up (islands, no-slip on the disc, free slip on the walls)."""
+    Lx, Ly, nh = 2., 1., 3
+    msk = W.base_mask(nx, ny, "xchannel")
+    xr, yr = W.cell_coords(nx, ny, Lx, Ly)
+    disc = np.where(np.sqrt((xr - 0.5) ** 2 + (yr - 0.5) ** 2) <= 0.12)
+    msk[disc] = 0
+    noslip = W.base_mask(nx, ny, "xchannel")
+    noslip[disc] = 0
+    noslip[:nh, :] = 1
+    noslip[-nh:, :] = 1
+    m = np.zeros_like(msk)
+    m[:nh, :] = 1
+    bottom = np.where(m == 1)
+    m = np.zeros_like(msk)
+    m[-nh:-1, :] = 1
+    top = np.where(m == 1)
+    w = 1e-2 * np.random.default_rng(seed).standard_normal(msk.shape)
+    w[:, :nh] = w[:, -2 * nh:-nh]  # periodic in x
+    w[:, -nh:] = w[:, nh:2 * nh]
+    w = w * msk
+    name = "pv" if model == "quasigeostrophic" else "vorticity"
+    return {"model": model, "geometry": "xchannel", "nx": nx, "ny": ny, "Lx": Lx, "Ly": Ly,
+            "msk": msk, "msknoslip": noslip, "fields": {name: w},
+            "islands": [(disc, 0.), (bottom, 0.1), (top, -0.1)]}
+
+
 def cases():
     qg = W.dipole(32, 32, seed=11)
     qg["model"] = "quasigeostrophic"
@@ -71,18 +100,25 @@ def cases():
                                          {"order": 3, "flux_splitting_method": "minmax"}),
         "boussinesq_xchannel_64x16_order2": (W.shear(64, 16, seed=8, delta=0.1),
                                              {"order": 2}),
+        # islands with a prescribed streamfunction (core/island.py)
+        "euler_xchannel_64x32_islands_noslip": (channel_with_islands(), {"noslip": True}),
+        "qg_xchannel_64x32_islands": (channel_with_islands("quasigeostrophic"),
+                                      {"Rd": 0.5, "beta": 1.0}),
     }
 
 
 def reference_model(core, wl, kw, with_param=False):
     over = dict(modelname=wl["model"], nx=wl["nx"], ny=wl["ny"], Lx=wl["Lx"], Ly=wl["Ly"],
-                geometry=wl["geometry"], gravity=wl.get("gravity", 1.), adaptable_dt=False)
+                geometry=wl["geometry"], gravity=wl.get("gravity", 1.), adaptable_dt=False,
+                isisland=bool(wl.get("islands")))
     over.update(kw)
     p = refshim.reference_param(core, **over)
     import grid as rgrid
     with contextlib.redirect_stdout(io.StringIO()):
         g = rgrid.Grid(p)
         g.msk[:] = wl["msk"]
+        if "msknoslip" in wl:
+            g.msknoslip[:] = wl["msknoslip"]
         g.finalize_msk()
         if wl["model"] == "euler":
             import euler
@@ -93,6 +129,12 @@ def reference_model(core, wl, kw, with_param=False):
         else:
             import quasigeostrophic
             M = quasigeostrophic.QG(p, g)
+        if wl.get("islands"):  # core/fluid2d.py:110-113
+            for idx, psi0 in wl["islands"]:
+                g.island.add(idx, psi0)
+            g.island.finalize(M.ope.mskp)
+            M.ope.rhsp = g.island.rhsp
+            M.ope.psi = g.island.psi
         for name, f in wl["fields"].items():
             M.var.get(name)[:] = f
         if wl["model"] == "quasigeostrophic":
@@ -247,8 +289,21 @@ def main_loop(core):
 
 
 def main(core, steps=4):
+    from fluid2d_gb300.island import Island
     for name, (wl, kw) in cases().items():
         R = reference_model(core, wl, kw)
+        extra = {}
+        if wl.get("islands"):
+            # the product's host restatement of core/island.py gives the same arrays
+            I = Island(wl["nx"] + 6, wl["ny"] + 6, wl["Lx"] / wl["nx"], wl["Ly"] / wl["ny"])
+            for idx, psi0 in wl["islands"]:
+                I.add(idx, psi0)
+            rhsp, psi = I.finalize()
+            assert np.array_equal(rhsp, R.ope.rhsp) and np.array_equal(psi, R.ope.psi), name
+            wl = dict(wl, island_arrays=(rhsp, psi))
+            extra = dict(rhsp=rhsp, psi_island=psi)
+        if "msknoslip" in wl:
+            extra["msknoslip"] = wl["msknoslip"]
         p, O = stepper.from_workload(wl, **kw)
         assert np.array_equal(R.var.state, O.state), name
         dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
@@ -266,7 +321,7 @@ def main(core, steps=4):
                 assert float(np.asarray(R.diags[key]).ravel()[0]) == O.diags[key], (name, k, key)
             states.append(O.state.copy())
             diags.append([O.diags[key] for key in sorted(O.diags)])
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), msk=wl["msk"],
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), msk=wl["msk"], **extra,
                             states=np.array(states), diags=np.array(diags),
                             diag_names=np.array(sorted(O.diags)), dt=dt,
                             varnames=np.array(O.varname_list),

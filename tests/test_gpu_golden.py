@@ -7,7 +7,8 @@ Exact build: bit-identical for the closed and channel geometries (the only
 reductions feeding the state are maxima); the periodic case differs by the
 rounding of the psi mean and the no-slip cases by that of the mean wall
 source.  Otherwise: 1e-10 of the largest value.  Covers diffusion at the
-forcing stage and no-slip walls for Euler, Boussinesq and QG.
+forcing stage, no-slip walls, islands with a prescribed streamfunction, line
+relaxation and the advection orders.
 """
 import ast
 import glob
@@ -32,9 +33,13 @@ def test_engine_replays_reference_steps(path, variant):
     prm = ast.literal_eval(str(z["params"][0]))
     kw = {k: prm[k] for k in ("Rd", "beta", "diffusion", "Kdiff", "noslip",
                                       "hydroepsilon", "order", "flux_splitting_method") if k in prm}
+    if "msknoslip" in z:
+        kw["msknoslip"] = z["msknoslip"]
     G = engine.Model(prm["model"], prm["nx"], prm["ny"], prm["Lx"], prm["Ly"],
                      prm["geometry"], msk=z["msk"], gravity=prm["gravity"], dt=float(z["dt"]),
                      variant=variant, **kw)
+    if "rhsp" in z:
+        G.set_islands(z["rhsp"], z["psi_island"])
     states = z["states"]
     G.var.state.copy_(torch.from_numpy(states[0]).cuda())
     G.diagnostics()

@@ -243,3 +243,18 @@ def test_writers_match_reference_layout(tmp_path):
         assert np.array_equal(v.a, rvar[k][2])
     for k, v in RR["attrs"].items():
         assert ratt[k] == v, k
+
+
+def test_island_arrays_match_reference_fixture():
+    """fluid2d_gb300.island (host restatement of core/island.py) gives the
+    rhsp and psi arrays the reference's Island computed for the fixture."""
+    from fluid2d_gb300.island import Island
+    mg = make_golden()
+    z = np.load(os.path.join(HERE, "golden", "euler_xchannel_64x32_islands_noslip.npz"))
+    wl = mg.channel_with_islands()
+    I = Island(wl["nx"] + 6, wl["ny"] + 6, wl["Lx"] / wl["nx"], wl["Ly"] / wl["ny"])
+    for idx, psi0 in wl["islands"]:
+        I.add(idx, psi0)
+    rhsp, psi = I.finalize()
+    assert np.array_equal(rhsp, z["rhsp"]) and np.array_equal(psi, z["psi_island"])
+    assert np.array_equal(wl["msknoslip"], z["msknoslip"])

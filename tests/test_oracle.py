@@ -43,8 +43,12 @@ def golden_model(path):
                       Ly=prm["Ly"], geometry=prm["geometry"], gravity=prm["gravity"], **kw)
     g = stepper.Grid(p)
     g.msk = z["msk"].copy()
+    if "msknoslip" in z:
+        g.msknoslip = z["msknoslip"].copy()
     g.finalize_msk()
     M = stepper.MODELS[prm["model"]](p, grid=g)
+    if "rhsp" in z:
+        M.set_islands(z["rhsp"], z["psi_island"])
     M.state[:] = z["states"][0]
     M.diagnostics()
     return z, p, M

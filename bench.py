@@ -147,6 +147,9 @@ def _cpu_worker(args):
     return steps, time.perf_counter() - t0
 
 
+SMOOTH_DRAM_BYTES_PER_POINT = (17996800 + 0 + 17964288 + 0) / 1060900.
+
+
 def cpu_baseline(n, budget, cores):
     """Cell-steps/s of the oracle path on `cores` host processes."""
     from oracle import oracle
@@ -271,14 +274,10 @@ def run_ours(a, rank, world, local):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg_bytes / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = _json.load(open(tf)).get("smooth_fp64_bytes_per_point")
-            traffic = traffic * pts if traffic else None
-        except (OSError, ValueError):
-            traffic = None
+    # dram__bytes_read.sum + dram__bytes_write.sum of one smoothtwicewitha call
+    # (k_sweep1 + k_sweep2) per grid point, from the ncu capture summarised in
+    # profiles/k_sweep_turbulence_1024_fp64_dram.md (1024^2, 1060900 points)
+    traffic = SMOOTH_DRAM_BYTES_PER_POINT * pts
 
     # ---- e2e through the public API with host buffers: every step uploads
     # the state (Var.state) from pinned memory, steps, reads it back

@@ -209,6 +209,12 @@ def run_ours(a, rank, world, local):
     dt = 0.8 * min(M.dx, M.dy) / d0["maxspeed"]
     M.set_dt(dt)
     s0 = M.var.state.clone()
+    # the coarse-CTA switch level that times fastest on this grid (the
+    # state it advanced is put back; results do not depend on the choice)
+    from fluid2d_gb300.autotune import tune_coarse_level
+    tune_coarse_level(M, steps=3, warmup=1)
+    M.var.state.copy_(s0)
+    M.diagnostics()
     stream = torch.cuda.Stream()
     # warm-up: capture the step graph and run W steps
     with torch.cuda.stream(stream):
@@ -364,6 +370,10 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
     Mm = engine.from_workload(wl, dt=dt, precision="mixed")
     Mm.var.state.copy_(s0)
     Mm.diagnostics()
+    from fluid2d_gb300.autotune import tune_coarse_level
+    tune_coarse_level(Mm, steps=3, warmup=1)
+    Mm.var.state.copy_(s0)
+    Mm.diagnostics()
     with torch.cuda.stream(stream):
         Mm.run(a.warmup, graph=True)
     stream.synchronize()
@@ -400,16 +410,21 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
 
 def bench_ensemble(a):
     """Config: 96 independent Euler instances (sides log-uniform 64-768,
-    multiples of 64, islands, 3-12 vortices; seed 4).  Batched = every
-    instance's step graph replayed on 32 streams; comparator = the plain
-    float64 path, one instance at a time."""
+    multiples of 64, islands, 3-12 vortices; seed 4).  Batched = the launch
+    structure the autotuner picks (fluid2d_gb300.autotune.tune_ensemble):
+    groups of instances whose steps are merged into one launch per kernel,
+    one graph per group on its own stream, or every instance's own step graph
+    replayed on 32 streams; comparator = the plain float64 path, one instance
+    at a time."""
     import torch
     from fluid2d_gb300 import engine, workloads as W
+    from fluid2d_gb300.autotune import tune_ensemble
     wls = W.ensemble(96, seed=4)
     cells = sum(w["nx"] * w["ny"] for w in wls)
     out = {"instances": len(wls), "cells": cells, "steps": a.ensemble_steps}
     for prec in ("mixed", "fp64"):
         E = engine.ensemble_from_workloads(wls, precision=prec, nstreams=32)
+        choice, times = tune_ensemble(E, steps=3, warmup=1)
         E.run(2)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -419,7 +434,13 @@ def bench_ensemble(a):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         out[prec + "_batched"] = {"cell_steps_per_s": cells * a.ensemble_steps / (ms * 1e-3),
-                                  "ms_per_ensemble_step": ms / a.ensemble_steps}
+                                  "ms_per_ensemble_step": ms / a.ensemble_steps,
+                                  "launch_structure": ("streams" if choice[0] == 0 else
+                                                       "batched groups=%d policy=%d" % choice),
+                                  "tuning_ms_per_step": {("streams" if k[0] == 0 else
+                                                          "groups=%d policy=%d" % k): round(v, 3)
+                                                         for k, v in times.items()}}
+        E.free_batch()
         del E
         torch.cuda.synchronize()
     # one at a time, plain float64

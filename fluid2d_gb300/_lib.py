@@ -22,10 +22,10 @@ BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
            "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu", "timeloop.cu", "fluxdiag.cu",
-           "kernels_walls.cu"]
+           "kernels_walls.cu", "batch.cu"]
 HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh",
            "f2d_loop.cuh", "f2d_flux.cuh", "f2d_walls.cuh",
-           "f2d_tri.cuh"]
+           "f2d_tri.cuh", "f2d_batch.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-fvisibility=hidden"]
@@ -212,6 +212,11 @@ SIGNATURES.update({
     "f2d_model_probe": [_P, _I, _PI, _PDd],
     "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],
+    "f2d_model_coarse_level": [_P, _I, _PI, _PI, _PI],
+    "f2d_batch_create": [ctypes.POINTER(ctypes.c_void_p), _I, _I, _PP],
+    "f2d_batch_step": [_P, _I, _P],
+    "f2d_batch_info": [_P, _PI, _PI],
+    "f2d_batch_destroy": [_P],
     "f2d_model_noslip": [_P, _P, _P],
     "f2d_model_islands": [_P, _P, _P, _P],
     "f2d_model_flux_setup": [_P, _P],

@@ -1,0 +1,73 @@
+"""Autotuning of the launch structure by timing it on the device.
+
+* ``tune_coarse_level(model)``: the level from which the multigrid runs in
+  one CTA out of shared memory.  A finer switch level moves more work onto
+  one SM (FP64-bound there), a coarser one adds small latency-bound
+  launches; the best split depends on the grid and the precision, so every
+  allowed level is timed on the model's captured step.  Results do not
+  depend on the choice (same arithmetic either way).
+* ``tune_ensemble(ens)``: the number of batched groups and the merge policy
+  of an Ensemble's batched launches, against the per-instance stream
+  replay.
+
+Timings use CUDA events on the launching stream after warm-up steps; the
+model's state advances while it is tuned, so tune on a copy when the
+trajectory matters.  Choices are cached per (kind, grid, precision) for the
+process.
+"""
+import torch
+
+_cache = {}
+
+
+def _time(run, steps, warmup):
+    s = torch.cuda.current_stream()
+    run(warmup)
+    s.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    run(steps)
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def tune_coarse_level(model, steps=5, warmup=2, use_cache=True):
+    """Time the captured step for every allowed coarse level, keep the
+    fastest; returns (best level, {level: ms per step})."""
+    key = (model.modelname, model.desc.nx, model.desc.ny, model.desc.precision)
+    if use_cache and key in _cache:
+        model.coarse_switch(_cache[key][0])
+        return _cache[key]
+    cur, first, nlev = model.coarse_switch()
+    times = {}
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for level in range(first, nlev + 1):
+            model.coarse_switch(level)
+            times[level] = _time(lambda n: model.run(n, graph=True), steps, warmup)
+    torch.cuda.current_stream().wait_stream(side)
+    best = min(times, key=times.get)
+    model.coarse_switch(best)
+    _cache[key] = (best, times)
+    return best, times
+
+
+def tune_ensemble(ens, candidates=((1, 1), (2, 1), (4, 1), (8, 1), (16, 1), (16, 0)), steps=5,
+                  warmup=2):
+    """Pick the batched grouping and merge policy (or the stream replay,
+    (0, None)) with the shortest ensemble step; returns (choice, {choice: ms})."""
+    times = {}
+    ens.free_batch()
+    ens.capture()
+    times[(0, None)] = _time(ens.run, steps, warmup)
+    for groups, policy in candidates:
+        ens.build_batch(groups, policy)
+        times[(groups, policy)] = _time(ens.run, steps, warmup)
+    best = min(times, key=times.get)
+    if best == (0, None):
+        ens.free_batch()
+    else:
+        ens.build_batch(*best)
+    return best, times

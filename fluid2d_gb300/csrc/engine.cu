@@ -24,9 +24,15 @@
 #include "f2d_loop.cuh"
 #include "f2d_flux.cuh"
 #include "f2d_walls.cuh"
+#include "f2d_batch.cuh"
 #include <string>
 
 namespace f2d {
+
+int batch_create(int n, int (*step_fn)(void *ctx, int i), void *ctx, int policy, void **out);
+int batch_step(void *b, int nsteps, cudaStream_t s);
+int batch_info(void *b, int *launches, int *ops);
+void batch_destroy(void *b);
 
 #define TRY(x)                      \
     do {                            \
@@ -124,8 +130,18 @@ struct SolveState {
 };
 
 // after the first residual: normb, res0, active (core/gmg/hierarchy.py:158-169)
-__global__ void k_solve_init(SolveState *st, const double *sumb, const double *sumr, int maxite,
-                             double tol) {
+struct SolveInitArgs {
+    SolveState *st;
+    const double *sumb, *sumr;
+    int maxite;
+    double tol;
+};
+
+F2D_DEV void solve_init_body(const SolveInitArgs &a, const VB) {
+    SolveState *st = a.st;
+    const double *sumb = a.sumb, *sumr = a.sumr;
+    const int maxite = a.maxite;
+    const double tol = a.tol;
     double normb = sqrt(sumb[0] / 1.0);
     st->normb = normb;
     st->nite = 0;
@@ -144,8 +160,30 @@ __global__ void k_solve_init(SolveState *st, const double *sumb, const double *s
     }
 }
 
+__global__ void k_solve_init(SolveInitArgs a) { solve_init_body(a, F2D_VB_NATIVE); }
+
+struct BSolveInit {
+    using Args = SolveInitArgs;
+    static constexpr int THREADS = 1, KIND = BK_SolveInit;
+    F2D_DEV static void run(const Args &a, VB vb) { solve_init_body(a, vb); }
+};
+F2D_BATCH_ENTRY(SolveInit, BSolveInit)
+
+static int solve_init(SolveState *st, const double *sumb, const double *sumr, int maxite,
+                      double tol, cudaStream_t s) {
+    return launch_body<BSolveInit>(k_solve_init, SolveInitArgs{st, sumb, sumr, maxite, tol},
+                                   dim3(1), dim3(1), 0, s, "solve init");
+}
+
 // after each F-cycle's residual (core/gmg/hierarchy.py:172-188)
-__global__ void k_solve_update(SolveState *st, const double *sumr) {
+struct SolveUpdateArgs {
+    SolveState *st;
+    const double *sumr;
+};
+
+F2D_DEV void solve_update_body(const SolveUpdateArgs &a, const VB) {
+    SolveState *st = a.st;
+    const double *sumr = a.sumr;
     if (!st->active) return;
     double res = sqrt(sumr[0] / 1.0) / st->normb;
     double conv = st->res0 / res;
@@ -159,6 +197,20 @@ __global__ void k_solve_update(SolveState *st, const double *sumr) {
         return;
     }
     st->active = (st->nite < st->maxite) && (st->res0 > st->tol);
+}
+
+__global__ void k_solve_update(SolveUpdateArgs a) { solve_update_body(a, F2D_VB_NATIVE); }
+
+struct BSolveUpdate {
+    using Args = SolveUpdateArgs;
+    static constexpr int THREADS = 1, KIND = BK_SolveUpdate;
+    F2D_DEV static void run(const Args &a, VB vb) { solve_update_body(a, vb); }
+};
+F2D_BATCH_ENTRY(SolveUpdate, BSolveUpdate)
+
+static int solve_update(SolveState *st, const double *sumr, cudaStream_t s) {
+    return launch_body<BSolveUpdate>(k_solve_update, SolveUpdateArgs{st, sumr}, dim3(1), dim3(1),
+                                     0, s, "solve update");
 }
 
 // ------------------------------------------------------------ Gmg
@@ -194,7 +246,8 @@ struct Gmg {
     AnalyticT<float> anf{};
     template <typename T>
     const AnalyticT<T> *analytic() const;
-    int cs = 1;  // first level of the coarse CTA (== nlev: none)
+    int cs = 1;      // first level of the coarse CTA (== nlev: none)
+    int cs_min = 1;  // the finest level whose suffix fits the CTA's shared memory
     size_t smem64 = 0, smem32 = 0;
     Arena mem;
     LevelView<double> d[MAX_LEVELS];
@@ -281,6 +334,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
         if (coarse_smem_bytes<double>(mv + l, nv + l, nlev - l) <= 200 * 1024) cs = l;
         else break;
     }
+    cs_min = cs;
     if (cs < nlev) {
         smem64 = coarse_smem_bytes<double>(mv + cs, nv + cs, nlev - cs);
         smem32 = coarse_smem_bytes<float>(mv + cs, nv + cs, nlev - cs);
@@ -315,6 +369,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
     size_t o_solve = mem.add(sizeof(SolveState));
     size_t o_sc9 = mem.add(16 * sizeof(double));
     size_t o_ones = mem.add(maxpl);
+    size_t o_nb = mem.add(sizeof(uint16_t) * (size_t)mv[0] * nv[0]);
     size_t o_gam[MAX_LEVELS] = {}, o_bet[MAX_LEVELS] = {};
     if (tri)
         for (int l = 0; l < nlev; l++) {
@@ -335,6 +390,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
         d[l].b = mem.at<double>(o_b[l]);
         d[l].r = mem.at<double>(o_r[l]);
         d[l].t = mem.at<double>(o_t[l]);
+        d[l].nb = f[l].nb = nullptr;
         if (f32) {
             f[l].x = mem.at<float>(o_xf[l]);
             f[l].b = mem.at<float>(o_bf[l]);
@@ -348,6 +404,11 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
     size_t pl0 = (size_t)mv[0] * nv[0];
     TRY(cuda_status(cudaMemcpyAsync((void *)d[0].msk, mskp_host, pl0, cudaMemcpyHostToDevice, s),
                     "mask upload"));
+    {  // the analytic operator's coefficient bits, read by every level-0 kernel
+        uint16_t *nb = mem.at<uint16_t>(o_nb);
+        TRY(mg_nbmask(d[0], nb, s));
+        d[0].nb = f[0].nb = nb;
+    }
     double bx = dy / dx * hydroeps, by = dx / dy;
     double a = -2 * (bx + by), b = 0., c = 0.;
     double st[9] = {c, by, c, bx, a, bx, c, by, c};
@@ -555,8 +616,7 @@ static int solve(Gmg &g, double *x, const double *b, int maxite, double tol, cud
     TRY(mg_residual<double>(L0, &g.an, x, b, L0.b, nullptr, s));
     TRY(launch_reduce(8, L0.msk, b, nullptr, NH, L0.mv, L0.nv, g.sums + 0, g.work, s));
     TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
-    k_solve_init<<<1, 1, 0, s>>>(g.solve_state, g.sums + 0, g.sums + 1, maxite, tol);
-    TRY(launch_status("solve init"));
+    TRY(solve_init(g.solve_state, g.sums + 0, g.sums + 1, maxite, tol, s));
     const int *active = &g.solve_state->active;
     const size_t pl = (size_t)L0.mv * L0.nv;
     for (int it = 0; it < maxite; it++) {
@@ -564,8 +624,7 @@ static int solve(Gmg &g, double *x, const double *b, int maxite, double tol, cud
         TRY(vec_add(x, L0.x, pl, active, s));
         TRY(mg_residual<double>(L0, &g.an, x, b, L0.b, active, s));
         TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
-        k_solve_update<<<1, 1, 0, s>>>(g.solve_state, g.sums + 1);
-        TRY(launch_status("solve update"));
+        TRY(solve_update(g.solve_state, g.sums + 1, s));
     }
     return OK;
 }
@@ -598,16 +657,14 @@ static int solve_mixed(Gmg &g, double *x, const double *b, int maxite, double to
     TRY(mg_residual_mixed(L0, g.an, x, b, L0.b, Lf[0].b, nullptr, s));
     TRY(launch_reduce(8, L0.msk, b, nullptr, NH, L0.mv, L0.nv, g.sums + 0, g.work, s));
     TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
-    k_solve_init<<<1, 1, 0, s>>>(g.solve_state, g.sums + 0, g.sums + 1, maxite, tol);
-    TRY(launch_status("solve init"));
+    TRY(solve_init(g.solve_state, g.sums + 0, g.sums + 1, maxite, tol, s));
     const int *active = &g.solve_state->active;
     for (int it = 0; it < maxite; it++) {
         TRY(g.fcycle(Lf, 0, active, s));
         TRY(vec_add_f32(x, Lf[0].x, pl, active, s));
         TRY(mg_residual_mixed(L0, g.an, x, b, L0.b, Lf[0].b, active, s));
         TRY(launch_reduce(8, L0.msk, L0.b, nullptr, NH, L0.mv, L0.nv, g.sums + 1, g.work, s));
-        k_solve_update<<<1, 1, 0, s>>>(g.solve_state, g.sums + 1);
-        TRY(launch_status("solve update"));
+        TRY(solve_update(g.solve_state, g.sums + 1, s));
     }
     return OK;
 }
@@ -634,21 +691,30 @@ struct DiagArgs {
     double gravity, Rd, area;
     double *part;      // partials
     double *out;       // NDIAG values
+    int nr;            // partial kernel: rows per block; final kernel: partial blocks
 };
 
 // diagnostics of core/euler.py:185-223, core/boussinesq.py:123-153,
 // core/quasigeostrophic.py:189-218 in one pass (8 accumulators)
-__global__ void __launch_bounds__(RED_THREADS) k_diag_partial(DiagArgs a, int rpb) {
+F2D_DEV void diag_partial_body(const DiagArgs &a, const VB blk) {
     __shared__ double sh[8 * RED_THREADS];
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int rpb = a.nr;
     const int rows = a.mv - 2 * NH, cols = a.nv - 2 * NH;
-    const int r0 = blockIdx.x * rpb, r1 = min(rows, r0 + rpb);
-    const long long cells = (long long)(r1 - r0) * cols;
+    const int r0 = blk.x * rpb, r1 = min(rows, r0 + rpb);
+    const int cells = (r1 - r0) * cols;
     const double *s = a.s;
     const size_t pl = a.pl;
     const int nv = a.nv;
-    for (long long q = threadIdx.x; q < cells; q += RED_THREADS) {
-        const int j = NH + r0 + (int)(q / cols), i = NH + (int)(q % cols);
+    // thread t takes cells t, t + RED_THREADS, ... in row-major order
+    int jr = (int)threadIdx.x / cols, ic = (int)threadIdx.x - jr * cols;
+    for (int q = threadIdx.x; q < cells; q += RED_THREADS) {
+        const int j = NH + r0 + jr, i = NH + ic;
+        ic += RED_THREADS;
+        while (ic >= cols) {
+            ic -= cols;
+            jr++;
+        }
         const size_t p = off(j, i, nv);
         const int mc = a.msk[p];
         const double *u = s + 2 * pl, *v = s + 3 * pl;
@@ -701,10 +767,15 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag_partial(DiagArgs a, int rp
     for (int k = 0; k < 8; k++) v8[k] = acc[k];
     block_reduce<8>(v8, mx, sh);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 8; k++) a.part[k * RED_MAX_BLOCKS + blockIdx.x] = v8[k];
+        for (int k = 0; k < 8; k++) a.part[k * RED_MAX_BLOCKS + blk.x] = v8[k];
 }
 
-__global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a, int nb) {
+__global__ void __launch_bounds__(RED_THREADS) k_diag_partial(DiagArgs a) {
+    diag_partial_body(a, F2D_VB_NATIVE);
+}
+
+F2D_DEV void diag_final_body(const DiagArgs &a, const VB) {
+    const int nb = a.nr;
     __shared__ double sh[8 * RED_THREADS];
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = threadIdx.x; b < nb; b += RED_THREADS)
@@ -747,6 +818,23 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a, int nb) 
     }
 }
 
+__global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a) {
+    diag_final_body(a, F2D_VB_NATIVE);
+}
+
+struct BDiagP {
+    using Args = DiagArgs;
+    static constexpr int THREADS = RED_THREADS, KIND = BK_DiagP;
+    F2D_DEV static void run(const Args &a, VB vb) { diag_partial_body(a, vb); }
+};
+struct BDiagF {
+    using Args = DiagArgs;
+    static constexpr int THREADS = RED_THREADS, KIND = BK_DiagF;
+    F2D_DEV static void run(const Args &a, VB vb) { diag_final_body(a, vb); }
+};
+F2D_BATCH_ENTRY(DiagP, BDiagP)
+F2D_BATCH_ENTRY(DiagF, BDiagF)
+
 static const char *DIAGNAMES[3][8] = {
     {"maxspeed", "ke", "vorticity", "enstrophy", "px", "py", "angmom", "source"},
     {"maxspeed", "ke", "pe", "energy", "vorticity", "enstrophy", "buoyancy", "brms"},
@@ -755,8 +843,20 @@ static const char *DIAGNAMES[3][8] = {
 // set_dt (core/fluid2d.py:376-397): dt and cst[3] = maxspeed of the last
 // diagnostics, plus the flux-splitting constants that adv_upwind derives
 // from cst (core/fortran_advection.f90:46-60), computed once per step
-__global__ void k_set_dt(double *dt, double *cst, SplitConst *advc, const double *diag,
-                         int adaptable, double dt0, double cfl, double hmin, double dtmax) {
+struct SetDtArgs {
+    double *dt, *cst;
+    SplitConst *advc;
+    const double *diag;
+    int adaptable;
+    double dt0, cfl, hmin, dtmax;
+};
+
+F2D_DEV void set_dt_body(const SetDtArgs &a, const VB) {
+    double *dt = a.dt, *cst = a.cst;
+    SplitConst *advc = a.advc;
+    const double *diag = a.diag;
+    const int adaptable = a.adaptable;
+    const double dt0 = a.dt0, cfl = a.cfl, hmin = a.hmin, dtmax = a.dtmax;
     const double maxspeed = diag[0];
     double d = dt0;
     if (adaptable && maxspeed != 0) {
@@ -766,6 +866,22 @@ __global__ void k_set_dt(double *dt, double *cst, SplitConst *advc, const double
     *dt = d;
     cst[3] = maxspeed;
     *advc = split_const(cst);
+}
+
+__global__ void k_set_dt(SetDtArgs a) { set_dt_body(a, F2D_VB_NATIVE); }
+
+struct BSetDt {
+    using Args = SetDtArgs;
+    static constexpr int THREADS = 1, KIND = BK_SetDt;
+    F2D_DEV static void run(const Args &a, VB vb) { set_dt_body(a, vb); }
+};
+F2D_BATCH_ENTRY(SetDt, BSetDt)
+
+static int set_dt(double *dt, double *cst, void *advc, const double *diag, int adaptable,
+                  double dt0, double cfl, double hmin, double dtmax, cudaStream_t s) {
+    return launch_body<BSetDt>(
+        k_set_dt, SetDtArgs{dt, cst, (SplitConst *)advc, diag, adaptable, dt0, cfl, hmin, dtmax},
+        dim3(1), dim3(1), 0, s, "set_dt");
 }
 
 // QG fields after the step (core/quasigeostrophic.py:120-122, :186) and the
@@ -779,11 +895,26 @@ __global__ void k_qg_post(double *s, size_t pl, const double *pvback, double rdm
     }
 }
 
-__global__ void k_banom(double *s, size_t pl, const double *bref) {
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < pl;
-         q += (size_t)gridDim.x * blockDim.x)
-        s[5 * pl + q] = s[4 * pl + q] - bref[q];
+struct BanomArgs {
+    double *s;
+    size_t pl;
+    const double *bref;
+};
+
+F2D_DEV void banom_body(const BanomArgs &a, const VB vb) {
+    for (size_t q = vb.x * (size_t)blockDim.x + threadIdx.x; q < a.pl;
+         q += (size_t)vb.gx * blockDim.x)
+        a.s[5 * a.pl + q] = a.s[4 * a.pl + q] - a.bref[q];
 }
+
+__global__ void k_banom(BanomArgs a) { banom_body(a, F2D_VB_NATIVE); }
+
+struct BBanom {
+    using Args = BanomArgs;
+    static constexpr int THREADS = 256, KIND = BK_Banom;
+    F2D_DEV static void run(const Args &a, VB vb) { banom_body(a, vb); }
+};
+F2D_BATCH_ENTRY(Banom, BBanom)
 
 struct Model {
     f2d_model_desc desc;
@@ -1229,17 +1360,17 @@ int Model::diagnostics(cudaStream_t s) {
     int nb = reduce_blocks(rows);
     int rpb = (rows + nb - 1) / nb;
     nb = (rows + rpb - 1) / rpb;
-    k_diag_partial<<<nb, RED_THREADS, 0, s>>>(a, rpb);
-    k_diag_final<<<1, RED_THREADS, 0, s>>>(a, nb);
-    return launch_status("diagnostics");
+    a.nr = rpb;
+    TRY(launch_body<BDiagP>(k_diag_partial, a, dim3(nb), dim3(RED_THREADS), 0, s, "diagnostics"));
+    a.nr = nb;
+    return launch_body<BDiagF>(k_diag_final, a, dim3(1), dim3(RED_THREADS), 0, s, "diagnostics");
 }
 
 // Fluid2d.loop body (core/fluid2d.py:237-268): set_dt, model.step, diagnostics
 int Model::step(cudaStream_t s) {
     gmg.nprobe = 0;
-    k_set_dt<<<1, 1, 0, s>>>(dt, cst, (SplitConst *)advc, diag, desc.adaptable_dt, desc.dt,
-                             desc.cfl, dx < dy ? dx : dy, desc.dtmax);
-    TRY(launch_status("set_dt"));
+    TRY(set_dt(dt, cst, advc, diag, desc.adaptable_dt, desc.dt, desc.cfl, dx < dy ? dx : dy,
+               desc.dtmax, s));
     TRY(advance(s));
     return diagnostics(s);
 }
@@ -1255,8 +1386,8 @@ int Model::advance(cudaStream_t s) {
     }
     if (noslip) TRY(add_noslip(s));
     if (kind == M_BOUSSINESQ) {
-        k_banom<<<blocks_for(pl), 256, 0, s>>>(X, pl, bref);
-        TRY(launch_status("banom"));
+        TRY(launch_body<BBanom>(k_banom, BanomArgs{X, pl, bref}, dim3(blocks_for(pl)), dim3(256),
+                                0, s, "banom"));
     } else {
         TRY(set_psi(s));
         if (kind == M_QG) {
@@ -1719,6 +1850,76 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
     return OK;
 }
 
+// Where the hierarchy switches to the single-CTA coarse solve: any level from
+// the finest whose suffix fits the CTA's shared memory to nlev (no CTA).  The
+// arithmetic is the same either way; only the launch structure changes.
+// level < 0 only queries.
+int f2d_model_coarse_level(void *model, int level, int *current, int *first, int *nlev) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    Gmg &g = M->gmg;
+    if (level >= 0) {
+        if (g.tri || level < g.cs_min || level > g.nlev) {
+            set_error("f2d_model_coarse_level: level %d outside [%d, %d]", level, g.cs_min,
+                      g.nlev);
+            return ERR_ARG;
+        }
+        if (level != g.cs) {
+            g.cs = level;
+            if (M->gexec) cudaGraphExecDestroy(M->gexec);
+            if (M->graph) cudaGraphDestroy(M->graph);
+            M->gexec = nullptr;
+            M->graph = nullptr;
+            if (M->loop) {
+                if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
+                if (M->loop->graph) cudaGraphDestroy(M->loop->graph);
+                M->loop->exec = nullptr;
+                M->loop->graph = nullptr;
+            }
+        }
+    }
+    if (current) *current = g.cs;
+    if (first) *first = g.cs_min;
+    if (nlev) *nlev = g.nlev;
+    return OK;
+}
+
+// ---- batched steps of many models (batch.cu)
+static int batch_record_step(void *ctx, int i) { return ((Model **)ctx)[i]->step(nullptr); }
+
+int f2d_batch_create(void **models, int n, int policy, void **batch) {
+    if (!models || n < 1 || !batch || policy < 0 || policy > 1) {
+        set_error("f2d_batch_create: bad argument");
+        return ERR_ARG;
+    }
+    for (int i = 0; i < n; i++) {
+        Model *M = (Model *)models[i];
+        if (!M) return ERR_ARG;
+        if (M->kind == M_QG || M->noslip || M->isl || M->gmg.tri || M->gmg.probe) {
+            set_error("f2d_batch_create: model %d uses a feature without a batched form "
+                      "(quasigeostrophic, no-slip walls, islands, line relaxation, probe)",
+                      i);
+            return ERR_ARG;
+        }
+    }
+    return batch_create(n, batch_record_step, (void *)models, policy, batch);
+}
+
+int f2d_batch_step(void *batch, int nsteps, void *stream) {
+    if (!batch || nsteps < 0) return ERR_ARG;
+    return batch_step(batch, nsteps, (cudaStream_t)stream);
+}
+
+int f2d_batch_info(void *batch, int *launches, int *ops) {
+    if (!batch) return ERR_ARG;
+    return batch_info(batch, launches, ops);
+}
+
+int f2d_batch_destroy(void *batch) {
+    if (batch) batch_destroy(batch);
+    return OK;
+}
+
 // ---- islands (core/island.py, core/fluid2d.py:110-113)
 int f2d_model_islands(void *model, const double *rhsp_host, const double *psi_host,
                       void *stream) {
@@ -1914,10 +2115,8 @@ int f2d_model_loop_start(void *model, void *stream) {
     TRY(M->diagnostics(s));
     if (M->loop->k.fluxes) {
         // set_dt then the flux diagnostic (core/fluid2d.py:203-210)
-        k_set_dt<<<1, 1, 0, s>>>(M->dt, M->cst, (SplitConst *)M->advc, M->diag,
-                                 M->desc.adaptable_dt, M->desc.dt, M->desc.cfl,
-                                 M->dx < M->dy ? M->dx : M->dy, M->desc.dtmax);
-        TRY(launch_status("set_dt"));
+        TRY(set_dt(M->dt, M->cst, M->advc, M->diag, M->desc.adaptable_dt, M->desc.dt,
+                   M->desc.cfl, M->dx < M->dy ? M->dx : M->dy, M->desc.dtmax, s));
         TRY(M->diag_fluxes(s));
     }
     TRY(loop_record(M->loop->clock, M->loop->k, M->diag, M->loop->r, s));

@@ -1,0 +1,106 @@
+// f2d_batch.cuh -- one launch per kernel for many independent instances.
+//
+// Every engine kernel is a body `run(args, vb)` that reads its block
+// coordinates from a VB (virtual block) instead of blockIdx/gridDim.  A
+// native launch passes the real coordinates; a batched launch covers the
+// blocks of many instances in one grid: a block finds its instance in the
+// prefix sums of the instances' block counts and runs the body with that
+// instance's arguments and local coordinates.  The arithmetic is the same
+// code, so an instance evolves bit for bit as it does alone.
+//
+// Batched steps are built by recording: while a Recorder is installed on the
+// host thread, the launchers append (body kind, arguments, grid, block,
+// shared memory) to it instead of launching (batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "f2d_common.cuh"
+
+namespace f2d {
+
+struct VB {
+    int x, y, gx, gy;
+};
+#define F2D_VB_NATIVE \
+    (VB{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x, (int)gridDim.y})
+
+// the block -> instance map of a batched launch
+struct BatchGrid {
+    const int *start;  // [n + 1] first block of each instance
+    const int *gxy;    // [2n] the instance's grid (x, y)
+    int n;
+};
+
+F2D_DEV int batch_instance(const BatchGrid &g, int b) {
+    int lo = 0, hi = g.n - 1;  // the last i with start[i] <= b
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g.start[mid] <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template <class Body>
+__global__ void __launch_bounds__(Body::THREADS)
+    k_batch(const typename Body::Args *args, BatchGrid g) {
+    const int i = batch_instance(g, (int)blockIdx.x);
+    const int lb = (int)blockIdx.x - g.start[i];
+    const int gx = g.gxy[2 * i];
+    Body::run(args[i], VB{lb % gx, lb / gx, gx, g.gxy[2 * i + 1]});
+}
+
+// body kinds (the registry in batch.cu maps each to its batched launcher)
+#define F2D_BODY_KINDS(X)                                                                      \
+    X(SetDt) X(SplitF32) X(ToF32) X(AdvMixed) X(C2CF32) X(ResidualMixed) X(AddF32)           \
+    X(OrthoMixed) X(Banom) X(CellToCorner) X(Reduce8P) X(Reduce8F) X(Reduce2P) X(Reduce2F)  \
+    X(SolveInit) X(SolveUpdate) X(DiagP) X(DiagF) X(StageAdv64) X(StageOrtho) X(VecAdd)     \
+    X(SubMean) X(Sweep1D1) X(Sweep2D1) X(ResidualD1) X(RestrictD) X(RestrictF) X(InterpD)   \
+    X(SmoothFusedD0) X(SmoothFusedF0) X(SmoothFusedF1) X(ResresD0) X(ResresF0) X(ResresF1) \
+    X(CoarseD) X(CoarseF)
+
+enum BodyKind {
+#define F2D_KIND_ENUM(n) BK_##n,
+    F2D_BODY_KINDS(F2D_KIND_ENUM)
+#undef F2D_KIND_ENUM
+        BK_COUNT
+};
+
+using BatchLaunchFn = int (*)(const void *args, const BatchGrid &g, unsigned blocks, dim3 block,
+                              size_t smem, cudaStream_t s);
+
+#define F2D_KIND_DECL(n)                                                                   \
+    int batch_launch_##n(const void *args, const BatchGrid &g, unsigned blocks, dim3 block, \
+                         size_t smem, cudaStream_t s);
+F2D_BODY_KINDS(F2D_KIND_DECL)
+#undef F2D_KIND_DECL
+
+// defines batch_launch_<kind> for a Body (in the translation unit of its body)
+#define F2D_BATCH_ENTRY(n, Body)                                                              \
+    int batch_launch_##n(const void *args, const BatchGrid &g, unsigned blocks, dim3 block,    \
+                         size_t smem, cudaStream_t s) {                                        \
+        k_batch<Body><<<blocks, block, smem, s>>>((const typename Body::Args *)args, g);      \
+        return launch_status("batched " #n);                                                  \
+    }
+
+struct Recorder {
+    virtual int add(int kind, const void *args, size_t bytes, dim3 grid, dim3 block,
+                    size_t smem) = 0;
+    virtual ~Recorder() {}
+};
+// the recorder installed on this host thread (null: launch normally)
+Recorder *&recorder();
+
+// launch a body natively, or record it
+template <class Body>
+int launch_body(void (*native)(typename Body::Args), const typename Body::Args &a, dim3 grid,
+                dim3 block, size_t smem, cudaStream_t s, const char *name) {
+    if (Recorder *r = recorder()) return r->add(Body::KIND, &a, sizeof(a), grid, block, smem);
+    native<<<grid, block, smem, s>>>(a);
+    return launch_status(name);
+}
+
+}  // namespace f2d

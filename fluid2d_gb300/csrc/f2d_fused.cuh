@@ -20,6 +20,10 @@ struct LevelView {
     const int8_t *msk;
     const T *A;
     T *x, *b, *r, *t;
+    // finest level: per point, which of its 8 off-diagonal coefficients
+    // (bits 0-7, the order of offdiag) and its diagonal (bit 8) are nonzero,
+    // with the periodic-image rule of the analytic operator; else null
+    const uint16_t *nb;
 };
 
 // Analytic finest-level operator: A_k(J,I) = sc[k] where msk(J',I') and
@@ -141,6 +145,8 @@ int mg_tri_factor(const LevelView<double> &L, const Analytic *a0, double *gam, d
                   cudaStream_t s);
 int mg_tri_sweep(const LevelView<double> &L, const Analytic *a0, const double *gam,
                  const double *bet, const int *active, cudaStream_t s);
+// the finest level's coefficient bits (LevelView::nb) of every point
+int mg_nbmask(const LevelView<double> &L, uint16_t *nb, cudaStream_t s);
 // x = 0 unless *active == 0
 int mg_zero(double *x, size_t n, const int *active, cudaStream_t s);
 // x = r (assign) or x += r over the whole array, unless *active == 0

@@ -20,6 +20,7 @@
 #include "f2d_kernels.cuh"
 #include "f2d_adv.cuh"
 #include "f2d_tri.cuh"
+#include "f2d_batch.cuh"
 
 namespace f2d {
 
@@ -43,7 +44,17 @@ F2D_DEV T analytic_coef(const LevelView<T> &L, const AnalyticT<T> &an, int k, in
 // coefficient is sc[k] where its neighbour cell is fluid.
 template <typename T, bool L0>
 F2D_DEV void offdiag(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T (&a)[8]) {
-    if (L0 && j >= NH && j <= L.mv - NH - 2 && i >= NH + 1 && i <= L.nv - NH - 2) {
+    if (L0 && L.nb) {  // the precomputed coefficient bits: one load
+        const unsigned b = L.nb[off(j, i, L.nv)];
+        a[0] = (b & 1u) ? an->sc[0] : (T)0;
+        a[1] = (b & 2u) ? an->sc[1] : (T)0;
+        a[2] = (b & 4u) ? an->sc[2] : (T)0;
+        a[3] = (b & 8u) ? an->sc[3] : (T)0;
+        a[4] = (b & 16u) ? an->sc[3] : (T)0;
+        a[5] = (b & 32u) ? an->sc[2] : (T)0;
+        a[6] = (b & 64u) ? an->sc[1] : (T)0;
+        a[7] = (b & 128u) ? an->sc[0] : (T)0;
+    } else if (L0 && j >= NH && j <= L.mv - NH - 2 && i >= NH + 1 && i <= L.nv - NH - 2) {
         const int nv = L.nv;
         const int8_t *m = L.msk + off(j, i, nv);
         a[0] = m[-nv - 1] ? an->sc[0] : (T)0;
@@ -80,6 +91,7 @@ F2D_DEV void offdiag(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i
 
 template <typename T, bool L0>
 F2D_DEV T diag_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i) {
+    if (L0 && L.nb) return (L.nb[off(j, i, L.nv)] & 256u) ? an->a5 : (T)0;
     if (L0) return analytic_coef(L, *an, 4, j, i);
     return L.A[4 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
 }
@@ -87,7 +99,7 @@ F2D_DEV T diag_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i)
 template <typename T, bool L0>
 F2D_DEV T c3_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T c1) {
     if (L0) {
-        T a5 = analytic_coef(L, *an, 4, j, i);
+        const T a5 = diag_coef<T, L0>(L, an, j, i);
         return a5 != (T)0 ? an->c3 : c1 / fabs(a5);
     }
     return L.A[5 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
@@ -190,145 +202,279 @@ static inline dim3 lv_grid(int rows, int cols) {
     return grid2d(rows > 0 ? rows : 1, cols > 0 ? cols : 1, dim3(LV_TX, LV_TY));
 }
 
+template <typename T>
+struct SweepArgs {
+    LevelView<T> L;
+    AnalyticT<T> an;
+    T c1, c2;
+    int zero_x;
+    const int *active;
+};
+
 template <typename T, bool L0>
-__global__ void __launch_bounds__(LV_TX *LV_TY)
-k_sweep1(LevelView<T> L, AnalyticT<T> an, T c1, T c2, int zero_x, const int *active) {
-    if (inactive(active)) return;
-    const int i = 2 + blockIdx.x * LV_TX + threadIdx.x;
-    const int j = 2 + blockIdx.y * LV_TY + threadIdx.y;
+F2D_DEV void sweep1_body(const SweepArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<T> L = A.L;
+    const int i = 2 + vb.x * LV_TX + threadIdx.x;
+    const int j = 2 + vb.y * LV_TY + threadIdx.y;
     if (i > L.nv - 3 || j > L.mv - 3) return;
-    L.t[off(j, i, L.nv)] = jacobi<T, L0>(L, &an, zero_x ? nullptr : L.x, L.b, j, i, c1, c2);
+    L.t[off(j, i, L.nv)] = jacobi<T, L0>(L, &A.an, A.zero_x ? nullptr : L.x, L.b, j, i, A.c1, A.c2);
 }
 
 template <typename T, bool L0>
-__global__ void __launch_bounds__(LV_TX *LV_TY)
-k_sweep2(LevelView<T> L, AnalyticT<T> an, T c1, T c2, const int *active) {
-    if (inactive(active)) return;
-    const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
-    const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
+F2D_DEV void sweep2_body(const SweepArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<T> L = A.L;
+    const int i = NH + vb.x * LV_TX + threadIdx.x;
+    const int j = NH + vb.y * LV_TY + threadIdx.y;
     if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
-    T v = jacobi<T, L0>(L, &an, L.t, L.b, j, i, c1, c2);
+    T v = jacobi<T, L0>(L, &A.an, L.t, L.b, j, i, A.c1, A.c2);
     store_images(L.x, j, i, L.mv, L.nv, v);
 }
 
 template <typename T, bool L0>
-__global__ void __launch_bounds__(LV_TX *LV_TY)
-k_residual(LevelView<T> L, AnalyticT<T> an, const T *x, const T *b, T *r, const int *active) {
-    if (inactive(active)) return;
-    const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
-    const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_sweep1(SweepArgs<T> a) {
+    sweep1_body<T, L0>(a, F2D_VB_NATIVE);
+}
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_sweep2(SweepArgs<T> a) {
+    sweep2_body<T, L0>(a, F2D_VB_NATIVE);
+}
+
+template <typename T>
+struct ResidualArgs {
+    LevelView<T> L;
+    AnalyticT<T> an;
+    const T *x, *b;
+    T *r;
+    float *rf;  // the mixed form's float copy (k_residual_mixed), else unused
+    const int *active;
+};
+
+template <typename T, bool L0>
+F2D_DEV void residual_body(const ResidualArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<T> L = A.L;
+    const int i = NH + vb.x * LV_TX + threadIdx.x;
+    const int j = NH + vb.y * LV_TY + threadIdx.y;
     if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
-    store_images(r, j, i, L.mv, L.nv, residual<T, L0>(L, &an, x, b, j, i));
+    store_images(A.r, j, i, L.mv, L.nv, residual<T, L0>(L, &A.an, A.x, A.b, j, i));
+}
+
+template <typename T, bool L0>
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_residual(ResidualArgs<T> a) {
+    residual_body<T, L0>(a, F2D_VB_NATIVE);
 }
 
 // FP64 residual of the finest level with a float copy (the right-hand side
 // of the FP32 correction cycles of the mixed form)
-__global__ void __launch_bounds__(LV_TX *LV_TY)
-k_residual_mixed(LevelView<double> L, Analytic an, const double *x, const double *b, double *r,
-                 float *rf, const int *active) {
-    if (inactive(active)) return;
-    const int i = NH + blockIdx.x * LV_TX + threadIdx.x;
-    const int j = NH + blockIdx.y * LV_TY + threadIdx.y;
+F2D_DEV void residual_mixed_body(const ResidualArgs<double> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<double> L = A.L;
+    const int i = NH + vb.x * LV_TX + threadIdx.x;
+    const int j = NH + vb.y * LV_TY + threadIdx.y;
     if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
-    const double v = residual<double, true>(L, &an, x, b, j, i);
-    store_images(r, j, i, L.mv, L.nv, v);
-    store_images(rf, j, i, L.mv, L.nv, (float)v);
+    const double v = residual<double, true>(L, &A.an, A.x, A.b, j, i);
+    store_images(A.r, j, i, L.mv, L.nv, v);
+    store_images(A.rf, j, i, L.mv, L.nv, (float)v);
 }
+
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_residual_mixed(ResidualArgs<double> a) {
+    residual_mixed_body(a, F2D_VB_NATIVE);
+}
+
+struct BResidualMixed {
+    using Args = ResidualArgs<double>;
+    static constexpr int THREADS = LV_TX * LV_TY, KIND = BK_ResidualMixed;
+    F2D_DEV static void run(const Args &a, VB vb) { residual_mixed_body(a, vb); }
+};
+F2D_BATCH_ENTRY(ResidualMixed, BResidualMixed)
 
 int mg_residual_mixed(const LevelView<double> &L, const Analytic &an, const double *x,
                       const double *b, double *r, float *rf, const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
-    k_residual_mixed<<<g, bl, 0, s>>>(L, an, x, b, r, rf, active);
-    return launch_status("mg_residual_mixed");
+    return launch_body<BResidualMixed>(k_residual_mixed, ResidualArgs<double>{L, an, x, b, r, rf,
+                                                                              active},
+                                       g, bl, 0, s, "mg_residual_mixed");
 }
 
 // x (float64) += e (float32), whole array
-__global__ void k_add_f32(double *x, const float *e, size_t n, const int *active) {
-    if (inactive(active)) return;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-         q += (size_t)gridDim.x * blockDim.x)
-        x[q] = x[q] + (double)e[q];
+struct AddF32Args {
+    double *x;
+    const float *e;
+    size_t n;
+    const int *active;
+};
+
+F2D_DEV void add_f32_body(const AddF32Args &A, const VB vb) {
+    if (inactive(A.active)) return;
+    for (size_t q = vb.x * (size_t)blockDim.x + threadIdx.x; q < A.n;
+         q += (size_t)vb.gx * blockDim.x)
+        A.x[q] = A.x[q] + (double)A.e[q];
 }
+
+__global__ void k_add_f32(AddF32Args a) { add_f32_body(a, F2D_VB_NATIVE); }
+
+struct BAddF32 {
+    using Args = AddF32Args;
+    static constexpr int THREADS = 256, KIND = BK_AddF32;
+    F2D_DEV static void run(const Args &a, VB vb) { add_f32_body(a, vb); }
+};
+F2D_BATCH_ENTRY(AddF32, BAddF32)
 
 int vec_add_f32(double *x, const float *e, size_t count, const int *active, cudaStream_t s) {
     int blocks = (int)((count + 255) / 256);
     if (blocks > 4096) blocks = 4096;
-    k_add_f32<<<blocks, 256, 0, s>>>(x, e, count, active);
-    return launch_status("vec_add_f32");
+    return launch_body<BAddF32>(k_add_f32, AddF32Args{x, e, count, active}, dim3(blocks), dim3(256),
+                                0, s, "vec_add_f32");
 }
 
 template <typename T>
-__global__ void __launch_bounds__(LV_TX *LV_TY)
-k_restrict(const T *src, int nv1, const int8_t *msk2, int mv2, int nv2, T *dst,
-           const int *active) {
-    if (inactive(active)) return;
-    const int I2 = NH + blockIdx.x * LV_TX + threadIdx.x;
-    const int J2 = NH + blockIdx.y * LV_TY + threadIdx.y;
-    if (I2 > nv2 - NH - 1 || J2 > mv2 - NH - 1) return;
-    store_images(dst, J2, I2, mv2, nv2, restrict_value(msk2, nv2, src, nv1, J2, I2));
+struct RestrictArgs {
+    const T *src;
+    int nv1;
+    const int8_t *msk2;
+    int mv2, nv2;
+    T *dst;
+    const int *active;
+};
+
+template <typename T>
+F2D_DEV void restrict_body(const RestrictArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const int I2 = NH + vb.x * LV_TX + threadIdx.x;
+    const int J2 = NH + vb.y * LV_TY + threadIdx.y;
+    if (I2 > A.nv2 - NH - 1 || J2 > A.mv2 - NH - 1) return;
+    store_images(A.dst, J2, I2, A.mv2, A.nv2, restrict_value(A.msk2, A.nv2, A.src, A.nv1, J2, I2));
 }
 
 template <typename T>
-__global__ void __launch_bounds__(LV_TX *LV_TY)
-k_interp(const int8_t *msk1, int mv1, int nv1, const int8_t *msk2, const T *x2, int nv2, T *dst,
-         int assign, const int *active) {
-    if (inactive(active)) return;
-    const int I1 = 1 + blockIdx.x * LV_TX + threadIdx.x;
-    const int J1 = 1 + blockIdx.y * LV_TY + threadIdx.y;
-    if (I1 > nv1 - 2 || J1 > mv1 - 2) return;
-    const T v = interp_value(msk1, nv1, msk2, x2, nv2, J1, I1);
-    const size_t p = off(J1, I1, nv1);
-    dst[p] = assign ? v : dst[p] + v;
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_restrict(RestrictArgs<T> a) {
+    restrict_body<T>(a, F2D_VB_NATIVE);
 }
+
+template <typename T>
+struct InterpArgs {
+    const int8_t *msk1;
+    int mv1, nv1;
+    const int8_t *msk2;
+    const T *x2;
+    int nv2;
+    T *dst;
+    int assign;
+    const int *active;
+};
+
+template <typename T>
+F2D_DEV void interp_body(const InterpArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const int I1 = 1 + vb.x * LV_TX + threadIdx.x;
+    const int J1 = 1 + vb.y * LV_TY + threadIdx.y;
+    if (I1 > A.nv1 - 2 || J1 > A.mv1 - 2) return;
+    const T v = interp_value(A.msk1, A.nv1, A.msk2, A.x2, A.nv2, J1, I1);
+    const size_t p = off(J1, I1, A.nv1);
+    A.dst[p] = A.assign ? v : A.dst[p] + v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_interp(InterpArgs<T> a) {
+    interp_body<T>(a, F2D_VB_NATIVE);
+}
+
+// the bodies of the level kernels, by type and finest-level flag; KIND is the
+// batched kind of the instantiations the batched steps use, else -1
+template <typename T, bool L0>
+struct BSweep1 {
+    using Args = SweepArgs<T>;
+    static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int KIND = (sizeof(T) == 8 && L0) ? BK_Sweep1D1 : -1;
+    F2D_DEV static void run(const Args &a, VB vb) { sweep1_body<T, L0>(a, vb); }
+};
+template <typename T, bool L0>
+struct BSweep2 {
+    using Args = SweepArgs<T>;
+    static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int KIND = (sizeof(T) == 8 && L0) ? BK_Sweep2D1 : -1;
+    F2D_DEV static void run(const Args &a, VB vb) { sweep2_body<T, L0>(a, vb); }
+};
+template <typename T, bool L0>
+struct BResidual {
+    using Args = ResidualArgs<T>;
+    static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int KIND = (sizeof(T) == 8 && L0) ? BK_ResidualD1 : -1;
+    F2D_DEV static void run(const Args &a, VB vb) { residual_body<T, L0>(a, vb); }
+};
+template <typename T>
+struct BRestrict {
+    using Args = RestrictArgs<T>;
+    static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int KIND = sizeof(T) == 8 ? BK_RestrictD : BK_RestrictF;
+    F2D_DEV static void run(const Args &a, VB vb) { restrict_body<T>(a, vb); }
+};
+template <typename T>
+struct BInterp {
+    using Args = InterpArgs<T>;
+    static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int KIND = sizeof(T) == 8 ? BK_InterpD : -1;
+    F2D_DEV static void run(const Args &a, VB vb) { interp_body<T>(a, vb); }
+};
+using BSweep1D1 = BSweep1<double, true>;
+using BSweep2D1 = BSweep2<double, true>;
+using BResidualD1 = BResidual<double, true>;
+using BRestrictD = BRestrict<double>;
+using BRestrictF = BRestrict<float>;
+using BInterpD = BInterp<double>;
+F2D_BATCH_ENTRY(Sweep1D1, BSweep1D1)
+F2D_BATCH_ENTRY(Sweep2D1, BSweep2D1)
+F2D_BATCH_ENTRY(ResidualD1, BResidualD1)
+F2D_BATCH_ENTRY(RestrictD, BRestrictD)
+F2D_BATCH_ENTRY(RestrictF, BRestrictF)
+F2D_BATCH_ENTRY(InterpD, BInterpD)
 
 template <typename T>
 int mg_sweep1(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, bool zero_x,
               const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 4, L.nv - 4), b(LV_TX, LV_TY);
-    if (an)
-        k_sweep1<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, zero_x, active);
-    else
-        k_sweep1<T, false><<<g, b, 0, s>>>(L, AnalyticT<T>{}, c1, c2, zero_x, active);
-    return launch_status("mg_sweep1");
+    SweepArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, zero_x ? 1 : 0, active};
+    if (an) return launch_body<BSweep1<T, true>>(k_sweep1<T, true>, a, g, b, 0, s, "mg_sweep1");
+    return launch_body<BSweep1<T, false>>(k_sweep1<T, false>, a, g, b, 0, s, "mg_sweep1");
 }
 
 template <typename T>
 int mg_sweep2(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, const int *active,
               cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), b(LV_TX, LV_TY);
-    if (an)
-        k_sweep2<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, active);
-    else
-        k_sweep2<T, false><<<g, b, 0, s>>>(L, AnalyticT<T>{}, c1, c2, active);
-    return launch_status("mg_sweep2");
+    SweepArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, 0, active};
+    if (an) return launch_body<BSweep2<T, true>>(k_sweep2<T, true>, a, g, b, 0, s, "mg_sweep2");
+    return launch_body<BSweep2<T, false>>(k_sweep2<T, false>, a, g, b, 0, s, "mg_sweep2");
 }
 
 template <typename T>
 int mg_residual(const LevelView<T> &L, const AnalyticT<T> *an, const T *x, const T *b, T *r,
                 const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
+    ResidualArgs<T> a{L, an ? *an : AnalyticT<T>{}, x, b, r, nullptr, active};
     if (an)
-        k_residual<T, true><<<g, bl, 0, s>>>(L, *an, x, b, r, active);
-    else
-        k_residual<T, false><<<g, bl, 0, s>>>(L, AnalyticT<T>{}, x, b, r, active);
-    return launch_status("mg_residual");
+        return launch_body<BResidual<T, true>>(k_residual<T, true>, a, g, bl, 0, s, "mg_residual");
+    return launch_body<BResidual<T, false>>(k_residual<T, false>, a, g, bl, 0, s, "mg_residual");
 }
 
 template <typename T>
 int mg_restrict(const LevelView<T> &fine, const T *src, const LevelView<T> &coarse, T *dst,
                 const int *active, cudaStream_t s) {
     dim3 g = lv_grid(coarse.mv - 2 * NH, coarse.nv - 2 * NH), b(LV_TX, LV_TY);
-    k_restrict<T><<<g, b, 0, s>>>(src, fine.nv, coarse.msk, coarse.mv, coarse.nv, dst, active);
-    return launch_status("mg_restrict");
+    RestrictArgs<T> a{src, fine.nv, coarse.msk, coarse.mv, coarse.nv, dst, active};
+    return launch_body<BRestrict<T>>(k_restrict<T>, a, g, b, 0, s, "mg_restrict");
 }
 
 template <typename T>
 int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine, T *dst,
               bool assign, const int *active, cudaStream_t s) {
     dim3 g = lv_grid(fine.mv - 2, fine.nv - 2), b(LV_TX, LV_TY);
-    k_interp<T><<<g, b, 0, s>>>(fine.msk, fine.mv, fine.nv, coarse.msk, src, coarse.nv, dst,
-                                assign, active);
-    return launch_status("mg_interp");
+    InterpArgs<T> a{fine.msk, fine.mv, fine.nv, coarse.msk, src, coarse.nv, dst,
+                    assign ? 1 : 0, active};
+    return launch_body<BInterp<T>>(k_interp<T>, a, g, b, 0, s, "mg_interp");
 }
 
 // ------------------------------------------------------------ fused level kernels
@@ -349,16 +495,31 @@ struct CoarseSrc {
 };
 
 
+template <typename T>
+struct SmoothFusedArgs {
+    LevelView<T> L;
+    AnalyticT<T> an;
+    T c1, c2;
+    int xmode;
+    CoarseSrc<T> cs;
+    T *out;
+    const int *active;
+};
+
 template <typename T, bool L0>
-__global__ void __launch_bounds__(FS_TX *FS_TY)
-k_smooth_fused(LevelView<T> L, AnalyticT<T> an, T c1, T c2, int xmode, CoarseSrc<T> cs, T *out,
-               const int *active) {
-    if (inactive(active)) return;
+F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
     constexpr int XW = FS_TX + 4, XH = FS_TY + 4, TW = FS_TX + 2, TH = FS_TY + 2;
     __shared__ T xs[XH * XW];
     __shared__ T ts[TH * TW];
+    const LevelView<T> L = A.L;
+    const AnalyticT<T> an = A.an;
+    const T c1 = A.c1, c2 = A.c2;
+    const int xmode = A.xmode;
+    const CoarseSrc<T> cs = A.cs;
+    T *out = A.out;
     const int mv = L.mv, nv = L.nv;
-    const int i0 = NH + blockIdx.x * FS_TX, j0 = NH + blockIdx.y * FS_TY;
+    const int i0 = NH + vb.x * FS_TX, j0 = NH + vb.y * FS_TY;
     const int tid = threadIdx.y * FS_TX + threadIdx.x;
     // input x on [j0-2, j0+FS_TY+1] x [i0-2, i0+FS_TX+1], inside rows/cols 1..m-2
     if (xmode != X_ZERO) {
@@ -430,6 +591,26 @@ k_smooth_fused(LevelView<T> L, AnalyticT<T> an, T c1, T c2, int xmode, CoarseSrc
     store_images(out, j, i, mv, nv, v);
 }
 
+template <typename T, bool L0>
+__global__ void __launch_bounds__(FS_TX *FS_TY) k_smooth_fused(SmoothFusedArgs<T> a) {
+    smooth_fused_body<T, L0>(a, F2D_VB_NATIVE);
+}
+
+template <typename T, bool L0>
+struct BSmoothFused {
+    using Args = SmoothFusedArgs<T>;
+    static constexpr int THREADS = FS_TX * FS_TY;
+    static constexpr int KIND = sizeof(T) == 8 ? (L0 ? -1 : BK_SmoothFusedD0)
+                                               : (L0 ? BK_SmoothFusedF1 : BK_SmoothFusedF0);
+    F2D_DEV static void run(const Args &a, VB vb) { smooth_fused_body<T, L0>(a, vb); }
+};
+using BSmoothFusedD0 = BSmoothFused<double, false>;
+using BSmoothFusedF0 = BSmoothFused<float, false>;
+using BSmoothFusedF1 = BSmoothFused<float, true>;
+F2D_BATCH_ENTRY(SmoothFusedD0, BSmoothFusedD0)
+F2D_BATCH_ENTRY(SmoothFusedF0, BSmoothFusedF0)
+F2D_BATCH_ENTRY(SmoothFusedF1, BSmoothFusedF1)
+
 template <typename T>
 int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
                     const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s) {
@@ -437,11 +618,12 @@ int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, i
     dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, b);
     CoarseSrc<T> cs{nullptr, nullptr, 0};
     if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
+    SmoothFusedArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, xmode, cs, out, active};
     if (an)
-        k_smooth_fused<T, true><<<g, b, 0, s>>>(L, *an, c1, c2, xmode, cs, out, active);
-    else
-        k_smooth_fused<T, false><<<g, b, 0, s>>>(L, AnalyticT<T>{}, c1, c2, xmode, cs, out, active);
-    return launch_status("mg_smooth_fused");
+        return launch_body<BSmoothFused<T, true>>(k_smooth_fused<T, true>, a, g, b, 0, s,
+                                                  "mg_smooth_fused");
+    return launch_body<BSmoothFused<T, false>>(k_smooth_fused<T, false>, a, g, b, 0, s,
+                                               "mg_smooth_fused");
 }
 
 // residual + full-weighting restriction: the fine residuals a coarse tile
@@ -450,14 +632,27 @@ int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, i
 // memory, then restricted.
 constexpr int RR_TX = 16, RR_TY = 8;
 
+template <typename T>
+struct ResresArgs {
+    LevelView<T> F;
+    AnalyticT<T> an;
+    const int8_t *msk2;
+    int mv2, nv2;
+    T *b2;
+    const int *active;
+};
+
 template <typename T, bool L0>
-__global__ void __launch_bounds__(RR_TX *RR_TY)
-k_resres(LevelView<T> F, AnalyticT<T> an, const int8_t *msk2, int mv2, int nv2, T *b2,
-         const int *active) {
-    if (inactive(active)) return;
+F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
     constexpr int RW = 2 * RR_TX + 1, RH = 2 * RR_TY + 1;
     __shared__ T rs[RH * RW];
-    const int I2a = NH + blockIdx.x * RR_TX, J2a = NH + blockIdx.y * RR_TY;
+    const LevelView<T> F = A.F;
+    const AnalyticT<T> an = A.an;
+    const int8_t *msk2 = A.msk2;
+    const int mv2 = A.mv2, nv2 = A.nv2;
+    T *b2 = A.b2;
+    const int I2a = NH + vb.x * RR_TX, J2a = NH + vb.y * RR_TY;
     const int jf0 = 2 * J2a - 3, if0 = 2 * I2a - 3;
     const int tid = threadIdx.y * RR_TX + threadIdx.x;
     const int mv = F.mv, nv = F.nv;
@@ -479,16 +674,34 @@ k_resres(LevelView<T> F, AnalyticT<T> an, const int8_t *msk2, int mv2, int nv2, 
     store_images(b2, J2, I2, mv2, nv2, v);
 }
 
+template <typename T, bool L0>
+__global__ void __launch_bounds__(RR_TX *RR_TY) k_resres(ResresArgs<T> a) {
+    resres_body<T, L0>(a, F2D_VB_NATIVE);
+}
+
+template <typename T, bool L0>
+struct BResres {
+    using Args = ResresArgs<T>;
+    static constexpr int THREADS = RR_TX * RR_TY;
+    static constexpr int KIND = sizeof(T) == 8 ? (L0 ? -1 : BK_ResresD0)
+                                               : (L0 ? BK_ResresF1 : BK_ResresF0);
+    F2D_DEV static void run(const Args &a, VB vb) { resres_body<T, L0>(a, vb); }
+};
+using BResresD0 = BResres<double, false>;
+using BResresF0 = BResres<float, false>;
+using BResresF1 = BResres<float, true>;
+F2D_BATCH_ENTRY(ResresD0, BResresD0)
+F2D_BATCH_ENTRY(ResresF0, BResresF0)
+F2D_BATCH_ENTRY(ResresF1, BResresF1)
+
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
               const int *active, cudaStream_t s) {
     dim3 b(RR_TX, RR_TY);
     dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, b);
-    if (an)
-        k_resres<T, true><<<g, b, 0, s>>>(F, *an, C.msk, C.mv, C.nv, b2, active);
-    else
-        k_resres<T, false><<<g, b, 0, s>>>(F, AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active);
-    return launch_status("mg_resres");
+    ResresArgs<T> a{F, an ? *an : AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active};
+    if (an) return launch_body<BResres<T, true>>(k_resres<T, true>, a, g, b, 0, s, "mg_resres");
+    return launch_body<BResres<T, false>>(k_resres<T, false>, a, g, b, 0, s, "mg_resres");
 }
 
 // ------------------------------------------------------------ coarse CTA
@@ -530,6 +743,7 @@ F2D_DEV LevelView<T> co_view(unsigned char *sm, const CoLv &d) {
     L.b = (T *)(sm + d.o_b);
     L.r = (T *)(sm + d.o_r);
     L.t = (T *)(sm + d.o_t);
+    L.nb = nullptr;
     return L;
 }
 
@@ -639,7 +853,7 @@ F2D_DEV void co_vcycle(unsigned char *sm, const CoLv *lv, int l1, int deep, bool
 }
 
 template <typename T>
-__global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
+F2D_DEV void coarse_body(const CoarseArgs<T> &a, const VB) {
     if (inactive(a.active)) return;
     extern __shared__ __align__(16) unsigned char sm[];
     __shared__ CoLv lv[MAX_LEVELS];
@@ -694,6 +908,36 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
     for (int q = tid; q < pts0; q += CO_THREADS) a.lev[0].x[q] = s0.x[q];
 }
 
+template <typename T>
+__global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
+    coarse_body<T>(a, F2D_VB_NATIVE);
+}
+
+template <typename T>
+struct BCoarse {
+    using Args = CoarseArgs<T>;
+    static constexpr int THREADS = CO_THREADS;
+    static constexpr int KIND = sizeof(T) == 8 ? BK_CoarseD : BK_CoarseF;
+    F2D_DEV static void run(const Args &a, VB vb) { coarse_body<T>(a, vb); }
+};
+using BCoarseD = BCoarse<double>;
+using BCoarseF = BCoarse<float>;
+F2D_BATCH_ENTRY(CoarseD, BCoarseD)
+F2D_BATCH_ENTRY(CoarseF, BCoarseF)
+
+// the batched coarse kernels need the same opt-in shared memory
+int configure_batched_coarse() {
+    int st = cuda_status(cudaFuncSetAttribute(k_batch<BCoarseD>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              COARSE_SMEM_MAX),
+                         "batched coarse smem");
+    if (st) return st;
+    return cuda_status(cudaFuncSetAttribute(k_batch<BCoarseF>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            COARSE_SMEM_MAX),
+                       "batched coarse smem");
+}
+
 namespace {
 // per library and device: the opt-in shared-memory size of k_coarse
 bool g_coarse_configured[2][64];
@@ -713,8 +957,8 @@ int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s) {
         if (st) return st;
         if (dev >= 0 && dev < 64) g_coarse_configured[idx][dev] = true;
     }
-    k_coarse<T><<<1, dim3(CO_TX, CO_TY), smem, s>>>(args);
-    return launch_status("mg_coarse");
+    return launch_body<BCoarse<T>>(k_coarse<T>, args, dim3(1), dim3(CO_TX, CO_TY), smem, s,
+                                   "mg_coarse");
 }
 
 // ------------------------------------------------------------ stage kernels
@@ -730,13 +974,13 @@ F2D_DEV double rk_combine(int rk, double base, double d0, double d1, double dq, 
 // (double, or float in the mixed form); loads, tendency and RK combination
 // stay float64.
 template <typename TC>
-__global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
+F2D_DEV void stage_adv_body(const AdvStage &a, const VB vb) {
     __shared__ TC sfx[8][33];
     __shared__ TC sfy[9][32];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nv = a.nv, mv = a.mv;
-    const int I = NH + blockIdx.x * 32 + tx;
-    const int J = NH + blockIdx.y * 8 + ty;
+    const int I = NH + vb.x * 32 + tx;
+    const int J = NH + vb.y * 8 + ty;
     const bool in = (I <= nv - NH - 1) && (J <= mv - NH - 1);
     const SplitT<TC> c = split_cast<TC>(*(const SplitConst *)a.advc);
     if (in) {
@@ -787,22 +1031,36 @@ __global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
         }
 }
 
+template <typename TC>
+__global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
+    stage_adv_body<TC>(a, F2D_VB_NATIVE);
+}
+
+template <typename TC>
+struct BStageAdv {
+    using Args = AdvStage;
+    static constexpr int THREADS = 256;
+    static constexpr int KIND = sizeof(TC) == 8 ? BK_StageAdv64 : -1;
+    F2D_DEV static void run(const Args &a, VB vb) { stage_adv_body<TC>(a, vb); }
+};
+using BStageAdv64 = BStageAdv<double>;
+F2D_BATCH_ENTRY(StageAdv64, BStageAdv64)
+
 int stage_advection(const AdvStage &a, cudaStream_t s) {
     dim3 b(32, 8);
     dim3 g = grid2d(a.mv - 2 * NH, a.nv - 2 * NH, b);
     if (a.fp32)
-        k_stage_adv<float><<<g, b, 0, s>>>(a);
-    else
-        k_stage_adv<double><<<g, b, 0, s>>>(a);
-    return launch_status("stage_advection");
+        return launch_body<BStageAdv<float>>(k_stage_adv<float>, a, g, b, 0, s,
+                                             "stage_advection");
+    return launch_body<BStageAdv<double>>(k_stage_adv<double>, a, g, b, 0, s, "stage_advection");
 }
 
 // psi <- psi*mskp (whole array, core/operators.py:481) and
 // u,v = orthogradient(psi) (core/fortran_operators.f90:22-37), with the RK
 // combinations of u, v (rows/cols 1..m-2) and of psi fused.
-__global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
+F2D_DEV void stage_ortho_body(const OrthoStage &a, const VB vb) {
+    const int i = vb.x * 32 + threadIdx.x;
+    const int j = vb.y * 8 + threadIdx.y;
     const int nv = a.nv, mv = a.mv;
     if (i >= nv || j >= mv) return;
     const size_t p = off(j, i, nv);
@@ -831,39 +1089,82 @@ __global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
     }
 }
 
-int stage_ortho(const OrthoStage &a, cudaStream_t s) {
-    dim3 b(32, 8);
-    k_stage_ortho<<<grid2d(a.mv, a.nv, b), b, 0, s>>>(a);
-    return launch_status("stage_ortho");
+__global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
+    stage_ortho_body(a, F2D_VB_NATIVE);
 }
 
-__global__ void k_vec_add(double *x, const double *y, size_t n, const int *active) {
-    if (inactive(active)) return;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-         q += (size_t)gridDim.x * blockDim.x)
-        x[q] = x[q] + y[q];
+struct BStageOrtho {
+    using Args = OrthoStage;
+    static constexpr int THREADS = 256, KIND = BK_StageOrtho;
+    F2D_DEV static void run(const Args &a, VB vb) { stage_ortho_body(a, vb); }
+};
+F2D_BATCH_ENTRY(StageOrtho, BStageOrtho)
+
+int stage_ortho(const OrthoStage &a, cudaStream_t s) {
+    dim3 b(32, 8);
+    return launch_body<BStageOrtho>(k_stage_ortho, a, grid2d(a.mv, a.nv, b), b, 0, s,
+                                    "stage_ortho");
 }
+
+struct VecAddArgs {
+    double *x;
+    const double *y;
+    size_t n;
+    const int *active;
+};
+
+F2D_DEV void vec_add_body(const VecAddArgs &A, const VB vb) {
+    if (inactive(A.active)) return;
+    for (size_t q = vb.x * (size_t)blockDim.x + threadIdx.x; q < A.n;
+         q += (size_t)vb.gx * blockDim.x)
+        A.x[q] = A.x[q] + A.y[q];
+}
+
+__global__ void k_vec_add(VecAddArgs a) { vec_add_body(a, F2D_VB_NATIVE); }
+
+struct BVecAdd {
+    using Args = VecAddArgs;
+    static constexpr int THREADS = 256, KIND = BK_VecAdd;
+    F2D_DEV static void run(const Args &a, VB vb) { vec_add_body(a, vb); }
+};
+F2D_BATCH_ENTRY(VecAdd, BVecAdd)
 
 int vec_add(double *x, const double *y, size_t count, const int *active, cudaStream_t s) {
     int blocks = (int)((count + 255) / 256);
     if (blocks > 4096) blocks = 4096;
-    k_vec_add<<<blocks, 256, 0, s>>>(x, y, count, active);
-    return launch_status("vec_add");
+    return launch_body<BVecAdd>(k_vec_add, VecAddArgs{x, y, count, active}, dim3(blocks),
+                                dim3(256), 0, s, "vec_add");
 }
 
 // x -= dev_scalar[0] / area (core/operators.py:474-477)
-__global__ void k_sub_mean(double *x, double area, const double *sum, size_t n) {
-    const double m = *sum / area;
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-         q += (size_t)gridDim.x * blockDim.x)
-        x[q] = x[q] - m;
+struct SubMeanArgs {
+    double *x;
+    double area;
+    const double *sum;
+    size_t n;
+};
+
+F2D_DEV void sub_mean_body(const SubMeanArgs &A, const VB vb) {
+    const double m = *A.sum / A.area;
+    for (size_t q = vb.x * (size_t)blockDim.x + threadIdx.x; q < A.n;
+         q += (size_t)vb.gx * blockDim.x)
+        A.x[q] = A.x[q] - m;
 }
+
+__global__ void k_sub_mean(SubMeanArgs a) { sub_mean_body(a, F2D_VB_NATIVE); }
+
+struct BSubMean {
+    using Args = SubMeanArgs;
+    static constexpr int THREADS = 256, KIND = BK_SubMean;
+    F2D_DEV static void run(const Args &a, VB vb) { sub_mean_body(a, vb); }
+};
+F2D_BATCH_ENTRY(SubMean, BSubMean)
 
 int vec_axpy_const(double *x, double area, const double *sum, size_t count, cudaStream_t s) {
     int blocks = (int)((count + 255) / 256);
     if (blocks > 4096) blocks = 4096;
-    k_sub_mean<<<blocks, 256, 0, s>>>(x, area, sum, count);
-    return launch_status("sub_mean");
+    return launch_body<BSubMean>(k_sub_mean, SubMeanArgs{x, area, sum, count}, dim3(blocks),
+                                 dim3(256), 0, s, "sub_mean");
 }
 
 // explicit instantiations
@@ -937,6 +1238,34 @@ int mg_tri_sweep(const LevelView<double> &L, const Analytic *a0, const double *g
             L.msk, AStored{L.A, (size_t)L.mv * L.nv, L.nv}, L.x, L.b, gam, bet, L.mv, L.nv,
             active);
     return launch_status("tri_sweep");
+}
+
+// the coefficient bits of the analytic finest level, from the same rule as
+// analytic_coef (a coefficient is nonzero when the point's and the
+// neighbour's periodic-image cells are fluid)
+__global__ void k_nbmask(LevelView<double> L, uint16_t *nb) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= L.nv || j >= L.mv) return;
+    AnalyticT<double> one;
+    for (int k = 0; k < 5; k++) one.sc[k] = 1.;
+    one.a5 = 1.;
+    one.c3 = 1.;
+    const double c[9] = {analytic_coef(L, one, 0, j, i),         analytic_coef(L, one, 1, j, i),
+                         analytic_coef(L, one, 2, j, i),         analytic_coef(L, one, 3, j, i),
+                         analytic_coef(L, one, 3, j, i + 1),     analytic_coef(L, one, 2, j + 1, i - 1),
+                         analytic_coef(L, one, 1, j + 1, i),     analytic_coef(L, one, 0, j + 1, i + 1),
+                         analytic_coef(L, one, 4, j, i)};
+    unsigned b = 0;
+    for (int k = 0; k < 9; k++)
+        if (c[k] != 0.) b |= 1u << k;
+    nb[off(j, i, L.nv)] = (uint16_t)b;
+}
+
+int mg_nbmask(const LevelView<double> &L, uint16_t *nb, cudaStream_t s) {
+    dim3 b(32, 8);
+    k_nbmask<<<grid2d(L.mv, L.nv, b), b, 0, s>>>(L, nb);
+    return launch_status("nbmask");
 }
 
 __global__ void k_zero_active(double *x, size_t n, const int *active) {

@@ -15,37 +15,70 @@
 #include "f2d_fused.cuh"
 #include "f2d_kernels.cuh"
 #include "f2d_mixed.cuh"
+#include "f2d_batch.cuh"
 
 namespace f2d {
 
 // float copies of the planes the advection reads (tracers, u, v)
-__global__ void k_to_f32(const double *x, float *y, size_t n) {
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n;
-         q += (size_t)gridDim.x * blockDim.x)
-        y[q] = (float)x[q];
+struct ToF32Args {
+    const double *x;
+    float *y;
+    size_t n;
+};
+
+F2D_DEV void to_f32_body(const ToF32Args &a, const VB vb) {
+    for (size_t q = vb.x * (size_t)blockDim.x + threadIdx.x; q < a.n;
+         q += (size_t)vb.gx * blockDim.x)
+        a.y[q] = (float)a.x[q];
 }
+
+__global__ void k_to_f32(ToF32Args a) { to_f32_body(a, F2D_VB_NATIVE); }
+
+struct BToF32 {
+    using Args = ToF32Args;
+    static constexpr int THREADS = 256, KIND = BK_ToF32;
+    F2D_DEV static void run(const Args &a, VB vb) { to_f32_body(a, vb); }
+};
+F2D_BATCH_ENTRY(ToF32, BToF32)
 
 int vec_to_f32(const double *x, float *y, size_t n, cudaStream_t s) {
     int blocks = (int)((n + 255) / 256);
     if (blocks > 4096) blocks = 4096;
-    k_to_f32<<<blocks, 256, 0, s>>>(x, y, n);
-    return launch_status("to_f32");
+    return launch_body<BToF32>(k_to_f32, ToF32Args{x, y, n}, dim3(blocks), dim3(256), 0, s,
+                               "to_f32");
 }
 
 // celltocorner of a float tendency into the float64 right-hand side
 // (core/fortran_operators.f90:58-62, rows/cols 0..m-2)
-__global__ void k_c2c_f32(const float *xr, double *xp, int m, int n) {
-    int i = blockIdx.x * 32 + threadIdx.x;
-    int j = blockIdx.y * 8 + threadIdx.y;
+struct C2CF32Args {
+    const float *xr;
+    double *xp;
+    int m, n;
+};
+
+F2D_DEV void c2c_f32_body(const C2CF32Args &a, const VB vb) {
+    const int m = a.m, n = a.n;
+    int i = vb.x * 32 + threadIdx.x;
+    int j = vb.y * 8 + threadIdx.y;
     if (i > n - 2 || j > m - 2) return;
     size_t p = off(j, i, n);
-    xp[p] = (double)(0.25f * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]));
+    const float *xr = a.xr;
+    a.xp[p] = (double)(0.25f * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]));
 }
+
+__global__ void k_c2c_f32(C2CF32Args a) { c2c_f32_body(a, F2D_VB_NATIVE); }
+
+struct BC2CF32 {
+    using Args = C2CF32Args;
+    static constexpr int THREADS = 256, KIND = BK_C2CF32;
+    F2D_DEV static void run(const Args &a, VB vb) { c2c_f32_body(a, vb); }
+};
+F2D_BATCH_ENTRY(C2CF32, BC2CF32)
 
 int c2c_f32(const float *xr, double *xp, int m, int n, cudaStream_t s) {
     dim3 b(32, 8);
-    k_c2c_f32<<<grid2d(m - 1, n - 1, b), b, 0, s>>>(xr, xp, m, n);
-    return launch_status("c2c_f32");
+    return launch_body<BC2CF32>(k_c2c_f32, C2CF32Args{xr, xp, m, n}, grid2d(m - 1, n - 1, b), b,
+                                0, s, "c2c_f32");
 }
 
 // float RK combinations of the stage states (core/timescheme.py:172-176)
@@ -57,13 +90,13 @@ F2D_DEV float rk_stage_f32(int rk, float base, float d0, float dq, float dt) {
 // Advection of one tracer, float32 fluxes from float32 stage states.
 // rk 1, 2: next stage state (float); rk 3: final float64 accumulation
 // x += (dt/6)*(dx0 + dx1 + 4*dx2) of the state.
-__global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
+F2D_DEV void stage_adv_mixed_body(const AdvMixed &a, const VB vb) {
     __shared__ float sfx[8][33];
     __shared__ float sfy[9][32];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int nv = a.nv, mv = a.mv;
-    const int I = NH + blockIdx.x * 32 + tx;
-    const int J = NH + blockIdx.y * 8 + ty;
+    const int I = NH + vb.x * 32 + tx;
+    const int J = NH + vb.y * 8 + ty;
     const bool in = (I <= nv - NH - 1) && (J <= mv - NH - 1);
     const SplitT<float> c = *a.advf;
     if (in) {
@@ -116,18 +149,29 @@ __global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
         }
 }
 
+__global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
+    stage_adv_mixed_body(a, F2D_VB_NATIVE);
+}
+
+struct BAdvMixed {
+    using Args = AdvMixed;
+    static constexpr int THREADS = 256, KIND = BK_AdvMixed;
+    F2D_DEV static void run(const Args &a, VB vb) { stage_adv_mixed_body(a, vb); }
+};
+F2D_BATCH_ENTRY(AdvMixed, BAdvMixed)
+
 int stage_advection_mixed(const AdvMixed &a, cudaStream_t s) {
     dim3 b(32, 8);
-    k_stage_adv_mixed<<<grid2d(a.mv - 2 * NH, a.nv - 2 * NH, b), b, 0, s>>>(a);
-    return launch_status("stage_advection_mixed");
+    return launch_body<BAdvMixed>(k_stage_adv_mixed, a, grid2d(a.mv - 2 * NH, a.nv - 2 * NH, b),
+                                  b, 0, s, "stage_advection_mixed");
 }
 
 // psi <- psi*mskp (float64, whole array), u, v = orthogradient(psi) in float64
 // (the differences of psi need it) stored as float tendencies, and the
 // stage-state / final combinations.
-__global__ void __launch_bounds__(256) k_stage_ortho_mixed(OrthoMixed a) {
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
+F2D_DEV void stage_ortho_mixed_body(const OrthoMixed &a, const VB vb) {
+    const int i = vb.x * 32 + threadIdx.x;
+    const int j = vb.y * 8 + threadIdx.y;
     const int nv = a.nv, mv = a.mv;
     if (i >= nv || j >= mv) return;
     const size_t p = off(j, i, nv);
@@ -157,21 +201,48 @@ __global__ void __launch_bounds__(256) k_stage_ortho_mixed(OrthoMixed a) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_stage_ortho_mixed(OrthoMixed a) {
+    stage_ortho_mixed_body(a, F2D_VB_NATIVE);
+}
+
+struct BOrthoMixed {
+    using Args = OrthoMixed;
+    static constexpr int THREADS = 256, KIND = BK_OrthoMixed;
+    F2D_DEV static void run(const Args &a, VB vb) { stage_ortho_mixed_body(a, vb); }
+};
+F2D_BATCH_ENTRY(OrthoMixed, BOrthoMixed)
+
 int stage_ortho_mixed(const OrthoMixed &a, cudaStream_t s) {
     dim3 b(32, 8);
-    k_stage_ortho_mixed<<<grid2d(a.mv, a.nv, b), b, 0, s>>>(a);
-    return launch_status("stage_ortho_mixed");
+    return launch_body<BOrthoMixed>(k_stage_ortho_mixed, a, grid2d(a.mv, a.nv, b), b, 0, s,
+                                    "stage_ortho_mixed");
 }
 
 // float32 split constants and dt (set once per step, after set_dt)
-__global__ void k_split_f32(const SplitConst *c, const double *dt, SplitT<float> *cf, float *dtf) {
-    *cf = split_cast<float>(*c);
-    *dtf = (float)*dt;
+struct SplitF32Args {
+    const SplitConst *c;
+    const double *dt;
+    SplitT<float> *cf;
+    float *dtf;
+};
+
+F2D_DEV void split_f32_body(const SplitF32Args &a, const VB) {
+    *a.cf = split_cast<float>(*a.c);
+    *a.dtf = (float)*a.dt;
 }
 
+__global__ void k_split_f32(SplitF32Args a) { split_f32_body(a, F2D_VB_NATIVE); }
+
+struct BSplitF32 {
+    using Args = SplitF32Args;
+    static constexpr int THREADS = 1, KIND = BK_SplitF32;
+    F2D_DEV static void run(const Args &a, VB vb) { split_f32_body(a, vb); }
+};
+F2D_BATCH_ENTRY(SplitF32, BSplitF32)
+
 int split_f32(const double *advc, const double *dt, void *advf, float *dtf, cudaStream_t s) {
-    k_split_f32<<<1, 1, 0, s>>>((const SplitConst *)advc, dt, (SplitT<float> *)advf, dtf);
-    return launch_status("split_f32");
+    SplitF32Args a{(const SplitConst *)advc, dt, (SplitT<float> *)advf, dtf};
+    return launch_body<BSplitF32>(k_split_f32, a, dim3(1), dim3(1), 0, s, "split_f32");
 }
 
 }  // namespace f2d

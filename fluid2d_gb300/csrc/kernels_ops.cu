@@ -16,6 +16,8 @@
 #include "f2d_common.cuh"
 #include "f2d_kernels.cuh"
 
+#include "f2d_batch.cuh"
+
 namespace f2d {
 
 constexpr int OP_TX = 32, OP_TY = 8;
@@ -45,19 +47,36 @@ int launch_orthogradient(const int8_t *msk, const double *psi, double dx, double
 }
 
 // xp(j,i) = 0.25*(xr(j,i)+xr(j,i+1)+xr(j+1,i)+xr(j+1,i+1)), j,i in 1..m-1
-__global__ void k_celltocorner(const double *__restrict__ xr, double *__restrict__ xp, int m, int n) {
-    int i = blockIdx.x * OP_TX + threadIdx.x;
-    int j = blockIdx.y * OP_TY + threadIdx.y;
+struct CellToCornerArgs {
+    const double *xr;
+    double *xp;
+    int m, n;
+};
+
+F2D_DEV void celltocorner_body(const CellToCornerArgs &a, const VB vb) {
+    const int m = a.m, n = a.n;
+    int i = vb.x * OP_TX + threadIdx.x;
+    int j = vb.y * OP_TY + threadIdx.y;
     if (i > n - 2 || j > m - 2) return;
     size_t p = off(j, i, n);
-    xp[p] = 0.25 * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]);
+    const double *xr = a.xr;
+    a.xp[p] = 0.25 * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]);
 }
+
+__global__ void k_celltocorner(CellToCornerArgs a) { celltocorner_body(a, F2D_VB_NATIVE); }
+
+struct BCellToCorner {
+    using Args = CellToCornerArgs;
+    static constexpr int THREADS = OP_TX * OP_TY, KIND = BK_CellToCorner;
+    F2D_DEV static void run(const Args &a, VB vb) { celltocorner_body(a, vb); }
+};
+F2D_BATCH_ENTRY(CellToCorner, BCellToCorner)
 
 int launch_celltocorner(const double *xr, double *xp, int m, int n, cudaStream_t s) {
     if (m < 2 || n < 2) return OK;
     dim3 b(OP_TX, OP_TY);
-    k_celltocorner<<<grid2d(m - 1, n - 1, b), b, 0, s>>>(xr, xp, m, n);
-    return launch_status("celltocorner");
+    return launch_body<BCellToCorner>(k_celltocorner, CellToCornerArgs{xr, xp, m, n},
+                                      grid2d(m - 1, n - 1, b), b, 0, s, "celltocorner");
 }
 
 // xr(j,i) = 0.25*(xp(j,i)+xp(j,i-1)+xp(j-1,i)+xp(j-1,i-1)), j,i in 2..m
@@ -197,22 +216,36 @@ F2D_DEV void red_point(const int8_t *msk, const double *x, const double *y, size
 
 // Stage 1: block b reduces interior rows [b*rpb, (b+1)*rpb) (threads stride
 // over the row-major cells of those rows), writes NV partials.
+struct ReducePartialArgs {
+    const int8_t *msk;
+    const double *x, *y;
+    int nh, m, n, rpb;
+    double *part;
+};
+
 template <int KIND>
-__global__ void __launch_bounds__(RED_THREADS)
-k_reduce_partial(const int8_t *__restrict__ msk, const double *__restrict__ x,
-                 const double *__restrict__ y, int nh, int m, int n, int rpb,
-                 double *__restrict__ part) {
+F2D_DEV void reduce_partial_body(const ReducePartialArgs &a, const VB vb) {
     __shared__ double sh[RED_MAX_VALUES * RED_THREADS];
     constexpr RedSpec spec = red_spec(KIND);
+    const int8_t *msk = a.msk;
+    const double *x = a.x, *y = a.y;
+    const int nh = a.nh, m = a.m, n = a.n, rpb = a.rpb;
+    double *part = a.part;
     double acc[RED_MAX_VALUES] = {0., 0., 0., 0.};
     const int rows = m - 2 * nh, cols = n - 2 * nh;
-    const int r0 = blockIdx.x * rpb;
+    const int r0 = vb.x * rpb;
     const int r1 = min(rows, r0 + rpb);
-    const long long cells = (long long)(r1 - r0) * cols;
-    for (long long q = threadIdx.x; q < cells; q += RED_THREADS) {
-        int j = nh + r0 + (int)(q / cols);
-        int i = nh + (int)(q % cols);
-        red_point<KIND>(msk, x, y, off(j, i, n), n, acc);
+    // thread t takes cells t, t + RED_THREADS, ... of the block's rows in
+    // row-major order; its (row, column) advances without a division per cell
+    const int cells = (r1 - r0) * cols;
+    int jr = (int)threadIdx.x / cols, ic = (int)threadIdx.x - jr * cols;
+    for (int q = threadIdx.x; q < cells; q += RED_THREADS) {
+        red_point<KIND>(msk, x, y, off(nh + r0 + jr, nh + ic, n), n, acc);
+        ic += RED_THREADS;
+        while (ic >= cols) {
+            ic -= cols;
+            jr++;
+        }
     }
     double v[RED_MAX_VALUES];
     bool mx[RED_MAX_VALUES];
@@ -220,14 +253,27 @@ k_reduce_partial(const int8_t *__restrict__ msk, const double *__restrict__ x,
     for (int k = 0; k < RED_MAX_VALUES; k++) { v[k] = acc[k]; mx[k] = spec.is_max[k]; }
     block_reduce<RED_MAX_VALUES>(v, mx, sh);
     if (threadIdx.x == 0)
-        for (int k = 0; k < spec.nv; k++) part[k * RED_MAX_BLOCKS + blockIdx.x] = v[k];
+        for (int k = 0; k < spec.nv; k++) part[k * RED_MAX_BLOCKS + vb.x] = v[k];
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(ReducePartialArgs a) {
+    reduce_partial_body<KIND>(a, F2D_VB_NATIVE);
 }
 
 // Stage 2: one block reduces the partials in block order and applies the
 // routine's final scaling.
+struct ReduceFinalArgs {
+    const double *part;
+    int nblocks;
+    double *out;
+};
+
 template <int KIND>
-__global__ void __launch_bounds__(RED_THREADS)
-k_reduce_final(const double *__restrict__ part, int nblocks, double *__restrict__ out) {
+F2D_DEV void reduce_final_body(const ReduceFinalArgs &a, const VB) {
+    const double *part = a.part;
+    const int nblocks = a.nblocks;
+    double *out = a.out;
     __shared__ double sh[RED_MAX_VALUES * RED_THREADS];
     constexpr RedSpec spec = red_spec(KIND);
     double acc[RED_MAX_VALUES] = {0., 0., 0., 0.};
@@ -255,6 +301,34 @@ k_reduce_final(const double *__restrict__ part, int nblocks, double *__restrict_
     }
 }
 
+template <int KIND>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_final(ReduceFinalArgs a) {
+    reduce_final_body<KIND>(a, F2D_VB_NATIVE);
+}
+
+template <int RK>
+struct BReducePartial {
+    using Args = ReducePartialArgs;
+    static constexpr int THREADS = RED_THREADS;
+    static constexpr int KIND = RK == R_NORM ? BK_Reduce8P : (RK == R_SUM ? BK_Reduce2P : -1);
+    F2D_DEV static void run(const Args &a, VB vb) { reduce_partial_body<RK>(a, vb); }
+};
+template <int RK>
+struct BReduceFinal {
+    using Args = ReduceFinalArgs;
+    static constexpr int THREADS = RED_THREADS;
+    static constexpr int KIND = RK == R_NORM ? BK_Reduce8F : (RK == R_SUM ? BK_Reduce2F : -1);
+    F2D_DEV static void run(const Args &a, VB vb) { reduce_final_body<RK>(a, vb); }
+};
+using BReduce8P = BReducePartial<R_NORM>;
+using BReduce8F = BReduceFinal<R_NORM>;
+using BReduce2P = BReducePartial<R_SUM>;
+using BReduce2F = BReduceFinal<R_SUM>;
+F2D_BATCH_ENTRY(Reduce8P, BReduce8P)
+F2D_BATCH_ENTRY(Reduce8F, BReduce8F)
+F2D_BATCH_ENTRY(Reduce2P, BReduce2P)
+F2D_BATCH_ENTRY(Reduce2F, BReduce2F)
+
 int reduce_blocks(int rows) {
     if (rows <= 0) return 1;
     int rpb = (rows + RED_MAX_BLOCKS - 1) / RED_MAX_BLOCKS;
@@ -270,9 +344,12 @@ static int launch_reduce_t(const int8_t *msk, const double *x, const double *y, 
     int nb = reduce_blocks(rows);
     int rpb = rows > 0 ? (rows + nb - 1) / nb : 1;
     nb = rows > 0 ? (rows + rpb - 1) / rpb : 1;
-    k_reduce_partial<KIND><<<nb, RED_THREADS, 0, s>>>(msk, x, y, nh, m, n, rpb, work);
-    k_reduce_final<KIND><<<1, RED_THREADS, 0, s>>>(work, nb, out);
-    return launch_status("reduction");
+    int st = launch_body<BReducePartial<KIND>>(k_reduce_partial<KIND>,
+                                               ReducePartialArgs{msk, x, y, nh, m, n, rpb, work},
+                                               dim3(nb), dim3(RED_THREADS), 0, s, "reduction");
+    if (st) return st;
+    return launch_body<BReduceFinal<KIND>>(k_reduce_final<KIND>, ReduceFinalArgs{work, nb, out},
+                                           dim3(1), dim3(RED_THREADS), 0, s, "reduction");
 }
 
 int launch_reduce(int kind, const int8_t *msk, const double *x, const double *y, int nh,

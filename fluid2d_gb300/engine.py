@@ -255,6 +255,15 @@ class Model(object):
                    ctypes.byref(st))
         return nite.value, res.value, st.value
 
+    def coarse_switch(self, level=None):
+        """Query (level=None) or set the level from which the multigrid runs in
+        one CTA; returns (current, first allowed, number of levels)."""
+        cur, first, nlev = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._call("f2d_model_coarse_level", self.h, -1 if level is None else int(level),
+                   ctypes.byref(cur), ctypes.byref(first), ctypes.byref(nlev))
+        self.coarse_level = cur.value
+        return cur.value, first.value, nlev.value
+
     def set_islands(self, rhsp, psi):
         """Islands with a prescribed streamfunction: the rhsp and psi arrays of
         core/island.py (``fluid2d_gb300.island.Island.finalize``)."""
@@ -445,9 +454,54 @@ class Ensemble(object):
     CUDA_DEVICE_MAX_CONNECTIONS (up to 32) before CUDA is initialised.
     """
 
-    def __init__(self, models, nstreams=32):
+    def __init__(self, models, nstreams=32, batched=False, groups=1, policy=1):
         self.models = list(models)
         self.streams = [torch.cuda.Stream() for _ in range(max(1, nstreams))]
+        self.batch = None
+        if batched:
+            self.build_batch(groups, policy)
+
+    def build_batch(self, groups=1, policy=1):
+        """Batched steps: the instances, sorted by size, are split into
+        `groups` groups; one step of every instance of a group is merged into
+        launches that each run one kernel for the whole group
+        (f2d_batch_create), captured as one graph per group, and the groups'
+        graphs run on their own streams."""
+        self.free_batch()
+        L = self.models[0].L
+        order = sorted(range(len(self.models)), key=lambda k: self.models[k].cells)
+        groups = max(1, min(int(groups), len(order)))
+        self.batch = []
+        for g in range(groups):
+            idx = order[g * len(order) // groups:(g + 1) * len(order) // groups]
+            arr = (ctypes.c_void_p * len(idx))(*[self.models[k].h.value for k in idx])
+            h = ctypes.c_void_p()
+            _lib.call("f2d_batch_create", arr, len(idx), int(policy), ctypes.byref(h),
+                      variant=self.models[0].variant)
+            self.batch.append(h)
+        self._L = L
+
+    def batch_info(self):
+        """(launches per step, operations recorded) summed over the groups"""
+        tot = [0, 0]
+        for h in self.batch:
+            n, ops = ctypes.c_int(), ctypes.c_int()
+            _lib.call("f2d_batch_info", h, ctypes.byref(n), ctypes.byref(ops),
+                      variant=self.models[0].variant)
+            tot[0] += n.value
+            tot[1] += ops.value
+        return tuple(tot)
+
+    def free_batch(self):
+        for h in getattr(self, "batch", None) or []:
+            self._L.f2d_batch_destroy(h)
+        self.batch = None
+
+    def __del__(self):
+        try:
+            self.free_batch()
+        except Exception:
+            pass
 
     @property
     def cells(self):
@@ -456,6 +510,16 @@ class Ensemble(object):
     def run(self, nsteps, lockstep=False):
         """Advance every instance by nsteps (asynchronous)."""
         cur = torch.cuda.current_stream()
+        if self.batch is not None:
+            streams = self.streams[:len(self.batch)]
+            for s in streams:
+                s.wait_stream(cur)
+            for h, s in zip(self.batch, streams):
+                _lib.call("f2d_batch_step", h, int(nsteps), s.cuda_stream,
+                          variant=self.models[0].variant)
+            for s in streams:
+                cur.wait_stream(s)
+            return
         for s in self.streams:
             s.wait_stream(cur)
         if lockstep:
@@ -475,9 +539,11 @@ class Ensemble(object):
         self.run(1)
 
 
-def ensemble_from_workloads(wls, precision="fp64", variant="product", nstreams=32, **kw):
+def ensemble_from_workloads(wls, precision="fp64", variant="product", nstreams=32, batched=False,
+                            groups=1, policy=1, **kw):
     """An Ensemble of initialised models (psi set, diagnostics, fixed dt from
-    CFL 0.8 on each instance's initial max|u|)."""
+    CFL 0.8 on each instance's initial max|u|); batched: one merged graph of
+    batched launches instead of per-instance graphs on streams."""
     models = []
     for wl in wls:
         m = from_workload(wl, precision=precision, variant=variant, **kw)
@@ -486,4 +552,4 @@ def ensemble_from_workloads(wls, precision="fp64", variant="product", nstreams=3
         if d["maxspeed"] > 0:
             m.set_dt(0.8 * min(m.dx, m.dy) / d["maxspeed"])
         models.append(m)
-    return Ensemble(models, nstreams=nstreams)
+    return Ensemble(models, nstreams=nstreams, batched=batched, groups=groups, policy=policy)

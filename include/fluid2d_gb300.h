@@ -263,6 +263,26 @@ int f2d_model_graph_kernels(void *model, int *nkernels);
  * grid.msknoslip: the geometry's mask before islands are carved). */
 int f2d_model_noslip(void *model, const int8_t *msknoslip_host, void *stream);
 
+/* The level from which the multigrid runs in one CTA out of shared memory
+ * (default: the finest level whose coarser suffix fits).  Any level from
+ * *first to nlev (no CTA) may be chosen; results are identical, only the
+ * launch structure (and speed) changes.  level < 0 only queries. */
+int f2d_model_coarse_level(void *model, int level, int *current, int *first, int *nlev);
+
+/* ---- batched steps: one step of each of n models (Euler or Boussinesq, float64
+ * or mixed, without no-slip walls, islands or line relaxation) recorded and
+ * merged into launches that each run one kernel for many models, captured in
+ * one CUDA graph.  Each model computes exactly what f2d_model_step computes.
+ * Rebuild after changing a model's dt or options. */
+/* policy 0: each launch runs the kernel the most models need next; 1: the
+ * next kernel of the model with the most work left, joined by every model
+ * that needs the same kernel next */
+int f2d_batch_create(void **models, int n, int policy, void **batch);
+int f2d_batch_step(void *batch, int nsteps, void *stream);
+/* launches per batched step and operations recorded over all models */
+int f2d_batch_info(void *batch, int *launches, int *ops);
+int f2d_batch_destroy(void *batch);
+
 /* ---- islands with a prescribed streamfunction (core/island.py:21-47 gives
  * the two arrays; core/fluid2d.py:110-113 hands them to the operators): the
  * full inversions, the no-slip inversion and QG's stage inversions subtract

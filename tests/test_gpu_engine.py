@@ -175,3 +175,32 @@ def test_gmg_line_relaxation(eng, geom, hyd, dyfac):
     xg = torch.from_numpy(x).cuda()
     G.solve(xg, torch.from_numpy(b).cuda())
     assert relerr(xg.cpu().numpy(), xo) <= 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_coarse_level_changes_nothing_but_launches(eng, precision):
+    """Any switch level of the single-CTA coarse solve gives the same state
+    bit for bit (exact build), and the autotuner picks one of them."""
+    import torch
+    from fluid2d_gb300 import workloads as W
+    from fluid2d_gb300.autotune import tune_coarse_level
+    wl = W.dipole(128, 96, seed=3)
+    states = []
+    probe = eng.from_workload(wl, variant="exact", precision=precision, dt=2e-3)
+    cur, first, nlev = probe.coarse_switch()
+    assert first <= cur <= nlev
+    for level in sorted({first, (first + nlev) // 2, nlev}):
+        M = eng.from_workload(wl, variant="exact", precision=precision, dt=2e-3)
+        M.set_psi_from_vorticity()
+        M.diagnostics()
+        M.coarse_switch(level)
+        M.run(3)
+        torch.cuda.synchronize()
+        states.append(M.var.state.clone())
+    for st in states[1:]:
+        assert torch.equal(st, states[0])
+    M = eng.from_workload(wl, precision=precision, dt=2e-3)
+    M.set_psi_from_vorticity()
+    M.diagnostics()
+    best, times = tune_coarse_level(M, steps=2, warmup=1, use_cache=False)
+    assert best in times and M.coarse_switch()[0] == best

@@ -236,6 +236,7 @@ EXTRA = {
     "f2d_model_buffer": ([_P, ctypes.c_char_p], _P),
     "f2d_model_flux_name": ([_P, _I], ctypes.c_char_p),
     "f2d_version": ([], _I),
+    "f2d_set_pdl": ([_I], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),
 }

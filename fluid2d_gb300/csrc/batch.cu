@@ -15,6 +15,7 @@
 
 #include "f2d_batch.cuh"
 #include "f2d_common.cuh"
+#include "../../include/fluid2d_gb300.h"
 
 namespace f2d {
 
@@ -27,6 +28,11 @@ namespace f2d {
 Recorder *&recorder() {
     static thread_local Recorder *r = nullptr;
     return r;
+}
+
+bool &pdl_enabled() {
+    static bool on = false;
+    return on;
 }
 
 static BatchLaunchFn batch_launcher(int kind) {
@@ -247,3 +253,16 @@ int batch_info(void *b, int *launches, int *ops) {
 void batch_destroy(void *b) { delete (Batch *)b; }
 
 }  // namespace f2d
+
+extern "C" {
+
+// programmatic dependent launch of the engine kernels: on (1) or off (0, the
+// default); returns the previous setting.  Graphs captured before a change
+// keep the launches they were captured with.
+int f2d_set_pdl(int enable) {
+    const int prev = f2d::pdl_enabled() ? 1 : 0;
+    if (enable >= 0) f2d::pdl_enabled() = enable != 0;
+    return prev;
+}
+
+}  // extern "C"

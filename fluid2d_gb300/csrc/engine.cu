@@ -160,7 +160,8 @@ F2D_DEV void solve_init_body(const SolveInitArgs &a, const VB) {
     }
 }
 
-__global__ void k_solve_init(SolveInitArgs a) { solve_init_body(a, F2D_VB_NATIVE); }
+__global__ void k_solve_init(SolveInitArgs a) { pdl_prologue();
+    solve_init_body(a, F2D_VB_NATIVE); }
 
 struct BSolveInit {
     using Args = SolveInitArgs;
@@ -199,7 +200,8 @@ F2D_DEV void solve_update_body(const SolveUpdateArgs &a, const VB) {
     st->active = (st->nite < st->maxite) && (st->res0 > st->tol);
 }
 
-__global__ void k_solve_update(SolveUpdateArgs a) { solve_update_body(a, F2D_VB_NATIVE); }
+__global__ void k_solve_update(SolveUpdateArgs a) { pdl_prologue();
+    solve_update_body(a, F2D_VB_NATIVE); }
 
 struct BSolveUpdate {
     using Args = SolveUpdateArgs;
@@ -771,6 +773,7 @@ F2D_DEV void diag_partial_body(const DiagArgs &a, const VB blk) {
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_diag_partial(DiagArgs a) {
+    pdl_prologue();
     diag_partial_body(a, F2D_VB_NATIVE);
 }
 
@@ -819,6 +822,7 @@ F2D_DEV void diag_final_body(const DiagArgs &a, const VB) {
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a) {
+    pdl_prologue();
     diag_final_body(a, F2D_VB_NATIVE);
 }
 
@@ -868,7 +872,8 @@ F2D_DEV void set_dt_body(const SetDtArgs &a, const VB) {
     *advc = split_const(cst);
 }
 
-__global__ void k_set_dt(SetDtArgs a) { set_dt_body(a, F2D_VB_NATIVE); }
+__global__ void k_set_dt(SetDtArgs a) { pdl_prologue();
+    set_dt_body(a, F2D_VB_NATIVE); }
 
 struct BSetDt {
     using Args = SetDtArgs;
@@ -907,7 +912,8 @@ F2D_DEV void banom_body(const BanomArgs &a, const VB vb) {
         a.s[5 * a.pl + q] = a.s[4 * a.pl + q] - a.bref[q];
 }
 
-__global__ void k_banom(BanomArgs a) { banom_body(a, F2D_VB_NATIVE); }
+__global__ void k_banom(BanomArgs a) { pdl_prologue();
+    banom_body(a, F2D_VB_NATIVE); }
 
 struct BBanom {
     using Args = BanomArgs;

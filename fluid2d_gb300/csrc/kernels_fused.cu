@@ -234,11 +234,13 @@ F2D_DEV void sweep2_body(const SweepArgs<T> &A, const VB vb) {
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY) k_sweep1(SweepArgs<T> a) {
+    pdl_prologue();
     sweep1_body<T, L0>(a, F2D_VB_NATIVE);
 }
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY) k_sweep2(SweepArgs<T> a) {
+    pdl_prologue();
     sweep2_body<T, L0>(a, F2D_VB_NATIVE);
 }
 
@@ -264,6 +266,7 @@ F2D_DEV void residual_body(const ResidualArgs<T> &A, const VB vb) {
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(LV_TX *LV_TY) k_residual(ResidualArgs<T> a) {
+    pdl_prologue();
     residual_body<T, L0>(a, F2D_VB_NATIVE);
 }
 
@@ -281,6 +284,7 @@ F2D_DEV void residual_mixed_body(const ResidualArgs<double> &A, const VB vb) {
 }
 
 __global__ void __launch_bounds__(LV_TX *LV_TY) k_residual_mixed(ResidualArgs<double> a) {
+    pdl_prologue();
     residual_mixed_body(a, F2D_VB_NATIVE);
 }
 
@@ -314,7 +318,8 @@ F2D_DEV void add_f32_body(const AddF32Args &A, const VB vb) {
         A.x[q] = A.x[q] + (double)A.e[q];
 }
 
-__global__ void k_add_f32(AddF32Args a) { add_f32_body(a, F2D_VB_NATIVE); }
+__global__ void k_add_f32(AddF32Args a) { pdl_prologue();
+    add_f32_body(a, F2D_VB_NATIVE); }
 
 struct BAddF32 {
     using Args = AddF32Args;
@@ -351,6 +356,7 @@ F2D_DEV void restrict_body(const RestrictArgs<T> &A, const VB vb) {
 
 template <typename T>
 __global__ void __launch_bounds__(LV_TX *LV_TY) k_restrict(RestrictArgs<T> a) {
+    pdl_prologue();
     restrict_body<T>(a, F2D_VB_NATIVE);
 }
 
@@ -379,6 +385,7 @@ F2D_DEV void interp_body(const InterpArgs<T> &A, const VB vb) {
 
 template <typename T>
 __global__ void __launch_bounds__(LV_TX *LV_TY) k_interp(InterpArgs<T> a) {
+    pdl_prologue();
     interp_body<T>(a, F2D_VB_NATIVE);
 }
 
@@ -593,6 +600,7 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(FS_TX *FS_TY) k_smooth_fused(SmoothFusedArgs<T> a) {
+    pdl_prologue();
     smooth_fused_body<T, L0>(a, F2D_VB_NATIVE);
 }
 
@@ -676,6 +684,7 @@ F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
 
 template <typename T, bool L0>
 __global__ void __launch_bounds__(RR_TX *RR_TY) k_resres(ResresArgs<T> a) {
+    pdl_prologue();
     resres_body<T, L0>(a, F2D_VB_NATIVE);
 }
 
@@ -910,6 +919,7 @@ F2D_DEV void coarse_body(const CoarseArgs<T> &a, const VB) {
 
 template <typename T>
 __global__ void __launch_bounds__(CO_THREADS) k_coarse(CoarseArgs<T> a) {
+    pdl_prologue();
     coarse_body<T>(a, F2D_VB_NATIVE);
 }
 
@@ -1033,6 +1043,7 @@ F2D_DEV void stage_adv_body(const AdvStage &a, const VB vb) {
 
 template <typename TC>
 __global__ void __launch_bounds__(256) k_stage_adv(AdvStage a) {
+    pdl_prologue();
     stage_adv_body<TC>(a, F2D_VB_NATIVE);
 }
 
@@ -1090,6 +1101,7 @@ F2D_DEV void stage_ortho_body(const OrthoStage &a, const VB vb) {
 }
 
 __global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
+    pdl_prologue();
     stage_ortho_body(a, F2D_VB_NATIVE);
 }
 
@@ -1120,7 +1132,8 @@ F2D_DEV void vec_add_body(const VecAddArgs &A, const VB vb) {
         A.x[q] = A.x[q] + A.y[q];
 }
 
-__global__ void k_vec_add(VecAddArgs a) { vec_add_body(a, F2D_VB_NATIVE); }
+__global__ void k_vec_add(VecAddArgs a) { pdl_prologue();
+    vec_add_body(a, F2D_VB_NATIVE); }
 
 struct BVecAdd {
     using Args = VecAddArgs;
@@ -1151,7 +1164,8 @@ F2D_DEV void sub_mean_body(const SubMeanArgs &A, const VB vb) {
         A.x[q] = A.x[q] - m;
 }
 
-__global__ void k_sub_mean(SubMeanArgs a) { sub_mean_body(a, F2D_VB_NATIVE); }
+__global__ void k_sub_mean(SubMeanArgs a) { pdl_prologue();
+    sub_mean_body(a, F2D_VB_NATIVE); }
 
 struct BSubMean {
     using Args = SubMeanArgs;

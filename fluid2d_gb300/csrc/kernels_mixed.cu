@@ -32,7 +32,8 @@ F2D_DEV void to_f32_body(const ToF32Args &a, const VB vb) {
         a.y[q] = (float)a.x[q];
 }
 
-__global__ void k_to_f32(ToF32Args a) { to_f32_body(a, F2D_VB_NATIVE); }
+__global__ void k_to_f32(ToF32Args a) { pdl_prologue();
+    to_f32_body(a, F2D_VB_NATIVE); }
 
 struct BToF32 {
     using Args = ToF32Args;
@@ -66,7 +67,8 @@ F2D_DEV void c2c_f32_body(const C2CF32Args &a, const VB vb) {
     a.xp[p] = (double)(0.25f * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]));
 }
 
-__global__ void k_c2c_f32(C2CF32Args a) { c2c_f32_body(a, F2D_VB_NATIVE); }
+__global__ void k_c2c_f32(C2CF32Args a) { pdl_prologue();
+    c2c_f32_body(a, F2D_VB_NATIVE); }
 
 struct BC2CF32 {
     using Args = C2CF32Args;
@@ -150,6 +152,7 @@ F2D_DEV void stage_adv_mixed_body(const AdvMixed &a, const VB vb) {
 }
 
 __global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
+    pdl_prologue();
     stage_adv_mixed_body(a, F2D_VB_NATIVE);
 }
 
@@ -202,6 +205,7 @@ F2D_DEV void stage_ortho_mixed_body(const OrthoMixed &a, const VB vb) {
 }
 
 __global__ void __launch_bounds__(256) k_stage_ortho_mixed(OrthoMixed a) {
+    pdl_prologue();
     stage_ortho_mixed_body(a, F2D_VB_NATIVE);
 }
 
@@ -231,7 +235,8 @@ F2D_DEV void split_f32_body(const SplitF32Args &a, const VB) {
     *a.dtf = (float)*a.dt;
 }
 
-__global__ void k_split_f32(SplitF32Args a) { split_f32_body(a, F2D_VB_NATIVE); }
+__global__ void k_split_f32(SplitF32Args a) { pdl_prologue();
+    split_f32_body(a, F2D_VB_NATIVE); }
 
 struct BSplitF32 {
     using Args = SplitF32Args;

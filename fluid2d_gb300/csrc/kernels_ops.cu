@@ -63,7 +63,8 @@ F2D_DEV void celltocorner_body(const CellToCornerArgs &a, const VB vb) {
     a.xp[p] = 0.25 * (xr[p] + xr[p + 1] + xr[p + n] + xr[p + n + 1]);
 }
 
-__global__ void k_celltocorner(CellToCornerArgs a) { celltocorner_body(a, F2D_VB_NATIVE); }
+__global__ void k_celltocorner(CellToCornerArgs a) { pdl_prologue();
+    celltocorner_body(a, F2D_VB_NATIVE); }
 
 struct BCellToCorner {
     using Args = CellToCornerArgs;
@@ -258,6 +259,7 @@ F2D_DEV void reduce_partial_body(const ReducePartialArgs &a, const VB vb) {
 
 template <int KIND>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_partial(ReducePartialArgs a) {
+    pdl_prologue();
     reduce_partial_body<KIND>(a, F2D_VB_NATIVE);
 }
 
@@ -303,6 +305,7 @@ F2D_DEV void reduce_final_body(const ReduceFinalArgs &a, const VB) {
 
 template <int KIND>
 __global__ void __launch_bounds__(RED_THREADS) k_reduce_final(ReduceFinalArgs a) {
+    pdl_prologue();
     reduce_final_body<KIND>(a, F2D_VB_NATIVE);
 }
 

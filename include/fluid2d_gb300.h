@@ -269,6 +269,12 @@ int f2d_model_noslip(void *model, const int8_t *msknoslip_host, void *stream);
  * launch structure (and speed) changes.  level < 0 only queries. */
 int f2d_model_coarse_level(void *model, int level, int *current, int *first, int *nlev);
 
+/* Programmatic dependent launch of the engine kernels (each kernel may be
+ * scheduled while its predecessor runs and waits for it before touching
+ * memory): 1 on, 0 off (default), < 0 query; returns the previous setting.
+ * Graphs captured before a change keep their launches. */
+int f2d_set_pdl(int enable);
+
 /* ---- batched steps: one step of each of n models (Euler or Boussinesq, float64
  * or mixed, without no-slip walls, islands or line relaxation) recorded and
  * merged into launches that each run one kernel for many models, captured in

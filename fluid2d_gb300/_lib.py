@@ -213,6 +213,7 @@ SIGNATURES.update({
     "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],
     "f2d_model_coarse_level": [_P, _I, _PI, _PI, _PI],
+    "f2d_model_coarse_op": [_P, _I, _PI],
     "f2d_batch_create": [ctypes.POINTER(ctypes.c_void_p), _I, _I, _PP],
     "f2d_batch_step": [_P, _I, _P],
     "f2d_batch_info": [_P, _PI, _PI],
@@ -237,6 +238,7 @@ EXTRA = {
     "f2d_model_flux_name": ([_P, _I], ctypes.c_char_p),
     "f2d_version": ([], _I),
     "f2d_set_pdl": ([_I], _I),
+    "f2d_set_level_tiles": ([_I], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),
 }

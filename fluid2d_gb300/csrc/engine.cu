@@ -265,10 +265,32 @@ struct Gmg {
     bool probe = false;
     int nprobe = 0;
     cudaEvent_t ev[MAX_PROBES][2] = {};
+    // The coarse part from level cs started from x = 0 as dense linear maps
+    // of the level's interior b (product build): [0] the V-cycle, [1] the
+    // F-cycle, for op_n <= COARSE_OP_MAX interior points.
+    static constexpr int COARSE_OP_MAX = 1024;
+    bool coarse_op = true;
+    int op_cs = -1, op_n = 0;
+    double *opd[2] = {};
+    float *opf[2] = {};
+    template <typename T>
+    const T *op(int k) const;
+    int build_coarse_op(cudaStream_t s);
+    void free_coarse_op() {
+        for (int k = 0; k < 2; k++) {
+            if (opd[k]) cudaFree(opd[k]);
+            if (opf[k]) cudaFree(opf[k]);
+            opd[k] = nullptr;
+            opf[k] = nullptr;
+        }
+        op_cs = -1;
+        op_n = 0;
+    }
     ~Gmg() {
         for (int k = 0; k < MAX_PROBES; k++)
             for (int e = 0; e < 2; e++)
                 if (ev[k][e]) cudaEventDestroy(ev[k][e]);
+        free_coarse_op();
     }
 
     int setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, double hydroeps,
@@ -299,6 +321,61 @@ template <>
 const AnalyticT<double> *Gmg::analytic<double>() const { return &an; }
 template <>
 const AnalyticT<float> *Gmg::analytic<float>() const { return &anf; }
+template <>
+const double *Gmg::op<double>(int k) const { return opd[k]; }
+template <>
+const float *Gmg::op<float>(int k) const { return opf[k]; }
+
+template <typename T>
+static CoarseArgs<T> coarse_args(const Gmg &g, const LevelView<T> *L, int start, int mode,
+                                 bool zero_first, const int *active) {
+    CoarseArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.nlev = g.nlev - start;
+    for (int l = start; l < g.nlev; l++) a.lev[l - start] = L[l];
+    a.c1 = (T)g.omega;
+    a.c2 = (T)(1. - g.omega);
+    a.mode = mode;
+    a.zero_first = zero_first;
+    a.ndeepest = g.ndeepest;
+    a.active = active;
+    return a;
+}
+
+// (Re)build the coarse operators for the current cs: column k of each is the
+// cycle applied to the unit vector of interior point k, computed by the same
+// shared-memory cycle kernel.  The exact build keeps the reference's order of
+// operations everywhere and builds none.
+int Gmg::build_coarse_op(cudaStream_t s) {
+    free_coarse_op();
+#ifdef F2D_EXACT
+    return OK;
+#else
+    if (!coarse_op || tri || cs >= nlev) return OK;
+    const int m2 = mv[cs] - 2 * NH, n2 = nv[cs] - 2 * NH;
+    if (m2 < NH || n2 < NH || (long long)m2 * n2 > COARSE_OP_MAX) return OK;
+    const int n = m2 * n2;
+    const size_t nn = (size_t)n * n;
+    for (int k = 0; k < 2; k++) {
+        TRY(cuda_status(cudaMalloc((void **)&opd[k], nn * sizeof(double)), "coarse operator"));
+        if (has_f32)
+            TRY(cuda_status(cudaMalloc((void **)&opf[k], nn * sizeof(float)), "coarse operator"));
+    }
+    const size_t sm64 = coarse_smem_bytes<double>(mv + cs, nv + cs, nlev - cs);
+    const size_t sm32 = coarse_smem_bytes<float>(mv + cs, nv + cs, nlev - cs);
+    for (int k = 0; k < 2; k++) {
+        const int mode = k == 0 ? CYCLE_V : CYCLE_F;
+        TRY(mg_coarse_columns<double>(coarse_args<double>(*this, d, cs, mode, true, nullptr), sm64,
+                                      opd[k], n, s));
+        if (has_f32)
+            TRY(mg_coarse_columns<float>(coarse_args<float>(*this, f, cs, mode, true, nullptr),
+                                         sm32, opf[k], n, s));
+    }
+    op_cs = cs;
+    op_n = n;
+    return OK;
+#endif
+}
 
 int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, double hydroeps,
                double om, bool qg, double Rd, bool f32, cudaStream_t s) {
@@ -480,7 +557,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
             bet[l] = mem.at<double>(o_bet[l]);
             TRY(mg_tri_factor(d[l], l == 0 ? &an : nullptr, gam[l], bet[l], s));
         }
-    return OK;
+    return build_coarse_op(s);
 }
 
 template <typename T>
@@ -538,18 +615,12 @@ int Gmg::smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream
 template <typename T>
 int Gmg::coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int *active,
                 cudaStream_t s) {
-    CoarseArgs<T> a;
-    memset(&a, 0, sizeof(a));
-    a.nlev = nlev - start;
-    for (int l = start; l < nlev; l++) a.lev[l - start] = L[l];
-    a.c1 = (T)omega;
-    a.c2 = (T)(1. - omega);
-    a.mode = mode;
-    a.zero_first = zero_first;
-    a.ndeepest = ndeepest;
-    a.active = active;
+    if (op_n > 0 && op_cs == cs && start == cs && (mode == CYCLE_F || zero_first)) {
+        const T *o = op<T>(mode == CYCLE_F ? 1 : 0);
+        if (o) return mg_coarse_apply<T>(o, op_n, L[start], active, s);
+    }
     size_t smem = coarse_smem_bytes<T>(mv + start, nv + start, nlev - start);
-    return mg_coarse<T>(a, smem, s);
+    return mg_coarse<T>(coarse_args<T>(*this, L, start, mode, zero_first, active), smem, s);
 }
 
 // core/gmg/hierarchy.py:98-126.  first_mode: the first level's input is x
@@ -1860,6 +1931,34 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
 // the finest whose suffix fits the CTA's shared memory to nlev (no CTA).  The
 // arithmetic is the same either way; only the launch structure changes.
 // level < 0 only queries.
+}  // extern "C"
+
+// the captured step and loop graphs hold the old launch structure
+static void drop_graphs(Model *M) {
+    if (M->gexec) cudaGraphExecDestroy(M->gexec);
+    if (M->graph) cudaGraphDestroy(M->graph);
+    M->gexec = nullptr;
+    M->graph = nullptr;
+    if (M->loop) {
+        if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
+        if (M->loop->graph) cudaGraphDestroy(M->loop->graph);
+        M->loop->exec = nullptr;
+        M->loop->graph = nullptr;
+    }
+}
+
+// rebuild the coarse operators on a private stream and wait for them
+static int rebuild_coarse_op(Gmg &g) {
+    cudaStream_t s = nullptr;
+    TRY(cuda_status(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "coarse op stream"));
+    int st = g.build_coarse_op(s);
+    const int st2 = cuda_status(cudaStreamSynchronize(s), "coarse op build");
+    cudaStreamDestroy(s);
+    return st ? st : st2;
+}
+
+extern "C" {
+
 int f2d_model_coarse_level(void *model, int level, int *current, int *first, int *nlev) {
     Model *M = (Model *)model;
     if (!M) return ERR_ARG;
@@ -1872,21 +1971,26 @@ int f2d_model_coarse_level(void *model, int level, int *current, int *first, int
         }
         if (level != g.cs) {
             g.cs = level;
-            if (M->gexec) cudaGraphExecDestroy(M->gexec);
-            if (M->graph) cudaGraphDestroy(M->graph);
-            M->gexec = nullptr;
-            M->graph = nullptr;
-            if (M->loop) {
-                if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
-                if (M->loop->graph) cudaGraphDestroy(M->loop->graph);
-                M->loop->exec = nullptr;
-                M->loop->graph = nullptr;
-            }
+            drop_graphs(M);
+            TRY(rebuild_coarse_op(g));
         }
     }
     if (current) *current = g.cs;
     if (first) *first = g.cs_min;
     if (nlev) *nlev = g.nlev;
+    return OK;
+}
+
+int f2d_model_coarse_op(void *model, int enable, int *n) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    Gmg &g = M->gmg;
+    if (enable >= 0 && (enable != 0) != g.coarse_op) {
+        g.coarse_op = enable != 0;
+        drop_graphs(M);
+        TRY(rebuild_coarse_op(g));
+    }
+    if (n) *n = g.op_n;
     return OK;
 }
 

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(Body::THREADS)
     X(SolveInit) X(SolveUpdate) X(DiagP) X(DiagF) X(StageAdv64) X(StageOrtho) X(VecAdd)     \
     X(SubMean) X(Sweep1D1) X(Sweep2D1) X(ResidualD1) X(RestrictD) X(RestrictF) X(InterpD)   \
     X(SmoothFusedD0) X(SmoothFusedF0) X(SmoothFusedF1) X(ResresD0) X(ResresF0) X(ResresF1) \
-    X(CoarseD) X(CoarseF)
+    X(CoarseD) X(CoarseF) X(CoarseApplyD) X(CoarseApplyF)
 
 enum BodyKind {
 #define F2D_KIND_ENUM(n) BK_##n,

@@ -71,6 +71,13 @@ int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine
               bool assign, const int *active, cudaStream_t s);
 template <typename T>
 int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s);
+// the coarse part as a linear map: its n x n operator (one CTA per column),
+// and its application to the first level's b into x
+template <typename T>
+int mg_coarse_columns(const CoarseArgs<T> &args, size_t smem, T *op, int n, cudaStream_t s);
+template <typename T>
+int mg_coarse_apply(const T *op, int n, const LevelView<T> &L, const int *active,
+                    cudaStream_t s);
 // fused smoothtwicewitha: input per xmode (0 x, 1 zero, 2 x + interp(coarse),
 // 3 interp(coarse)), result into `out` (not x)
 template <typename T>

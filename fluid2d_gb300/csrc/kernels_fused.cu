@@ -21,6 +21,7 @@
 #include "f2d_adv.cuh"
 #include "f2d_tri.cuh"
 #include "f2d_batch.cuh"
+#include "../../include/fluid2d_gb300.h"
 
 namespace f2d {
 
@@ -197,6 +198,50 @@ F2D_DEV bool inactive(const int *active) { return active != nullptr && *active =
 
 // ------------------------------------------------------------ level kernels
 constexpr int LV_TX = 32, LV_TY = 8;
+
+// The number of CTAs a level kernel's grid aims at before its tile stops
+// shrinking: < 0 twice the SM count, 0 always the largest tile (default:
+// a warp's float64 instructions issue at most one per 64 cycles whatever its
+// active lanes, so a smaller tile does not shorten a small level's chain and
+// measured slower on the 1024^2 step and the ensemble).
+int &level_tile_target() {
+    static int t = 0;
+    return t;
+}
+
+static int sm_count() {
+    static int n[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!n[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) v = 0;
+        n[dev] = v > 0 ? v : 152;
+    }
+    return n[dev];
+}
+
+// The CTA tile of a level kernel over rows x cols points: start from the
+// kernel's largest tile (tx, ty) and halve it (the longer side first, down to
+// 8 x 4, one warp) while the grid has fewer CTAs than the target.
+dim3 level_tile(int rows, int cols, int tx, int ty) {
+    int target = level_tile_target();
+    if (target == 0) return dim3(tx, ty);
+    if (target < 0) target = 2 * sm_count();
+    rows = rows > 0 ? rows : 1;
+    cols = cols > 0 ? cols : 1;
+    while ((long long)((cols + tx - 1) / tx) * ((rows + ty - 1) / ty) < target) {
+        if (tx > ty && tx > 8)
+            tx /= 2;
+        else if (ty > 4)
+            ty /= 2;
+        else if (tx > 8)
+            tx /= 2;
+        else
+            break;
+    }
+    return dim3(tx, ty);
+}
 
 static inline dim3 lv_grid(int rows, int cols) {
     return grid2d(rows > 0 ? rows : 1, cols > 0 ? cols : 1, dim3(LV_TX, LV_TY));
@@ -492,7 +537,19 @@ int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine
 // writes the tile (and its periodic halo images) to a separate output array:
 // x is read by neighbouring CTAs while they run, so it is never updated in
 // place.  Same arithmetic, same order as the unfused kernels.
+//
+// The tile is the CTA shape (blockDim), chosen per level by level_tile().
 constexpr int FS_TX = 32, FS_TY = 16;
+
+// quotient and remainder of a small index by a small divisor through a float
+// reciprocal: q < 2^16 and d <= 64 keep the error of (q + 0.5) * (1/d) far
+// below the 0.5/d margin to the next integer, so the floor is exact.
+F2D_DEV int small_div(int q, float inv) { return (int)(((float)q + 0.5f) * inv); }
+
+template <typename T>
+size_t smooth_fused_smem(dim3 b) {
+    return sizeof(T) * ((size_t)(b.y + 4) * (b.x + 4) + (size_t)(b.y + 2) * (b.x + 2));
+}
 
 template <typename T>
 struct CoarseSrc {
@@ -516,9 +573,11 @@ struct SmoothFusedArgs {
 template <typename T, bool L0>
 F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
-    constexpr int XW = FS_TX + 4, XH = FS_TY + 4, TW = FS_TX + 2, TH = FS_TY + 2;
-    __shared__ T xs[XH * XW];
-    __shared__ T ts[TH * TW];
+    const int TX = (int)blockDim.x, TY = (int)blockDim.y, NT = TX * TY;
+    const int XW = TX + 4, XH = TY + 4, TW = TX + 2, TH = TY + 2;
+    extern __shared__ __align__(16) unsigned char sm[];
+    T *xs = (T *)sm;
+    T *ts = xs + XH * XW;
     const LevelView<T> L = A.L;
     const AnalyticT<T> an = A.an;
     const T c1 = A.c1, c2 = A.c2;
@@ -526,12 +585,14 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     const CoarseSrc<T> cs = A.cs;
     T *out = A.out;
     const int mv = L.mv, nv = L.nv;
-    const int i0 = NH + vb.x * FS_TX, j0 = NH + vb.y * FS_TY;
-    const int tid = threadIdx.y * FS_TX + threadIdx.x;
-    // input x on [j0-2, j0+FS_TY+1] x [i0-2, i0+FS_TX+1], inside rows/cols 1..m-2
+    const int i0 = NH + vb.x * TX, j0 = NH + vb.y * TY;
+    const int tid = threadIdx.y * TX + threadIdx.x;
+    // input x on [j0-2, j0+TY+1] x [i0-2, i0+TX+1], inside rows/cols 1..m-2
     if (xmode != X_ZERO) {
-        for (int q = tid; q < XH * XW; q += FS_TX * FS_TY) {
-            const int j = j0 - 2 + q / XW, i = i0 - 2 + q % XW;
+        const float inv = 1.0f / (float)XW;
+        for (int q = tid; q < XH * XW; q += NT) {
+            const int qj = small_div(q, inv);
+            const int j = j0 - 2 + qj, i = i0 - 2 + (q - qj * XW);
             if (j < 1 || j > mv - 2 || i < 1 || i > nv - 2) continue;
             const size_t p = off(j, i, nv);
             T v;
@@ -545,9 +606,11 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
         }
     }
     __syncthreads();
-    // first sweep on [j0-1, j0+FS_TY] x [i0-1, i0+FS_TX], inside rows/cols 2..m-3
-    for (int q = tid; q < TH * TW; q += FS_TX * FS_TY) {
-        const int j = j0 - 1 + q / TW, i = i0 - 1 + q % TW;
+    // first sweep on [j0-1, j0+TY] x [i0-1, i0+TX], inside rows/cols 2..m-3
+    const float invt = 1.0f / (float)TW;
+    for (int q = tid; q < TH * TW; q += NT) {
+        const int qj = small_div(q, invt);
+        const int j = j0 - 1 + qj, i = i0 - 1 + (q - qj * TW);
         if (j < 2 || j > mv - 3 || i < 2 || i > nv - 3) continue;
         const size_t p = off(j, i, nv);
         T v;
@@ -622,23 +685,29 @@ F2D_BATCH_ENTRY(SmoothFusedF1, BSmoothFusedF1)
 template <typename T>
 int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
                     const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s) {
-    dim3 b(FS_TX, FS_TY);
-    dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, b);
+    const dim3 b = level_tile(L.mv - 2 * NH, L.nv - 2 * NH, FS_TX, FS_TY);
+    const dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, b);
+    const size_t smem = smooth_fused_smem<T>(b);
     CoarseSrc<T> cs{nullptr, nullptr, 0};
     if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
     SmoothFusedArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, xmode, cs, out, active};
     if (an)
-        return launch_body<BSmoothFused<T, true>>(k_smooth_fused<T, true>, a, g, b, 0, s,
+        return launch_body<BSmoothFused<T, true>>(k_smooth_fused<T, true>, a, g, b, smem, s,
                                                   "mg_smooth_fused");
-    return launch_body<BSmoothFused<T, false>>(k_smooth_fused<T, false>, a, g, b, 0, s,
+    return launch_body<BSmoothFused<T, false>>(k_smooth_fused<T, false>, a, g, b, smem, s,
                                                "mg_smooth_fused");
 }
 
 // residual + full-weighting restriction: the fine residuals a coarse tile
 // needs (fine halo positions through their periodic images, as the
 // reference's halo fill of r makes them) are computed once into shared
-// memory, then restricted.
+// memory, then restricted.  The coarse tile is the CTA shape (level_tile()).
 constexpr int RR_TX = 16, RR_TY = 8;
+
+template <typename T>
+size_t resres_smem(dim3 b) {
+    return sizeof(T) * (size_t)(2 * b.y + 1) * (2 * b.x + 1);
+}
 
 template <typename T>
 struct ResresArgs {
@@ -653,19 +722,23 @@ struct ResresArgs {
 template <typename T, bool L0>
 F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
-    constexpr int RW = 2 * RR_TX + 1, RH = 2 * RR_TY + 1;
-    __shared__ T rs[RH * RW];
+    const int TX = (int)blockDim.x, TY = (int)blockDim.y;
+    const int RW = 2 * TX + 1, RH = 2 * TY + 1;
+    extern __shared__ __align__(16) unsigned char sm[];
+    T *rs = (T *)sm;
     const LevelView<T> F = A.F;
     const AnalyticT<T> an = A.an;
     const int8_t *msk2 = A.msk2;
     const int mv2 = A.mv2, nv2 = A.nv2;
     T *b2 = A.b2;
-    const int I2a = NH + vb.x * RR_TX, J2a = NH + vb.y * RR_TY;
+    const int I2a = NH + vb.x * TX, J2a = NH + vb.y * TY;
     const int jf0 = 2 * J2a - 3, if0 = 2 * I2a - 3;
-    const int tid = threadIdx.y * RR_TX + threadIdx.x;
+    const int tid = threadIdx.y * TX + threadIdx.x;
     const int mv = F.mv, nv = F.nv;
-    for (int q = tid; q < RH * RW; q += RR_TX * RR_TY) {
-        const int jf = jf0 + q / RW, iff = if0 + q % RW;
+    const float inv = 1.0f / (float)RW;
+    for (int q = tid; q < RH * RW; q += TX * TY) {
+        const int qj = small_div(q, inv);
+        const int jf = jf0 + qj, iff = if0 + (q - qj * RW);
         if (jf > mv - 3 || iff > nv - 3) continue;  // beyond the last coarse point's stencil
         rs[q] = residual<T, L0>(F, &an, F.x, F.b, wrap(jf, mv, NH), wrap(iff, nv, NH));
     }
@@ -706,11 +779,13 @@ F2D_BATCH_ENTRY(ResresF1, BResresF1)
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
               const int *active, cudaStream_t s) {
-    dim3 b(RR_TX, RR_TY);
-    dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, b);
+    const dim3 b = level_tile(C.mv - 2 * NH, C.nv - 2 * NH, RR_TX, RR_TY);
+    const dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, b);
+    const size_t smem = resres_smem<T>(b);
     ResresArgs<T> a{F, an ? *an : AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active};
-    if (an) return launch_body<BResres<T, true>>(k_resres<T, true>, a, g, b, 0, s, "mg_resres");
-    return launch_body<BResres<T, false>>(k_resres<T, false>, a, g, b, 0, s, "mg_resres");
+    if (an)
+        return launch_body<BResres<T, true>>(k_resres<T, true>, a, g, b, smem, s, "mg_resres");
+    return launch_body<BResres<T, false>>(k_resres<T, false>, a, g, b, smem, s, "mg_resres");
 }
 
 // ------------------------------------------------------------ coarse CTA
@@ -861,31 +936,33 @@ F2D_DEV void co_vcycle(unsigned char *sm, const CoLv *lv, int l1, int deep, bool
     }
 }
 
+// shared-memory layout of the levels (thread 0 writes the table)
 template <typename T>
-F2D_DEV void coarse_body(const CoarseArgs<T> &a, const VB) {
-    if (inactive(a.active)) return;
-    extern __shared__ __align__(16) unsigned char sm[];
-    __shared__ CoLv lv[MAX_LEVELS];
-    const int tid = threadIdx.y * CO_TX + threadIdx.x;
-    if (tid == 0) {
-        unsigned o = 0;
-        for (int l = 0; l < a.nlev; l++) {
-            const unsigned pts = (unsigned)(a.lev[l].mv * a.lev[l].nv);
-            CoLv d;
-            d.mv = a.lev[l].mv;
-            d.nv = a.lev[l].nv;
-            d.o_msk = o;
-            o += (unsigned)align16(pts);
-            d.o_A = o;
-            d.o_x = o + 6 * pts * sizeof(T);
-            d.o_b = o + 7 * pts * sizeof(T);
-            d.o_r = o + 8 * pts * sizeof(T);
-            d.o_t = o + 9 * pts * sizeof(T);
-            o += (unsigned)align16(sizeof(T) * pts * 10);
-            lv[l] = d;
-        }
+F2D_DEV void coarse_layout(const CoarseArgs<T> &a, CoLv *lv) {
+    unsigned o = 0;
+    for (int l = 0; l < a.nlev; l++) {
+        const unsigned pts = (unsigned)(a.lev[l].mv * a.lev[l].nv);
+        CoLv d;
+        d.mv = a.lev[l].mv;
+        d.nv = a.lev[l].nv;
+        d.o_msk = o;
+        o += (unsigned)align16(pts);
+        d.o_A = o;
+        d.o_x = o + 6 * pts * sizeof(T);
+        d.o_b = o + 7 * pts * sizeof(T);
+        d.o_r = o + 8 * pts * sizeof(T);
+        d.o_t = o + 9 * pts * sizeof(T);
+        o += (unsigned)align16(sizeof(T) * pts * 10);
+        lv[l] = d;
     }
-    __syncthreads();
+}
+
+// masks and operators of every level into shared memory; the first level's
+// b and x from the arrays (unit < 0), or b = the unit vector of interior
+// point `unit` (with its periodic images) and x = 0
+template <typename T>
+F2D_DEV void coarse_load(const CoarseArgs<T> &a, const CoLv *lv, unsigned char *sm, int unit) {
+    const int tid = threadIdx.y * CO_TX + threadIdx.x;
     for (int l = 0; l < a.nlev; l++) {
         const LevelView<T> &g = a.lev[l];
         const LevelView<T> s = co_view<T>(sm, lv[l]);
@@ -894,11 +971,23 @@ F2D_DEV void coarse_body(const CoarseArgs<T> &a, const VB) {
         for (int q = tid; q < 6 * pts; q += CO_THREADS) ((T *)s.A)[q] = g.A[q];
         if (l == 0)
             for (int q = tid; q < pts; q += CO_THREADS) {
-                s.b[q] = g.b[q];
-                s.x[q] = (a.mode == CYCLE_V && !a.zero_first) ? g.x[q] : (T)0;
+                s.b[q] = unit < 0 ? g.b[q] : (T)0;
+                s.x[q] = (unit < 0 && a.mode == CYCLE_V && !a.zero_first) ? g.x[q] : (T)0;
             }
     }
-    __syncthreads();
+    if (unit >= 0) {
+        __syncthreads();
+        if (tid == 0) {
+            const LevelView<T> s = co_view<T>(sm, lv[0]);
+            const int n2 = s.nv - 2 * NH;
+            store_images(s.b, NH + unit / n2, NH + unit % n2, s.mv, s.nv, (T)1);
+        }
+    }
+}
+
+// core/gmg/hierarchy.py:98-151 on the levels in shared memory
+template <typename T>
+F2D_DEV void coarse_cycle(const CoarseArgs<T> &a, const CoLv *lv, unsigned char *sm) {
     const int deep = a.nlev - 1;
     CoSched sc{false};
     if (a.mode == CYCLE_V) {
@@ -911,10 +1000,46 @@ F2D_DEV void coarse_body(const CoarseArgs<T> &a, const VB) {
             co_vcycle<T>(sm, lv, l, deep, false, a.c1, a.c2, a.ndeepest, sc);
         }
     }
+}
+
+template <typename T>
+F2D_DEV void coarse_body(const CoarseArgs<T> &a, const VB) {
+    if (inactive(a.active)) return;
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ CoLv lv[MAX_LEVELS];
+    const int tid = threadIdx.y * CO_TX + threadIdx.x;
+    if (tid == 0) coarse_layout(a, lv);
+    __syncthreads();
+    coarse_load(a, lv, sm, -1);
+    __syncthreads();
+    coarse_cycle(a, lv, sm);
     __syncthreads();
     const LevelView<T> s0 = co_view<T>(sm, lv[0]);
     const int pts0 = a.lev[0].mv * a.lev[0].nv;
     for (int q = tid; q < pts0; q += CO_THREADS) a.lev[0].x[q] = s0.x[q];
+}
+
+// The coarse part of a cycle started from x = 0 (a V-cycle with zero_first,
+// or the F-cycle) is a fixed linear map of the first level's right-hand
+// side.  CTA k runs it on the unit vector of interior point k and writes the
+// resulting interior values into column k of op (row-major, n x n).
+template <typename T>
+__global__ void __launch_bounds__(CO_THREADS) k_coarse_columns(CoarseArgs<T> a, T *op, int n) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __shared__ CoLv lv[MAX_LEVELS];
+    const int tid = threadIdx.y * CO_TX + threadIdx.x;
+    const int k = (int)blockIdx.x;
+    if (k >= n) return;
+    if (tid == 0) coarse_layout(a, lv);
+    __syncthreads();
+    coarse_load(a, lv, sm, k);
+    __syncthreads();
+    coarse_cycle(a, lv, sm);
+    __syncthreads();
+    const LevelView<T> s0 = co_view<T>(sm, lv[0]);
+    const int n2 = s0.nv - 2 * NH;
+    for (int i = tid; i < n; i += CO_THREADS)
+        op[(size_t)i * n + k] = s0.x[off(NH + i / n2, NH + i % n2, s0.nv)];
 }
 
 template <typename T>
@@ -969,6 +1094,91 @@ int mg_coarse(const CoarseArgs<T> &args, size_t smem, cudaStream_t s) {
     }
     return launch_body<BCoarse<T>>(k_coarse<T>, args, dim3(1), dim3(CO_TX, CO_TY), smem, s,
                                    "mg_coarse");
+}
+
+// The coarse part applied as its linear map: x(interior i) = sum_k op[i][k]
+// b(interior k), written with its periodic images (every halo point of the
+// first level is the image of an interior point, as the cycle leaves it).
+// One warp per interior point; the first level's interior b is staged in
+// shared memory.  The same function as the cycle on the levels, summed in a
+// different order: used by the product build only.
+constexpr int CA_WARPS = 8;
+
+template <typename T>
+struct CoarseApplyArgs {
+    const T *op;
+    int n, n2, mv, nv;
+    const T *b;
+    T *x;
+    const int *active;
+};
+
+template <typename T>
+F2D_DEV void coarse_apply_body(const CoarseApplyArgs<T> &a, const VB vb) {
+    if (inactive(a.active)) return;
+    extern __shared__ __align__(16) unsigned char sm[];
+    T *bs = (T *)sm;
+    const int tid = (int)threadIdx.x, n = a.n, n2 = a.n2;
+    for (int k = tid; k < n; k += CA_WARPS * 32) {
+        const int qj = k / n2;
+        bs[k] = a.b[off(NH + qj, NH + (k - qj * n2), a.nv)];
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    const int i = vb.x * CA_WARPS + warp;
+    if (i >= n) return;
+    const T *row = a.op + (size_t)i * n;
+    T s0 = (T)0, s1 = (T)0;
+    int k = lane;
+    for (; k + 32 < n; k += 64) {
+        s0 = fma(row[k], bs[k], s0);
+        s1 = fma(row[k + 32], bs[k + 32], s1);
+    }
+    if (k < n) s0 = fma(row[k], bs[k], s0);
+    T v = s0 + s1;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+        const int qj = i / n2;
+        store_images(a.x, NH + qj, NH + (i - qj * n2), a.mv, a.nv, v);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CA_WARPS * 32) k_coarse_apply(CoarseApplyArgs<T> a) {
+    pdl_prologue();
+    coarse_apply_body<T>(a, F2D_VB_NATIVE);
+}
+
+template <typename T>
+struct BCoarseApply {
+    using Args = CoarseApplyArgs<T>;
+    static constexpr int THREADS = CA_WARPS * 32;
+    static constexpr int KIND = sizeof(T) == 8 ? BK_CoarseApplyD : BK_CoarseApplyF;
+    F2D_DEV static void run(const Args &a, VB vb) { coarse_apply_body<T>(a, vb); }
+};
+using BCoarseApplyD = BCoarseApply<double>;
+using BCoarseApplyF = BCoarseApply<float>;
+F2D_BATCH_ENTRY(CoarseApplyD, BCoarseApplyD)
+F2D_BATCH_ENTRY(CoarseApplyF, BCoarseApplyF)
+
+template <typename T>
+int mg_coarse_columns(const CoarseArgs<T> &args, size_t smem, T *op, int n, cudaStream_t s) {
+    int st = cuda_status(cudaFuncSetAttribute(k_coarse_columns<T>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              COARSE_SMEM_MAX),
+                         "coarse columns smem attribute");
+    if (st) return st;
+    k_coarse_columns<T><<<n, dim3(CO_TX, CO_TY), smem, s>>>(args, op, n);
+    return launch_status("mg_coarse_columns");
+}
+
+template <typename T>
+int mg_coarse_apply(const T *op, int n, const LevelView<T> &L, const int *active,
+                    cudaStream_t s) {
+    CoarseApplyArgs<T> a{op, n, L.nv - 2 * NH, L.mv, L.nv, L.b, L.x, active};
+    const dim3 g((unsigned)((n + CA_WARPS - 1) / CA_WARPS)), b(CA_WARPS * 32);
+    return launch_body<BCoarseApply<T>>(k_coarse_apply<T>, a, g, b, sizeof(T) * (size_t)n, s,
+                                        "mg_coarse_apply");
 }
 
 // ------------------------------------------------------------ stage kernels
@@ -1194,6 +1404,9 @@ int vec_axpy_const(double *x, double area, const double *sum, size_t count, cuda
     template int mg_interp<T>(const LevelView<T> &, const T *, const LevelView<T> &, T *, bool,  \
                               const int *, cudaStream_t);                                        \
     template int mg_coarse<T>(const CoarseArgs<T> &, size_t, cudaStream_t);                     \
+    template int mg_coarse_columns<T>(const CoarseArgs<T> &, size_t, T *, int, cudaStream_t);    \
+    template int mg_coarse_apply<T>(const T *, int, const LevelView<T> &, const int *,           \
+                                    cudaStream_t);                                               \
     template int mg_smooth_fused<T>(const LevelView<T> &, const AnalyticT<T> *, T, T, int,       \
                                     const LevelView<T> *, T *, const int *, cudaStream_t);       \
     template int mg_resres<T>(const LevelView<T> &, const AnalyticT<T> *, const LevelView<T> &,  \
@@ -1311,3 +1524,16 @@ int mg_zero(double *x, size_t n, const int *active, cudaStream_t s) {
 }
 
 }  // namespace f2d
+
+extern "C" {
+
+// the CTA count the multigrid level kernels aim at when they choose their
+// tile: -1 twice the SM count, 0 always the largest tile (the default), > 0
+// that count, < -1 only queries; returns the previous setting.
+int f2d_set_level_tiles(int target) {
+    const int prev = f2d::level_tile_target();
+    if (target >= -1) f2d::level_tile_target() = target;
+    return prev;
+}
+
+}  // extern "C"

@@ -264,6 +264,14 @@ class Model(object):
         self.coarse_level = cur.value
         return cur.value, first.value, nlev.value
 
+    def coarse_operator(self, enable=None):
+        """Query (enable=None) or switch the coarse part of the multigrid as a
+        precomputed linear map (product build); returns its size (0: none)."""
+        n = ctypes.c_int()
+        self._call("f2d_model_coarse_op", self.h, -1 if enable is None else int(bool(enable)),
+                   ctypes.byref(n))
+        return n.value
+
     def set_islands(self, rhsp, psi):
         """Islands with a prescribed streamfunction: the rhsp and psi arrays of
         core/island.py (``fluid2d_gb300.island.Island.finalize``)."""

@@ -269,11 +269,27 @@ int f2d_model_noslip(void *model, const int8_t *msknoslip_host, void *stream);
  * launch structure (and speed) changes.  level < 0 only queries. */
 int f2d_model_coarse_level(void *model, int level, int *current, int *first, int *nlev);
 
+/* The coarse part of the multigrid cycles that start from x = 0 (every
+ * V-cycle below the coarse level, and the F-cycle) applied as its dense
+ * linear map of the coarse level's right-hand side, built by running the
+ * cycle on unit vectors (at most 1024 interior points; product build only:
+ * the exact build keeps the reference's order of operations).  enable: 1 on
+ * (default), 0 off, < 0 query; *n receives the operator's size (0: none). */
+int f2d_model_coarse_op(void *model, int enable, int *n);
+
 /* Programmatic dependent launch of the engine kernels (each kernel may be
  * scheduled while its predecessor runs and waits for it before touching
  * memory): 1 on, 0 off (default), < 0 query; returns the previous setting.
  * Graphs captured before a change keep their launches. */
 int f2d_set_pdl(int enable);
+
+/* The CTA count the multigrid level kernels (fused smoothing, residual +
+ * restriction) aim at when they choose their tile: the largest tile is
+ * halved, down to one warp, while the level's grid has fewer CTAs.  -1 twice
+ * the SM count, 0 always the largest tile (default), > 0 that count, < -1
+ * only queries; returns the previous setting.  Results do not depend on it;
+ * graphs captured before a change keep their tiles. */
+int f2d_set_level_tiles(int target);
 
 /* ---- batched steps: one step of each of n models (Euler or Boussinesq, float64
  * or mixed, without no-slip walls, islands or line relaxation) recorded and

@@ -204,3 +204,36 @@ def test_coarse_level_changes_nothing_but_launches(eng, precision):
     M.diagnostics()
     best, times = tune_coarse_level(M, steps=2, warmup=1, use_cache=False)
     assert best in times and M.coarse_switch()[0] == best
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["euler-perio-turb", "euler-closed-dipole", "boussinesq-xchannel"])
+def test_coarse_operator_matches_the_cycle(eng, name, precision):
+    """The product build applies the coarse part of the cycles started from
+    x = 0 as its precomputed linear map: the same function summed in another
+    order, so states agree with the cycle-by-cycle path to rounding, at every
+    switch level.  The exact build never builds it."""
+    import torch
+    wl = _workloads()[name]
+    X = eng.from_workload(wl, variant="exact", precision=precision, dt=1e-3)
+    assert X.coarse_operator() == 0
+    probe = eng.from_workload(wl, precision=precision, dt=1e-3)
+    cur, first, nlev = probe.coarse_switch()
+    for level in sorted({first, nlev - 1}):
+        states = []
+        for on in (True, False):
+            M = eng.from_workload(wl, precision=precision, dt=1e-3)
+            M.coarse_switch(level)
+            n = M.coarse_operator(on)
+            if on:
+                lv = M.coarse_switch()[0]
+                assert n > 0 or lv >= nlev
+            else:
+                assert n == 0
+            M.set_psi_from_vorticity()
+            M.diagnostics()
+            M.run(4)
+            torch.cuda.synchronize()
+            states.append(M.var.state.cpu().numpy())
+        for k in range(states[0].shape[0]):
+            assert relerr(states[0][k], states[1][k]) <= 1e-11, (level, k)

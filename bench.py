@@ -408,6 +408,14 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
             "solve_residual_last_step": res}
 
 
+def _structure(choice):
+    off, groups, policy = choice
+    lev = "coarse switch first+%d" % off
+    if groups == 0:
+        return "streams, " + lev
+    return "batched groups=%d policy=%d, %s" % (groups, policy, lev)
+
+
 def bench_ensemble(a):
     """Config: 96 independent Euler instances (sides log-uniform 64-768,
     multiples of 64, islands, 3-12 vortices; seed 4).  Batched = the launch
@@ -435,10 +443,8 @@ def bench_ensemble(a):
         ms = e0.elapsed_time(e1)
         out[prec + "_batched"] = {"cell_steps_per_s": cells * a.ensemble_steps / (ms * 1e-3),
                                   "ms_per_ensemble_step": ms / a.ensemble_steps,
-                                  "launch_structure": ("streams" if choice[0] == 0 else
-                                                       "batched groups=%d policy=%d" % choice),
-                                  "tuning_ms_per_step": {("streams" if k[0] == 0 else
-                                                          "groups=%d policy=%d" % k): round(v, 3)
+                                  "launch_structure": _structure(choice),
+                                  "tuning_ms_per_step": {_structure(k): round(v, 3)
                                                          for k, v in times.items()}}
         E.free_batch()
         del E

@@ -1,14 +1,16 @@
 """Autotuning of the launch structure by timing it on the device.
 
-* ``tune_coarse_level(model)``: the level from which the multigrid runs in
-  one CTA out of shared memory.  A finer switch level moves more work onto
-  one SM (FP64-bound there), a coarser one adds small latency-bound
-  launches; the best split depends on the grid and the precision, so every
-  allowed level is timed on the model's captured step.  Results do not
-  depend on the choice (same arithmetic either way).
-* ``tune_ensemble(ens)``: the number of batched groups and the merge policy
-  of an Ensemble's batched launches, against the per-instance stream
-  replay.
+* ``tune_coarse_level(model)``: the level from which the multigrid's coarse
+  part runs as one unit: the shared-memory CTA of the cycle (exact build), or
+  its precomputed linear map (product build, at most 1024 points).  A finer
+  switch level means a longer one-SM chain or a larger operator, a coarser
+  one adds small latency-bound launches; the best split depends on the grid
+  and the precision, so every allowed level is timed on the model's
+  captured step.  Results do not depend on the choice beyond rounding.
+* ``tune_ensemble(ens)``: the instances' coarse-switch offset (their
+  operators' total size against the L2 cache), the number of batched groups
+  and the merge policy of an Ensemble's batched launches, against the
+  per-instance stream replay.
 
 Timings use CUDA events on the launching stream after warm-up steps; the
 model's state advances while it is tuned, so tune on a copy when the
@@ -54,20 +56,25 @@ def tune_coarse_level(model, steps=5, warmup=2, use_cache=True):
     return best, times
 
 
-def tune_ensemble(ens, candidates=((1, 1), (2, 1), (4, 1), (8, 1), (16, 1), (16, 0)), steps=5,
-                  warmup=2):
-    """Pick the batched grouping and merge policy (or the stream replay,
-    (0, None)) with the shortest ensemble step; returns (choice, {choice: ms})."""
+def tune_ensemble(ens, candidates=((1, 1), (2, 1), (4, 1), (8, 1), (16, 1), (16, 0)),
+                  offsets=(0, 1), steps=5, warmup=2):
+    """Pick the coarse-switch offset of the instances (Ensemble.coarse_offset:
+    the sum of the instances' coarse operators against the L2 cache) and the
+    batched grouping and merge policy (groups 0: every instance's own graph
+    replayed on streams) with the shortest ensemble step; returns
+    ((offset, groups, policy), {choice: ms})."""
     times = {}
-    ens.free_batch()
-    ens.capture()
-    times[(0, None)] = _time(ens.run, steps, warmup)
-    for groups, policy in candidates:
-        ens.build_batch(groups, policy)
-        times[(groups, policy)] = _time(ens.run, steps, warmup)
-    best = min(times, key=times.get)
-    if best == (0, None):
+    for off in offsets:
         ens.free_batch()
-    else:
-        ens.build_batch(*best)
+        ens.coarse_offset(off)
+        ens.capture()
+        times[(off, 0, None)] = _time(ens.run, steps, warmup)
+        for groups, policy in candidates:
+            ens.build_batch(groups, policy)
+            times[(off, groups, policy)] = _time(ens.run, steps, warmup)
+    best = min(times, key=times.get)
+    ens.free_batch()
+    ens.coarse_offset(best[0])
+    if best[1] != 0:
+        ens.build_batch(best[1], best[2])
     return best, times

@@ -476,6 +476,7 @@ class Ensemble(object):
         (f2d_batch_create), captured as one graph per group, and the groups'
         graphs run on their own streams."""
         self.free_batch()
+        self._batch_args = (groups, policy)
         L = self.models[0].L
         order = sorted(range(len(self.models)), key=lambda k: self.models[k].cells)
         groups = max(1, min(int(groups), len(order)))
@@ -488,6 +489,19 @@ class Ensemble(object):
                       variant=self.models[0].variant)
             self.batch.append(h)
         self._L = L
+
+    def coarse_offset(self, d):
+        """Put every instance's coarse switch at its first allowed level + d
+        (clamped to the number of levels): each step larger means a quarter of
+        the coarse operator's points (and a sixteenth of its bytes) per
+        instance.  A built batch is rebuilt."""
+        args = getattr(self, "_batch_args", None) if self.batch is not None else None
+        self.free_batch()
+        for m in self.models:
+            cur, first, nlev = m.coarse_switch()
+            m.coarse_switch(min(first + int(d), nlev))
+        if args is not None:
+            self.build_batch(*args)
 
     def batch_info(self):
         """(launches per step, operations recorded) summed over the groups"""

@@ -239,6 +239,7 @@ EXTRA = {
     "f2d_version": ([], _I),
     "f2d_set_pdl": ([_I], _I),
     "f2d_set_level_tiles": ([_I], _I),
+    "f2d_set_level_threads": ([_I], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),
 }

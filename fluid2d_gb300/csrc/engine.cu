@@ -899,7 +899,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a) {
 
 struct BDiagP {
     using Args = DiagArgs;
-    static constexpr int THREADS = RED_THREADS, KIND = BK_DiagP;
+    static constexpr int THREADS = RED_THREADS, KIND = BK_DiagP, MIN_BLOCKS = 4;
     F2D_DEV static void run(const Args &a, VB vb) { diag_partial_body(a, vb); }
 };
 struct BDiagF {

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <type_traits>
+
 #include "f2d_common.cuh"
 
 namespace f2d {
@@ -74,8 +76,19 @@ F2D_DEV int batch_instance(const BatchGrid &g, int b) {
     return lo;
 }
 
+// a Body may ask for a minimum of resident CTAs per SM (MIN_BLOCKS), which
+// caps its registers as in its native kernel
+template <class B, class = void>
+struct body_min_blocks {
+    static constexpr int value = 1;
+};
+template <class B>
+struct body_min_blocks<B, std::void_t<decltype(B::MIN_BLOCKS)>> {
+    static constexpr int value = B::MIN_BLOCKS;
+};
+
 template <class Body>
-__global__ void __launch_bounds__(Body::THREADS)
+__global__ void __launch_bounds__(Body::THREADS, body_min_blocks<Body>::value)
     k_batch(const typename Body::Args *args, BatchGrid g) {
     pdl_prologue();
     const int i = batch_instance(g, (int)blockIdx.x);

@@ -47,8 +47,14 @@ k_advection(const int8_t *__restrict__ msk, const double *__restrict__ x,
         size_t p = off(J, I, n);
         sfx[ty][tx + 1] = edge_flux<KIND>(msk, x, u, p, 1, method, order, c);
         sfy[ty + 1][tx] = edge_flux<KIND>(msk, x, v, p, n, method, order, c);
-        if (tx == 0) sfx[ty][0] = edge_flux<KIND>(msk, x, u, p - 1, 1, method, order, c);
         if (ty == 0) sfy[0][tx] = edge_flux<KIND>(msk, x, v, p - n, n, method, order, c);
+    }
+    // the tile's west faces: lanes 0..ADV_TY-1 of warp 1, one row each (a warp
+    // issues a float64 instruction for all its lanes)
+    if (ty == 1 && tx < ADV_TY) {
+        const int Jr = nh + blockIdx.y * ADV_TY + tx, I0 = nh + blockIdx.x * ADV_TX;
+        if (I0 <= n - nh - 1 && Jr <= m - nh - 1)
+            sfx[tx][0] = edge_flux<KIND>(msk, x, u, off(Jr, I0, n) - 1, 1, method, order, c);
     }
     __syncthreads();
     if (!in) return;

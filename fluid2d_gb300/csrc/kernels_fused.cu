@@ -99,6 +99,9 @@ F2D_DEV T diag_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i)
 
 template <typename T, bool L0>
 F2D_DEV T c3_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T c1) {
+    if (L0 && L.nb) {  // the diagonal's bit decides a5 != 0 without a float64 compare
+        return (L.nb[off(j, i, L.nv)] & 256u) ? an->c3 : c1 / fabs((T)0);
+    }
     if (L0) {
         const T a5 = diag_coef<T, L0>(L, an, j, i);
         return a5 != (T)0 ? an->c3 : c1 / fabs(a5);
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(LV_TX *LV_TY) k_residual_mixed(ResidualArgs<do
 
 struct BResidualMixed {
     using Args = ResidualArgs<double>;
-    static constexpr int THREADS = LV_TX * LV_TY, KIND = BK_ResidualMixed;
+    static constexpr int THREADS = LV_TX * LV_TY, KIND = BK_ResidualMixed, MIN_BLOCKS = 6;
     F2D_DEV static void run(const Args &a, VB vb) { residual_mixed_body(a, vb); }
 };
 F2D_BATCH_ENTRY(ResidualMixed, BResidualMixed)
@@ -440,6 +443,7 @@ template <typename T, bool L0>
 struct BSweep1 {
     using Args = SweepArgs<T>;
     static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int MIN_BLOCKS = 5;  // near the native kernel's occupancy
     static constexpr int KIND = (sizeof(T) == 8 && L0) ? BK_Sweep1D1 : -1;
     F2D_DEV static void run(const Args &a, VB vb) { sweep1_body<T, L0>(a, vb); }
 };
@@ -447,6 +451,7 @@ template <typename T, bool L0>
 struct BSweep2 {
     using Args = SweepArgs<T>;
     static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int MIN_BLOCKS = 5;
     static constexpr int KIND = (sizeof(T) == 8 && L0) ? BK_Sweep2D1 : -1;
     F2D_DEV static void run(const Args &a, VB vb) { sweep2_body<T, L0>(a, vb); }
 };
@@ -454,6 +459,7 @@ template <typename T, bool L0>
 struct BResidual {
     using Args = ResidualArgs<T>;
     static constexpr int THREADS = LV_TX * LV_TY;
+    static constexpr int MIN_BLOCKS = 5;
     static constexpr int KIND = (sizeof(T) == 8 && L0) ? BK_ResidualD1 : -1;
     F2D_DEV static void run(const Args &a, VB vb) { residual_body<T, L0>(a, vb); }
 };
@@ -546,6 +552,31 @@ constexpr int FS_TX = 32, FS_TY = 16;
 // below the 0.5/d margin to the next integer, so the floor is exact.
 F2D_DEV int small_div(int q, float inv) { return (int)(((float)q + 0.5f) * inv); }
 
+// CTA threads: one per tile point (the input ring and the first sweep's ring
+// take a second pass), or one per input point so that every phase is a
+// single pass (level_one_pass()).
+constexpr int FS_THREADS_MAX = ((FS_TX + 4) * (FS_TY + 4) + 31) / 32 * 32;
+// two resident CTAs of the largest shape per SM: at most 44 registers, so a
+// 512-thread CTA keeps the occupancy (two to three per SM) of a kernel bounded
+// for 512 threads alone
+constexpr int FS_MIN_BLOCKS = 2;
+
+// 0 (default): one thread per tile point; 1: one per input point when the
+// grid has fewer than two CTAs per SM; 2: always one per input point.  On the
+// 1024^2 steps and the 96-instance ensemble 1 and 2 measured equal or slower
+// than 0 (the small levels' time is not in the second passes).
+int &level_one_pass() {
+    static int m = 0;
+    return m;
+}
+
+static inline unsigned smooth_fused_threads(dim3 tile, dim3 grid) {
+    const int m = level_one_pass();
+    const bool one = m == 2 || (m == 1 && (long long)grid.x * grid.y < 2LL * sm_count());
+    if (!one) return tile.x * tile.y;
+    return ((tile.x + 4) * (tile.y + 4) + 31) / 32 * 32;
+}
+
 template <typename T>
 size_t smooth_fused_smem(dim3 b) {
     return sizeof(T) * ((size_t)(b.y + 4) * (b.x + 4) + (size_t)(b.y + 2) * (b.x + 2));
@@ -568,12 +599,13 @@ struct SmoothFusedArgs {
     CoarseSrc<T> cs;
     T *out;
     const int *active;
+    int tx, ty;  // the tile
 };
 
 template <typename T, bool L0>
 F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
-    const int TX = (int)blockDim.x, TY = (int)blockDim.y, NT = TX * TY;
+    const int TX = A.tx, TY = A.ty, NT = (int)blockDim.x;
     const int XW = TX + 4, XH = TY + 4, TW = TX + 2, TH = TY + 2;
     extern __shared__ __align__(16) unsigned char sm[];
     T *xs = (T *)sm;
@@ -586,7 +618,7 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     T *out = A.out;
     const int mv = L.mv, nv = L.nv;
     const int i0 = NH + vb.x * TX, j0 = NH + vb.y * TY;
-    const int tid = threadIdx.y * TX + threadIdx.x;
+    const int tid = (int)threadIdx.x;
     // input x on [j0-2, j0+TY+1] x [i0-2, i0+TX+1], inside rows/cols 1..m-2
     if (xmode != X_ZERO) {
         const float inv = 1.0f / (float)XW;
@@ -639,30 +671,34 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     }
     __syncthreads();
     // second sweep on the tile's interior points
-    const int j = j0 + threadIdx.y, i = i0 + threadIdx.x;
-    if (j > mv - NH - 1 || i > nv - NH - 1) return;
-    const size_t p = off(j, i, nv);
-    T v = (T)0;
-    if (L.msk[p] != 0) {
-        const T c3 = c3_coef<T, L0>(L, &an, j, i, c1);
-        T a[8];
-        offdiag<T, L0>(L, &an, j, i, a);
-        const T *t = ts + (j - (j0 - 1)) * TW + (i - (i0 - 1));
-        v = t[0] * c2 + c3 * (+a[0] * t[-TW - 1]
-                              + a[1] * t[-TW]
-                              + a[2] * t[-TW + 1]
-                              + a[3] * t[-1]
-                              + a[4] * t[1]
-                              + a[5] * t[TW - 1]
-                              + a[6] * t[TW]
-                              + a[7] * t[TW + 1]
-                              - L.b[p]);
+    const float invx = 1.0f / (float)TX;
+    for (int q = tid; q < TX * TY; q += NT) {
+        const int qj = small_div(q, invx);
+        const int j = j0 + qj, i = i0 + (q - qj * TX);
+        if (j > mv - NH - 1 || i > nv - NH - 1) continue;
+        const size_t p = off(j, i, nv);
+        T v = (T)0;
+        if (L.msk[p] != 0) {
+            const T c3 = c3_coef<T, L0>(L, &an, j, i, c1);
+            T a[8];
+            offdiag<T, L0>(L, &an, j, i, a);
+            const T *t = ts + (j - (j0 - 1)) * TW + (i - (i0 - 1));
+            v = t[0] * c2 + c3 * (+a[0] * t[-TW - 1]
+                                  + a[1] * t[-TW]
+                                  + a[2] * t[-TW + 1]
+                                  + a[3] * t[-1]
+                                  + a[4] * t[1]
+                                  + a[5] * t[TW - 1]
+                                  + a[6] * t[TW]
+                                  + a[7] * t[TW + 1]
+                                  - L.b[p]);
+        }
+        store_images(out, j, i, mv, nv, v);
     }
-    store_images(out, j, i, mv, nv, v);
 }
 
 template <typename T, bool L0>
-__global__ void __launch_bounds__(FS_TX *FS_TY) k_smooth_fused(SmoothFusedArgs<T> a) {
+__global__ void __launch_bounds__(FS_THREADS_MAX, FS_MIN_BLOCKS) k_smooth_fused(SmoothFusedArgs<T> a) {
     pdl_prologue();
     smooth_fused_body<T, L0>(a, F2D_VB_NATIVE);
 }
@@ -670,7 +706,8 @@ __global__ void __launch_bounds__(FS_TX *FS_TY) k_smooth_fused(SmoothFusedArgs<T
 template <typename T, bool L0>
 struct BSmoothFused {
     using Args = SmoothFusedArgs<T>;
-    static constexpr int THREADS = FS_TX * FS_TY;
+    static constexpr int THREADS = FS_THREADS_MAX;
+    static constexpr int MIN_BLOCKS = FS_MIN_BLOCKS;
     static constexpr int KIND = sizeof(T) == 8 ? (L0 ? -1 : BK_SmoothFusedD0)
                                                : (L0 ? BK_SmoothFusedF1 : BK_SmoothFusedF0);
     F2D_DEV static void run(const Args &a, VB vb) { smooth_fused_body<T, L0>(a, vb); }
@@ -685,12 +722,14 @@ F2D_BATCH_ENTRY(SmoothFusedF1, BSmoothFusedF1)
 template <typename T>
 int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
                     const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s) {
-    const dim3 b = level_tile(L.mv - 2 * NH, L.nv - 2 * NH, FS_TX, FS_TY);
-    const dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, b);
-    const size_t smem = smooth_fused_smem<T>(b);
+    const dim3 tile = level_tile(L.mv - 2 * NH, L.nv - 2 * NH, FS_TX, FS_TY);
+    const dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, tile);
+    const dim3 b(smooth_fused_threads(tile, g));
+    const size_t smem = smooth_fused_smem<T>(tile);
     CoarseSrc<T> cs{nullptr, nullptr, 0};
     if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
-    SmoothFusedArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, xmode, cs, out, active};
+    SmoothFusedArgs<T> a{L,   an ? *an : AnalyticT<T>{}, c1, c2, xmode, cs, out, active,
+                         (int)tile.x, (int)tile.y};
     if (an)
         return launch_body<BSmoothFused<T, true>>(k_smooth_fused<T, true>, a, g, b, smem, s,
                                                   "mg_smooth_fused");
@@ -701,12 +740,21 @@ int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, i
 // residual + full-weighting restriction: the fine residuals a coarse tile
 // needs (fine halo positions through their periodic images, as the
 // reference's halo fill of r makes them) are computed once into shared
-// memory, then restricted.  The coarse tile is the CTA shape (level_tile()).
+// memory, then restricted.  The CTA has one thread per fine residual of its
+// region ((2ty+1) x (2tx+1) for a coarse tile tx x ty, rounded up to whole
+// warps): each thread waits for its loads once, and its float64 chain is one
+// residual plus at most one restriction.
 constexpr int RR_TX = 16, RR_TY = 8;
+constexpr int RR_THREADS = ((2 * RR_TX + 1) * (2 * RR_TY + 1) + 31) / 32 * 32;
+constexpr int RR_MIN_BLOCKS = 2;  // at most 56 registers: two CTAs of 576 per SM
+
+static inline unsigned resres_threads(dim3 tile) {
+    return ((2 * tile.x + 1) * (2 * tile.y + 1) + 31) / 32 * 32;
+}
 
 template <typename T>
-size_t resres_smem(dim3 b) {
-    return sizeof(T) * (size_t)(2 * b.y + 1) * (2 * b.x + 1);
+size_t resres_smem(dim3 tile) {
+    return sizeof(T) * (size_t)(2 * tile.y + 1) * (2 * tile.x + 1);
 }
 
 template <typename T>
@@ -717,12 +765,13 @@ struct ResresArgs {
     int mv2, nv2;
     T *b2;
     const int *active;
+    int tx, ty;  // the coarse tile
 };
 
 template <typename T, bool L0>
 F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
-    const int TX = (int)blockDim.x, TY = (int)blockDim.y;
+    const int TX = A.tx, TY = A.ty, NT = (int)blockDim.x;
     const int RW = 2 * TX + 1, RH = 2 * TY + 1;
     extern __shared__ __align__(16) unsigned char sm[];
     T *rs = (T *)sm;
@@ -733,30 +782,34 @@ F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
     T *b2 = A.b2;
     const int I2a = NH + vb.x * TX, J2a = NH + vb.y * TY;
     const int jf0 = 2 * J2a - 3, if0 = 2 * I2a - 3;
-    const int tid = threadIdx.y * TX + threadIdx.x;
+    const int tid = (int)threadIdx.x;
     const int mv = F.mv, nv = F.nv;
     const float inv = 1.0f / (float)RW;
-    for (int q = tid; q < RH * RW; q += TX * TY) {
+    for (int q = tid; q < RH * RW; q += NT) {
         const int qj = small_div(q, inv);
         const int jf = jf0 + qj, iff = if0 + (q - qj * RW);
         if (jf > mv - 3 || iff > nv - 3) continue;  // beyond the last coarse point's stencil
         rs[q] = residual<T, L0>(F, &an, F.x, F.b, wrap(jf, mv, NH), wrap(iff, nv, NH));
     }
     __syncthreads();
-    const int J2 = J2a + threadIdx.y, I2 = I2a + threadIdx.x;
-    if (J2 > mv2 - NH - 1 || I2 > nv2 - NH - 1) return;
-    T v = (T)0;
-    if (msk2[off(J2, I2, nv2)] != 0) {
-        const T *r = rs + (2 * J2 - 2 - jf0) * RW + (2 * I2 - 2 - if0);
-        v = (T)0.25 * r[0]
-            + (T)0.125 * (r[-1] + r[1] + r[-RW] + r[RW])
-            + (T)0.0625 * (r[-RW - 1] + r[-RW + 1] + r[RW - 1] + r[RW + 1]);
+    const float invt = 1.0f / (float)TX;
+    for (int c = tid; c < TX * TY; c += NT) {
+        const int cj = small_div(c, invt);
+        const int J2 = J2a + cj, I2 = I2a + (c - cj * TX);
+        if (J2 > mv2 - NH - 1 || I2 > nv2 - NH - 1) continue;
+        T v = (T)0;
+        if (msk2[off(J2, I2, nv2)] != 0) {
+            const T *r = rs + (2 * J2 - 2 - jf0) * RW + (2 * I2 - 2 - if0);
+            v = (T)0.25 * r[0]
+                + (T)0.125 * (r[-1] + r[1] + r[-RW] + r[RW])
+                + (T)0.0625 * (r[-RW - 1] + r[-RW + 1] + r[RW - 1] + r[RW + 1]);
+        }
+        store_images(b2, J2, I2, mv2, nv2, v);
     }
-    store_images(b2, J2, I2, mv2, nv2, v);
 }
 
 template <typename T, bool L0>
-__global__ void __launch_bounds__(RR_TX *RR_TY) k_resres(ResresArgs<T> a) {
+__global__ void __launch_bounds__(RR_THREADS, RR_MIN_BLOCKS) k_resres(ResresArgs<T> a) {
     pdl_prologue();
     resres_body<T, L0>(a, F2D_VB_NATIVE);
 }
@@ -764,7 +817,8 @@ __global__ void __launch_bounds__(RR_TX *RR_TY) k_resres(ResresArgs<T> a) {
 template <typename T, bool L0>
 struct BResres {
     using Args = ResresArgs<T>;
-    static constexpr int THREADS = RR_TX * RR_TY;
+    static constexpr int THREADS = RR_THREADS;
+    static constexpr int MIN_BLOCKS = RR_MIN_BLOCKS;
     static constexpr int KIND = sizeof(T) == 8 ? (L0 ? -1 : BK_ResresD0)
                                                : (L0 ? BK_ResresF1 : BK_ResresF0);
     F2D_DEV static void run(const Args &a, VB vb) { resres_body<T, L0>(a, vb); }
@@ -779,10 +833,12 @@ F2D_BATCH_ENTRY(ResresF1, BResresF1)
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
               const int *active, cudaStream_t s) {
-    const dim3 b = level_tile(C.mv - 2 * NH, C.nv - 2 * NH, RR_TX, RR_TY);
-    const dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, b);
-    const size_t smem = resres_smem<T>(b);
-    ResresArgs<T> a{F, an ? *an : AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active};
+    const dim3 tile = level_tile(C.mv - 2 * NH, C.nv - 2 * NH, RR_TX, RR_TY);
+    const dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, tile);
+    const dim3 b(resres_threads(tile));
+    const size_t smem = resres_smem<T>(tile);
+    ResresArgs<T> a{F,  an ? *an : AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active,
+                    (int)tile.x, (int)tile.y};
     if (an)
         return launch_body<BResres<T, true>>(k_resres<T, true>, a, g, b, smem, s, "mg_resres");
     return launch_body<BResres<T, false>>(k_resres<T, false>, a, g, b, smem, s, "mg_resres");
@@ -1207,10 +1263,18 @@ F2D_DEV void stage_adv_body(const AdvStage &a, const VB vb) {
         const size_t p = off(J, I, nv);
         sfx[ty][tx + 1] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.u, p, 1, a.method, a.order, c);
         sfy[ty + 1][tx] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.v, p, nv, a.method, a.order, c);
-        if (tx == 0)
-            sfx[ty][0] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.u, p - 1, 1, a.method, a.order, c);
+        // the tile's south faces: warp 0, one face per lane
         if (ty == 0)
             sfy[0][tx] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.v, p - nv, nv, a.method, a.order, c);
+    }
+    // the tile's west faces: lanes 0-7 of warp 1, one row each (a warp
+    // issues a float64 instruction for all its lanes, so one warp per ring
+    // instead of lane 0 of every row's warp)
+    if (ty == 1 && tx < 8) {
+        const int Jr = NH + vb.y * 8 + tx, I0 = NH + vb.x * 32;
+        if (I0 <= nv - NH - 1 && Jr <= mv - NH - 1)
+            sfx[tx][0] = edge_flux_rt_t<TC>(a.kind, a.msk, a.q, a.u, off(Jr, I0, nv) - 1, 1,
+                                            a.method, a.order, c);
     }
     __syncthreads();
     if (!in) return;
@@ -1261,6 +1325,7 @@ template <typename TC>
 struct BStageAdv {
     using Args = AdvStage;
     static constexpr int THREADS = 256;
+    static constexpr int MIN_BLOCKS = 4;
     static constexpr int KIND = sizeof(TC) == 8 ? BK_StageAdv64 : -1;
     F2D_DEV static void run(const Args &a, VB vb) { stage_adv_body<TC>(a, vb); }
 };
@@ -1317,7 +1382,7 @@ __global__ void __launch_bounds__(256) k_stage_ortho(OrthoStage a) {
 
 struct BStageOrtho {
     using Args = OrthoStage;
-    static constexpr int THREADS = 256, KIND = BK_StageOrtho;
+    static constexpr int THREADS = 256, KIND = BK_StageOrtho, MIN_BLOCKS = 6;
     F2D_DEV static void run(const Args &a, VB vb) { stage_ortho_body(a, vb); }
 };
 F2D_BATCH_ENTRY(StageOrtho, BStageOrtho)
@@ -1533,6 +1598,15 @@ extern "C" {
 int f2d_set_level_tiles(int target) {
     const int prev = f2d::level_tile_target();
     if (target >= -1) f2d::level_tile_target() = target;
+    return prev;
+}
+
+// threads of the fused smoother: 0 one per tile point (the default), 1 one per
+// input point for grids of fewer than two CTAs per SM, 2 always one per input
+// point; < 0 only queries; returns the previous setting.
+int f2d_set_level_threads(int mode) {
+    const int prev = f2d::level_one_pass();
+    if (mode >= 0 && mode <= 2) f2d::level_one_pass() = mode;
     return prev;
 }
 

@@ -105,10 +105,15 @@ F2D_DEV void stage_adv_mixed_body(const AdvMixed &a, const VB vb) {
         const size_t p = off(J, I, nv);
         sfx[ty][tx + 1] = edge_flux_f32(a.kind, a.msk, a.q, a.u, p, 1, a.method, a.order, c);
         sfy[ty + 1][tx] = edge_flux_f32(a.kind, a.msk, a.q, a.v, p, nv, a.method, a.order, c);
-        if (tx == 0)
-            sfx[ty][0] = edge_flux_f32(a.kind, a.msk, a.q, a.u, p - 1, 1, a.method, a.order, c);
         if (ty == 0)
             sfy[0][tx] = edge_flux_f32(a.kind, a.msk, a.q, a.v, p - nv, nv, a.method, a.order, c);
+    }
+    // the tile's west faces: lanes 0-7 of warp 1, one row each
+    if (ty == 1 && tx < 8) {
+        const int Jr = NH + vb.y * 8 + tx, I0 = NH + vb.x * 32;
+        if (I0 <= nv - NH - 1 && Jr <= mv - NH - 1)
+            sfx[tx][0] = edge_flux_f32(a.kind, a.msk, a.q, a.u, off(Jr, I0, nv) - 1, 1, a.method,
+                                       a.order, c);
     }
     __syncthreads();
     if (!in) return;
@@ -158,7 +163,7 @@ __global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {
 
 struct BAdvMixed {
     using Args = AdvMixed;
-    static constexpr int THREADS = 256, KIND = BK_AdvMixed;
+    static constexpr int THREADS = 256, KIND = BK_AdvMixed, MIN_BLOCKS = 5;
     F2D_DEV static void run(const Args &a, VB vb) { stage_adv_mixed_body(a, vb); }
 };
 F2D_BATCH_ENTRY(AdvMixed, BAdvMixed)

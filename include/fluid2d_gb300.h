@@ -291,6 +291,13 @@ int f2d_set_pdl(int enable);
  * graphs captured before a change keep their tiles. */
 int f2d_set_level_tiles(int target);
 
+/* Threads of the fused level smoother's CTA: 0 one per tile point (the
+ * input ring and the first sweep's ring take a second pass; default), 1 one
+ * per input point, so that every phase is one pass, for grids of fewer than
+ * two CTAs per SM, 2 always one per input point; < 0 only queries; returns
+ * the previous setting.  Results do not depend on it. */
+int f2d_set_level_threads(int mode);
+
 /* ---- batched steps: one step of each of n models (Euler or Boussinesq, float64
  * or mixed, without no-slip walls, islands or line relaxation) recorded and
  * merged into launches that each run one kernel for many models, captured in

@@ -356,20 +356,24 @@ int Gmg::build_coarse_op(cudaStream_t s) {
     if (m2 < NH || n2 < NH || (long long)m2 * n2 > COARSE_OP_MAX) return OK;
     const int n = m2 * n2;
     const size_t nn = (size_t)n * n;
+    // a hierarchy with float levels (the mixed form) cycles in float; its
+    // float64 cycles (the flux diagnostic's) keep the shared-memory CTA
     for (int k = 0; k < 2; k++) {
-        TRY(cuda_status(cudaMalloc((void **)&opd[k], nn * sizeof(double)), "coarse operator"));
         if (has_f32)
             TRY(cuda_status(cudaMalloc((void **)&opf[k], nn * sizeof(float)), "coarse operator"));
+        else
+            TRY(cuda_status(cudaMalloc((void **)&opd[k], nn * sizeof(double)), "coarse operator"));
     }
     const size_t sm64 = coarse_smem_bytes<double>(mv + cs, nv + cs, nlev - cs);
     const size_t sm32 = coarse_smem_bytes<float>(mv + cs, nv + cs, nlev - cs);
     for (int k = 0; k < 2; k++) {
         const int mode = k == 0 ? CYCLE_V : CYCLE_F;
-        TRY(mg_coarse_columns<double>(coarse_args<double>(*this, d, cs, mode, true, nullptr), sm64,
-                                      opd[k], n, s));
         if (has_f32)
             TRY(mg_coarse_columns<float>(coarse_args<float>(*this, f, cs, mode, true, nullptr),
                                          sm32, opf[k], n, s));
+        else
+            TRY(mg_coarse_columns<double>(coarse_args<double>(*this, d, cs, mode, true, nullptr),
+                                          sm64, opd[k], n, s));
     }
     op_cs = cs;
     op_n = n;

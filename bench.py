@@ -147,6 +147,10 @@ def _cpu_worker(args):
     return steps, time.perf_counter() - t0
 
 
+# float64 FMA throughput of a GB300 of this machine (independent DFMA chains on
+# every SM, CUDA events), used only if the live measurement (f2d_fp64_peak)
+# fails: the FP64-ALU roofline of the float64 kernels
+FP64_PEAK_TFLOPS = 1.20
 SMOOTH_DRAM_BYTES_PER_POINT = (17996800 + 0 + 17964288 + 0) / 1060900.
 
 
@@ -284,6 +288,20 @@ def run_ours(a, rank, world, local):
     # (k_sweep1 + k_sweep2) per grid point, from the ncu capture summarised in
     # profiles/k_sweep_turbulence_1024_fp64_dram.md (1024^2, 1060900 points)
     traffic = SMOOTH_DRAM_BYTES_PER_POINT * pts
+    # the same kernel against the float64 pipe, its real bound on this part:
+    # one damped-Jacobi update is 1 mul + 7 fma + 1 sub + 1 mul + 1 fma =
+    # 19 flops, two sweeps per call
+    fp64_flops = 2 * 19 * pts
+    fp64_achieved = fp64_flops / (probe_ms * 1e-3) / 1e12 if probe_ms > 0 else None
+    fp64_peak, fp64_src = FP64_PEAK_TFLOPS, "earlier FMA-chain measurement on this pool"
+    try:
+        import ctypes as _ct
+        from fluid2d_gb300 import _lib as _l
+        _v = _ct.c_double()
+        if _l.lib().f2d_fp64_peak(_ct.byref(_v)) == 0 and _v.value > 0:
+            fp64_peak, fp64_src = _v.value, "f2d_fp64_peak: FMA chains measured live on this GPU"
+    except Exception as exc:
+        print("fp64 peak failed: %s" % exc, file=sys.stderr)
 
     # ---- e2e through the public API with host buffers: every step uploads
     # the state (Var.state) from pinned memory, steps, reads it back
@@ -346,7 +364,11 @@ def run_ours(a, rank, world, local):
                      "traffic": traffic, "launches_probed": nprobe,
                      "avg_launch_ms": probe_ms,
                      "alg_bytes_per_launch": alg_bytes,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                     "fp64": {"achieved": fp64_achieved, "peak": fp64_peak,
+                              "unit": "TFLOP/s",
+                              "frac": (fp64_achieved / fp64_peak) if fp64_achieved else None,
+                              "flops_per_launch": fp64_flops, "peak_source": fp64_src}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": a.e2e_steps},

@@ -22,7 +22,7 @@ BUILD = os.path.join(_HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(_HERE), "include")
 SOURCES = ["api.cu", "kernels_adv.cu", "kernels_ops.cu", "kernels_mg.cu", "engine.cu",
            "kernels_fused.cu", "noalloc.cu", "kernels_mixed.cu", "timeloop.cu", "fluxdiag.cu",
-           "kernels_walls.cu", "batch.cu"]
+           "kernels_walls.cu", "batch.cu", "peaks.cu"]
 HEADERS = ["f2d_common.cuh", "f2d_kernels.cuh", "f2d_fused.cuh", "f2d_adv.cuh", "f2d_mixed.cuh",
            "f2d_loop.cuh", "f2d_flux.cuh", "f2d_walls.cuh",
            "f2d_tri.cuh", "f2d_batch.cuh"]
@@ -240,6 +240,7 @@ EXTRA = {
     "f2d_set_pdl": ([_I], _I),
     "f2d_set_level_tiles": ([_I], _I),
     "f2d_set_level_threads": ([_I], _I),
+    "f2d_fp64_peak": ([ctypes.POINTER(ctypes.c_double)], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),
 }

@@ -2,7 +2,7 @@
 
     python -m fluid2d_gb300.profile_step [--n 1024] [--precision fp64|mixed]
         [--coarse-level L] [--no-coarse-operator] [--steps K]
-        [--ensemble N --groups G --policy P]
+        [--ensemble N --groups G --policy P --coarse-offset D]
 
 Builds the decaying-turbulence workload on an n x n periodic grid, sets psi,
 the diagnostics and dt (CFL 0.8), runs one warm-up step, then K steps inside
@@ -13,8 +13,9 @@ only the launches of the profiled steps.
 
 ``--ensemble N`` profiles instead the batched step of the N-instance ensemble
 of ``workloads.ensemble(N, seed=4)`` (G groups of batched launches, merge
-policy P; G = 0: every instance's own graph on streams), one warm-up step
-and K steps inside "step".
+policy P; G = 0: every instance's own graph on streams; coarse switch D
+levels below each instance's first allowed level), one warm-up step and K
+steps inside "step".
 """
 import argparse
 import os
@@ -35,6 +36,7 @@ def main(argv=None):
     ap.add_argument("--ensemble", type=int, default=0)
     ap.add_argument("--groups", type=int, default=1)
     ap.add_argument("--policy", type=int, default=1)
+    ap.add_argument("--coarse-offset", type=int, default=0)
     a = ap.parse_args(argv)
     import torch
     from fluid2d_gb300 import engine, workloads
@@ -42,6 +44,8 @@ def main(argv=None):
         E = engine.ensemble_from_workloads(workloads.ensemble(a.ensemble, seed=4),
                                            precision=a.precision, batched=a.groups > 0,
                                            groups=max(1, a.groups), policy=a.policy)
+        if a.coarse_offset:
+            E.coarse_offset(a.coarse_offset)
         E.run(1)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("step")

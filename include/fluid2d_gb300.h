@@ -298,6 +298,11 @@ int f2d_set_level_tiles(int target);
  * the previous setting.  Results do not depend on it. */
 int f2d_set_level_threads(int mode);
 
+/* The device's float64 FMA throughput in TFLOP/s, measured (independent FMA
+ * chains on every SM, CUDA events, best of three after a warm-up): the
+ * FP64-ALU roofline of the float64 kernels.  Synchronises the device. */
+int f2d_fp64_peak(double *tflops);
+
 /* ---- batched steps: one step of each of n models (Euler or Boussinesq, float64
  * or mixed, without no-slip walls, islands or line relaxation) recorded and
  * merged into launches that each run one kernel for many models, captured in

@@ -469,20 +469,25 @@ class Ensemble(object):
         if batched:
             self.build_batch(groups, policy)
 
-    def build_batch(self, groups=1, policy=1):
+    def build_batch(self, groups=1, policy=1, balanced=False):
         """Batched steps: the instances, sorted by size, are split into
-        `groups` groups; one step of every instance of a group is merged into
+        `groups` groups (consecutive runs of the sorted list, or, balanced,
+        dealt round-robin so that every group holds a share of the large
+        instances); one step of every instance of a group is merged into
         launches that each run one kernel for the whole group
         (f2d_batch_create), captured as one graph per group, and the groups'
         graphs run on their own streams."""
         self.free_batch()
-        self._batch_args = (groups, policy)
+        self._batch_args = (groups, policy, balanced)
         L = self.models[0].L
         order = sorted(range(len(self.models)), key=lambda k: self.models[k].cells)
         groups = max(1, min(int(groups), len(order)))
         self.batch = []
         for g in range(groups):
-            idx = order[g * len(order) // groups:(g + 1) * len(order) // groups]
+            if balanced:
+                idx = order[g::groups]
+            else:
+                idx = order[g * len(order) // groups:(g + 1) * len(order) // groups]
             arr = (ctypes.c_void_p * len(idx))(*[self.models[k].h.value for k in idx])
             h = ctypes.c_void_p()
             _lib.call("f2d_batch_create", arr, len(idx), int(policy), ctypes.byref(h),

@@ -37,6 +37,7 @@ def main(argv=None):
     ap.add_argument("--groups", type=int, default=1)
     ap.add_argument("--policy", type=int, default=1)
     ap.add_argument("--coarse-offset", type=int, default=0)
+    ap.add_argument("--balanced", action="store_true")
     a = ap.parse_args(argv)
     import torch
     from fluid2d_gb300 import engine, workloads
@@ -44,6 +45,8 @@ def main(argv=None):
         E = engine.ensemble_from_workloads(workloads.ensemble(a.ensemble, seed=4),
                                            precision=a.precision, batched=a.groups > 0,
                                            groups=max(1, a.groups), policy=a.policy)
+        if a.balanced and E.batch is not None:
+            E.build_batch(max(1, a.groups), a.policy, balanced=True)
         if a.coarse_offset:
             E.coarse_offset(a.coarse_offset)
         E.run(1)

@@ -61,3 +61,34 @@ def test_batched_launches_equal_each_instance_alone(precision, groups, policy):
         torch.cuda.synchronize()
         assert torch.equal(alone.models[0].var.state, batched.models[k].var.state), k
         assert torch.equal(alone.models[0]._diag, batched.models[k]._diag), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_product_with_coarse_operators(precision):
+    """Product build: batched groups dealt round-robin, with every instance's
+    coarse part applied as its precomputed operator (the batched form of
+    the operator launch) and the coarse switch moved one level down, agree
+    with each instance run alone to rounding."""
+    import numpy as np
+    import torch
+    from fluid2d_gb300 import engine, workloads as W
+    wls = W.ensemble(4, seed=29, nmin=64, nmax=256)
+    wls.append(W.turbulence(128, 128, seed=8))
+    E = engine.ensemble_from_workloads(wls, precision=precision)
+    assert all(m.coarse_operator() > 0 for m in E.models)
+    E.coarse_offset(1)
+    E.build_batch(2, 1, balanced=True)
+    launches, ops = E.batch_info()
+    assert 0 < launches < ops
+    E.run(3)
+    torch.cuda.synchronize()
+    for k, wl in enumerate(wls):
+        M = engine.ensemble_from_workloads([wl], precision=precision, nstreams=1).models[0]
+        cur, first, nlev = M.coarse_switch()
+        M.coarse_switch(min(first + 1, nlev))
+        M.run(3)
+        torch.cuda.synchronize()
+        a, b = M.var.state.cpu().numpy(), E.models[k].var.state.cpu().numpy()
+        for v in range(a.shape[0]):
+            err = np.abs(a[v] - b[v]).max() / max(1e-300, np.abs(a[v]).max())
+            assert err <= 1e-10, (k, v, err)

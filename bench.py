@@ -215,8 +215,10 @@ def run_ours(a, rank, world, local):
     s0 = M.var.state.clone()
     # the coarse-CTA switch level that times fastest on this grid (the
     # state it advanced is put back; results do not depend on the choice)
-    from fluid2d_gb300.autotune import tune_coarse_level
+    from fluid2d_gb300.autotune import tune_coarse_level, tune_level_tiles
     tune_coarse_level(M, steps=3, warmup=1)
+    # and the level kernels' tile shape and block size (process-wide)
+    tiles, _ = tune_level_tiles(M, steps=3, warmup=1)
     M.var.state.copy_(s0)
     M.diagnostics()
     stream = torch.cuda.Stream()
@@ -354,6 +356,8 @@ def run_ours(a, rank, world, local):
         "config": {"workload": "euler-decaying-turbulence-%dx%d-perio-fp64" % (n, n),
                    "nx": n, "ny": n, "precision": "fp64", "cuda_graph": True,
                    "multigrid_levels": M.nlevs, "coarse_cta_from_level": M.coarse_level,
+                   "coarse_operator_points": M.coarse_operator(),
+                   "level_tiles": {"cta_target": tiles[0], "one_pass_threads": tiles[1]},
                    "solve_iterations_last_step": nite, "solve_residual_last_step": res,
                    "dt": dt, "maxspeed": diags.get("maxspeed"),
                    "l2": "working set > L2 (state, tendencies, hierarchy ~0.3 GB); no flush",

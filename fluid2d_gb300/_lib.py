@@ -214,6 +214,7 @@ SIGNATURES.update({
     "f2d_model_graph_kernels": [_P, _PI],
     "f2d_model_coarse_level": [_P, _I, _PI, _PI, _PI],
     "f2d_model_coarse_op": [_P, _I, _PI],
+    "f2d_model_reset_graphs": [_P],
     "f2d_batch_create": [ctypes.POINTER(ctypes.c_void_p), _I, _I, _PP],
     "f2d_batch_step": [_P, _I, _P],
     "f2d_batch_info": [_P, _PI, _PI],

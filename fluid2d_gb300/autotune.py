@@ -7,6 +7,8 @@
   one adds small latency-bound launches; the best split depends on the grid
   and the precision, so every allowed level is timed on the model's
   captured step.  Results do not depend on the choice beyond rounding.
+* ``tune_level_tiles(model)``: the CTA tile shape and block size of the
+  multigrid level kernels (process-wide settings read at graph capture).
 * ``tune_ensemble(ens)``: the instances' coarse-switch offset (their
   operators' total size against the L2 cache), the number of batched groups
   and the merge policy of an Ensemble's batched launches, against the
@@ -52,6 +54,42 @@ def tune_coarse_level(model, steps=5, warmup=2, use_cache=True):
     torch.cuda.current_stream().wait_stream(side)
     best = min(times, key=times.get)
     model.coarse_switch(best)
+    _cache[key] = (best, times)
+    return best, times
+
+
+def tune_level_tiles(model, steps=5, warmup=2, use_cache=True):
+    """The CTA tile shape and block size of the multigrid level kernels:
+    the CTA count a level's grid aims at before its tile stops shrinking
+    (f2d_set_level_tiles: 0 the largest tile, else a multiple of the SM
+    count) and the fused smoother's threads (f2d_set_level_threads: one per
+    tile point, or one per input point on small grids).  Both are process
+    settings read when a graph is captured; the fastest pair on the model's
+    captured step is kept set.  Returns ((target, threads), {pair: ms})."""
+    from . import _lib
+    L = _lib.lib(model.variant)
+    key = ("tiles", model.modelname, model.desc.nx, model.desc.ny, model.desc.precision)
+    if use_cache and key in _cache:
+        best = _cache[key][0]
+        L.f2d_set_level_tiles(best[0])
+        L.f2d_set_level_threads(best[1])
+        model.reset_graphs()
+        return _cache[key]
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    times = {}
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for pair in ((0, 0), (2 * sms, 0), (4 * sms, 0), (0, 1)):
+            L.f2d_set_level_tiles(pair[0])
+            L.f2d_set_level_threads(pair[1])
+            model.reset_graphs()
+            times[pair] = _time(lambda n: model.run(n, graph=True), steps, warmup)
+    torch.cuda.current_stream().wait_stream(side)
+    best = min(times, key=times.get)
+    L.f2d_set_level_tiles(best[0])
+    L.f2d_set_level_threads(best[1])
+    model.reset_graphs()
     _cache[key] = (best, times)
     return best, times
 

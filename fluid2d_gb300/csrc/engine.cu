@@ -1985,6 +1985,13 @@ int f2d_model_coarse_level(void *model, int level, int *current, int *first, int
     return OK;
 }
 
+int f2d_model_reset_graphs(void *model) {
+    Model *M = (Model *)model;
+    if (!M) return ERR_ARG;
+    drop_graphs(M);
+    return OK;
+}
+
 int f2d_model_coarse_op(void *model, int enable, int *n) {
     Model *M = (Model *)model;
     if (!M) return ERR_ARG;

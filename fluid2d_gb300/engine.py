@@ -264,6 +264,11 @@ class Model(object):
         self.coarse_level = cur.value
         return cur.value, first.value, nlev.value
 
+    def reset_graphs(self):
+        """Drop the captured graphs; the next graph run captures again with
+        the launch settings then current."""
+        self._call("f2d_model_reset_graphs", self.h)
+
     def coarse_operator(self, enable=None):
         """Query (enable=None) or switch the coarse part of the multigrid as a
         precomputed linear map (product build); returns its size (0: none)."""

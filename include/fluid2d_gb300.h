@@ -277,6 +277,11 @@ int f2d_model_coarse_level(void *model, int level, int *current, int *first, int
  * (default), 0 off, < 0 query; *n receives the operator's size (0: none). */
 int f2d_model_coarse_op(void *model, int enable, int *n);
 
+/* Drop the model's captured step and loop graphs: the next graph run
+ * captures again, with the launch settings then current (level tiles and
+ * threads, programmatic dependent launch). */
+int f2d_model_reset_graphs(void *model);
+
 /* Programmatic dependent launch of the engine kernels (each kernel may be
  * scheduled while its predecessor runs and waits for it before touching
  * memory): 1 on, 0 off (default), < 0 query; returns the previous setting.

@@ -239,3 +239,39 @@ def test_coarse_operator_matches_the_cycle(eng, name, precision):
         for k in range(on.shape[0]):
             fma = relerr(off[k], ex[k])
             assert relerr(on[k], off[k]) <= max(1e-12, 10 * fma), (level, k, fma)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_level_tiles_change_nothing_but_launches(eng, precision):
+    """Every CTA tile target and smoother block size of the level kernels
+    gives the same state bit for bit (exact build); the tuner keeps one."""
+    import torch
+    from fluid2d_gb300 import _lib, workloads as W
+    from fluid2d_gb300.autotune import tune_level_tiles
+    L = _lib.lib("exact")
+    prev = (L.f2d_set_level_tiles(-2), L.f2d_set_level_threads(-1))
+    wl = W.dipole(160, 96, seed=5)
+    states = []
+    try:
+        for target, threads in ((0, 0), (64, 0), (1000, 0), (0, 1), (0, 2), (500, 2)):
+            L.f2d_set_level_tiles(target)
+            L.f2d_set_level_threads(threads)
+            M = eng.from_workload(wl, variant="exact", precision=precision, dt=2e-3)
+            M.set_psi_from_vorticity()
+            M.diagnostics()
+            M.run(3)
+            torch.cuda.synchronize()
+            states.append(M.var.state.clone())
+    finally:
+        L.f2d_set_level_tiles(prev[0])
+        L.f2d_set_level_threads(prev[1])
+    for st in states[1:]:
+        assert torch.equal(st, states[0])
+    M = eng.from_workload(wl, precision=precision, dt=2e-3)
+    M.set_psi_from_vorticity()
+    M.diagnostics()
+    best, times = tune_level_tiles(M, steps=2, warmup=1, use_cache=False)
+    assert best in times and len(times) >= 2
+    P = _lib.lib("product")
+    P.f2d_set_level_tiles(0)
+    P.f2d_set_level_threads(0)

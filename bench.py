@@ -334,6 +334,14 @@ def run_ours(a, rank, world, local):
     e2e_val = world * n * n * a.e2e_steps / (e2e_ms * 1e-3)
 
     extra = {}
+    # the ensemble and the served stream tune their own launch structure;
+    # the level kernels go back to their default tiles and block sizes
+    try:
+        from fluid2d_gb300 import _lib as _l
+        _l.lib().f2d_set_level_tiles(0)
+        _l.lib().f2d_set_level_threads(0)
+    except Exception as exc:
+        print("level tiles reset failed: %s" % exc, file=sys.stderr)
     if not a.no_extra and rank == 0:
         for key, fn in (("ensemble", bench_ensemble), ("served", bench_served)):
             try:

@@ -708,20 +708,179 @@ struct BSmoothFused {
     using Args = SmoothFusedArgs<T>;
     static constexpr int THREADS = FS_THREADS_MAX;
     static constexpr int MIN_BLOCKS = FS_MIN_BLOCKS;
+    // (the float finest level runs smooth_l0_body, batched as SmoothFusedF1)
     static constexpr int KIND = sizeof(T) == 8 ? (L0 ? -1 : BK_SmoothFusedD0)
-                                               : (L0 ? BK_SmoothFusedF1 : BK_SmoothFusedF0);
+                                               : (L0 ? -1 : BK_SmoothFusedF0);
     F2D_DEV static void run(const Args &a, VB vb) { smooth_fused_body<T, L0>(a, vb); }
 };
 using BSmoothFusedD0 = BSmoothFused<double, false>;
 using BSmoothFusedF0 = BSmoothFused<float, false>;
-using BSmoothFusedF1 = BSmoothFused<float, true>;
 F2D_BATCH_ENTRY(SmoothFusedD0, BSmoothFusedD0)
 F2D_BATCH_ENTRY(SmoothFusedF0, BSmoothFusedF0)
-F2D_BATCH_ENTRY(SmoothFusedF1, BSmoothFusedF1)
+
+// The finest level's fused smoother (analytic operator through the
+// coefficient bits), for the float form whose kernel is bound by its
+// instruction count: a 32 x 32 tile per CTA of 256 threads, each thread a
+// column of four points of the tile; x on the tile's 2-ring, and the first
+// sweep's inputs (coefficient bits, mask, b) on its 1-ring, are staged in
+// shared memory once with 32-bit offsets from the tile's origin, so both
+// sweeps read only shared memory.  Same arithmetic in the same order as
+// jacobi(); the bits give the coefficients exactly as offdiag() selects them.
+constexpr int SL_T = 32, SL_TY = 8, SL_THREADS = SL_T * SL_TY;
+constexpr int SL_XW = SL_T + 4, SL_TW = SL_T + 2;
+
+template <typename T>
+size_t smooth_l0_smem() {
+    return sizeof(T) * (size_t)(SL_XW * SL_XW + 2 * SL_TW * SL_TW) +
+           sizeof(uint16_t) * SL_TW * SL_TW + SL_TW * SL_TW;
+}
+
+template <typename T>
+F2D_DEV T jacobi_bits(unsigned bits, const T *x, int W, T bq, const AnalyticT<T> &an, T c2,
+                      T c3z) {
+    const T c3 = (bits & 256u) ? an.c3 : c3z;
+    const T a0 = (bits & 1u) ? an.sc[0] : (T)0, a1 = (bits & 2u) ? an.sc[1] : (T)0,
+            a2 = (bits & 4u) ? an.sc[2] : (T)0, a3 = (bits & 8u) ? an.sc[3] : (T)0,
+            a4 = (bits & 16u) ? an.sc[3] : (T)0, a5 = (bits & 32u) ? an.sc[2] : (T)0,
+            a6 = (bits & 64u) ? an.sc[1] : (T)0, a7 = (bits & 128u) ? an.sc[0] : (T)0;
+    return x[0] * c2 + c3 * (+a0 * x[-W - 1]
+                             + a1 * x[-W]
+                             + a2 * x[-W + 1]
+                             + a3 * x[-1]
+                             + a4 * x[1]
+                             + a5 * x[W - 1]
+                             + a6 * x[W]
+                             + a7 * x[W + 1]
+                             - bq);
+}
+
+template <typename T>
+F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    extern __shared__ __align__(16) unsigned char sm[];
+    T *xs = (T *)sm;                      // x on [j0-2, j0+33] x [i0-2, i0+33]
+    T *ts = xs + SL_XW * SL_XW;           // first sweep on [j0-1, j0+32] x [i0-1, i0+32]
+    T *bs = ts + SL_TW * SL_TW;           // b on the first sweep's points
+    uint16_t *nbs = (uint16_t *)(bs + SL_TW * SL_TW);
+    int8_t *ms = (int8_t *)(nbs + SL_TW * SL_TW);
+    const LevelView<T> L = A.L;
+    const AnalyticT<T> an = A.an;
+    const T c2 = A.c2, c3z = A.c1 / fabs((T)0);  // c3 where the diagonal is 0
+    const int xmode = A.xmode;
+    const int mv = L.mv, nv = L.nv;
+    const int i0 = NH + vb.x * SL_T, j0 = NH + vb.y * SL_T;
+    const int tx = (int)threadIdx.x & (SL_T - 1), ty = (int)threadIdx.x >> 5;
+    // the x ring (rows/cols 1..m-2), 32-bit offsets from (j0-2, i0-2)
+    const size_t o2 = off(j0 - 2, i0 - 2, nv);
+    if (xmode != X_ZERO) {
+        const T *xg = L.x + o2;
+        for (int r = ty; r < SL_XW; r += SL_TY) {
+            const int j = j0 - 2 + r;
+            if (j < 1 || j > mv - 2) continue;
+            for (int c = tx; c < SL_XW; c += SL_T) {
+                const int i = i0 - 2 + c;
+                if (i < 1 || i > nv - 2) continue;
+                const int o = r * nv + c;
+                T v;
+                if (xmode == X_IN) {
+                    v = xg[o];
+                } else {
+                    const T cv = interp_value(L.msk, nv, A.cs.msk, A.cs.x, A.cs.nv, j, i);
+                    v = xmode == X_PLUS_INTERP ? xg[o] + cv : cv;
+                }
+                xs[r * SL_XW + c] = v;
+            }
+        }
+    }
+    // bits, mask and b of the first sweep's points (rows/cols 2..m-3)
+    {
+        const size_t o1 = off(j0 - 1, i0 - 1, nv);
+        const uint16_t *nbg = L.nb + o1;
+        const int8_t *mg = L.msk + o1;
+        const T *bg = L.b + o1;
+        for (int r = ty; r < SL_TW; r += SL_TY) {
+            const int j = j0 - 1 + r;
+            if (j < 2 || j > mv - 3) continue;
+            for (int c = tx; c < SL_TW; c += SL_T) {
+                const int i = i0 - 1 + c;
+                if (i < 2 || i > nv - 3) continue;
+                const int o = r * nv + c, q = r * SL_TW + c;
+                nbs[q] = nbg[o];
+                ms[q] = mg[o];
+                bs[q] = bg[o];
+            }
+        }
+    }
+    __syncthreads();
+    // first sweep
+    for (int r = ty; r < SL_TW; r += SL_TY) {
+        const int j = j0 - 1 + r;
+        if (j < 2 || j > mv - 3) continue;
+        for (int c = tx; c < SL_TW; c += SL_T) {
+            const int i = i0 - 1 + c;
+            if (i < 2 || i > nv - 3) continue;
+            const int q = r * SL_TW + c;
+            T v;
+            if (ms[q] == 0) {
+                v = (T)0;
+            } else if (xmode == X_ZERO) {
+                v = ((nbs[q] & 256u) ? an.c3 : c3z) * (-bs[q]);
+            } else {
+                v = jacobi_bits<T>(nbs[q], xs + (r + 1) * SL_XW + (c + 1), SL_XW, bs[q], an, c2,
+                                   c3z);
+            }
+            ts[q] = v;
+        }
+    }
+    __syncthreads();
+    // second sweep: the tile, each thread rows ty, ty+8, ty+16, ty+24 of column tx
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    const bool direct = j0 >= 2 * NH && j0 + SL_T <= m2 && i0 >= 2 * NH && i0 + SL_T <= n2;
+    T *out = A.out;
+    const int i = i0 + tx;
+    if (i > nv - NH - 1) return;
+    for (int r = ty; r < SL_T; r += SL_TY) {
+        const int j = j0 + r;
+        if (j > mv - NH - 1) break;
+        const int q = (r + 1) * SL_TW + (tx + 1);
+        T v = (T)0;
+        if (ms[q] != 0)
+            v = jacobi_bits<T>(nbs[q], ts + q, SL_TW, bs[q], an, c2, c3z);
+        if (direct)
+            out[off(j, i, nv)] = v;
+        else
+            store_images(out, j, i, mv, nv, v);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SL_THREADS) k_smooth_l0(SmoothFusedArgs<T> a) {
+    pdl_prologue();
+    smooth_l0_body<T>(a, F2D_VB_NATIVE);
+}
+
+template <typename T>
+struct BSmoothL0 {
+    using Args = SmoothFusedArgs<T>;
+    static constexpr int THREADS = SL_THREADS;
+    static constexpr int MIN_BLOCKS = 6;
+    static constexpr int KIND = sizeof(T) == 4 ? BK_SmoothFusedF1 : -1;
+    F2D_DEV static void run(const Args &a, VB vb) { smooth_l0_body<T>(a, vb); }
+};
+using BSmoothL0F = BSmoothL0<float>;
+F2D_BATCH_ENTRY(SmoothFusedF1, BSmoothL0F)
 
 template <typename T>
 int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
                     const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s) {
+    if (an && L.nb && sizeof(T) == 4) {  // the float finest level
+        CoarseSrc<T> cs{nullptr, nullptr, 0};
+        if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
+        SmoothFusedArgs<T> a{L, *an, c1, c2, xmode, cs, out, active, SL_T, SL_T};
+        const dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, dim3(SL_T, SL_T));
+        return launch_body<BSmoothL0<T>>(k_smooth_l0<T>, a, g, dim3(SL_THREADS),
+                                         smooth_l0_smem<T>(), s, "mg_smooth_l0");
+    }
     const dim3 tile = level_tile(L.mv - 2 * NH, L.nv - 2 * NH, FS_TX, FS_TY);
     const dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, tile);
     const dim3 b(smooth_fused_threads(tile, g));

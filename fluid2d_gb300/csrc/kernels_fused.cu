@@ -772,24 +772,24 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
     const int tx = (int)threadIdx.x & (SL_T - 1), ty = (int)threadIdx.x >> 5;
     // the x ring (rows/cols 1..m-2), 32-bit offsets from (j0-2, i0-2)
     const size_t o2 = off(j0 - 2, i0 - 2, nv);
+    // the rings are walked as flat index ranges (full warps; the constant
+    // widths make the row/column split a multiply-shift)
+    const int tid = (int)threadIdx.x;
     if (xmode != X_ZERO) {
         const T *xg = L.x + o2;
-        for (int r = ty; r < SL_XW; r += SL_TY) {
-            const int j = j0 - 2 + r;
-            if (j < 1 || j > mv - 2) continue;
-            for (int c = tx; c < SL_XW; c += SL_T) {
-                const int i = i0 - 2 + c;
-                if (i < 1 || i > nv - 2) continue;
-                const int o = r * nv + c;
-                T v;
-                if (xmode == X_IN) {
-                    v = xg[o];
-                } else {
-                    const T cv = interp_value(L.msk, nv, A.cs.msk, A.cs.x, A.cs.nv, j, i);
-                    v = xmode == X_PLUS_INTERP ? xg[o] + cv : cv;
-                }
-                xs[r * SL_XW + c] = v;
+        for (int q = tid; q < SL_XW * SL_XW; q += SL_THREADS) {
+            const int r = q / SL_XW, c = q - r * SL_XW;
+            const int j = j0 - 2 + r, i = i0 - 2 + c;
+            if (j < 1 || j > mv - 2 || i < 1 || i > nv - 2) continue;
+            const int o = r * nv + c;
+            T v;
+            if (xmode == X_IN) {
+                v = xg[o];
+            } else {
+                const T cv = interp_value(L.msk, nv, A.cs.msk, A.cs.x, A.cs.nv, j, i);
+                v = xmode == X_PLUS_INTERP ? xg[o] + cv : cv;
             }
+            xs[q] = v;
         }
     }
     // bits, mask and b of the first sweep's points (rows/cols 2..m-3)
@@ -798,39 +798,31 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
         const uint16_t *nbg = L.nb + o1;
         const int8_t *mg = L.msk + o1;
         const T *bg = L.b + o1;
-        for (int r = ty; r < SL_TW; r += SL_TY) {
-            const int j = j0 - 1 + r;
-            if (j < 2 || j > mv - 3) continue;
-            for (int c = tx; c < SL_TW; c += SL_T) {
-                const int i = i0 - 1 + c;
-                if (i < 2 || i > nv - 3) continue;
-                const int o = r * nv + c, q = r * SL_TW + c;
-                nbs[q] = nbg[o];
-                ms[q] = mg[o];
-                bs[q] = bg[o];
-            }
+        for (int q = tid; q < SL_TW * SL_TW; q += SL_THREADS) {
+            const int r = q / SL_TW, c = q - r * SL_TW;
+            const int j = j0 - 1 + r, i = i0 - 1 + c;
+            if (j < 2 || j > mv - 3 || i < 2 || i > nv - 3) continue;
+            const int o = r * nv + c;
+            nbs[q] = nbg[o];
+            ms[q] = mg[o];
+            bs[q] = bg[o];
         }
     }
     __syncthreads();
     // first sweep
-    for (int r = ty; r < SL_TW; r += SL_TY) {
-        const int j = j0 - 1 + r;
-        if (j < 2 || j > mv - 3) continue;
-        for (int c = tx; c < SL_TW; c += SL_T) {
-            const int i = i0 - 1 + c;
-            if (i < 2 || i > nv - 3) continue;
-            const int q = r * SL_TW + c;
-            T v;
-            if (ms[q] == 0) {
-                v = (T)0;
-            } else if (xmode == X_ZERO) {
-                v = ((nbs[q] & 256u) ? an.c3 : c3z) * (-bs[q]);
-            } else {
-                v = jacobi_bits<T>(nbs[q], xs + (r + 1) * SL_XW + (c + 1), SL_XW, bs[q], an, c2,
-                                   c3z);
-            }
-            ts[q] = v;
+    for (int q = tid; q < SL_TW * SL_TW; q += SL_THREADS) {
+        const int r = q / SL_TW, c = q - r * SL_TW;
+        const int j = j0 - 1 + r, i = i0 - 1 + c;
+        if (j < 2 || j > mv - 3 || i < 2 || i > nv - 3) continue;
+        T v;
+        if (ms[q] == 0) {
+            v = (T)0;
+        } else if (xmode == X_ZERO) {
+            v = ((nbs[q] & 256u) ? an.c3 : c3z) * (-bs[q]);
+        } else {
+            v = jacobi_bits<T>(nbs[q], xs + (r + 1) * SL_XW + (c + 1), SL_XW, bs[q], an, c2, c3z);
         }
+        ts[q] = v;
     }
     __syncthreads();
     // second sweep: the tile, each thread rows ty, ty+8, ty+16, ty+24 of column tx

@@ -151,7 +151,7 @@ def _cpu_worker(args):
 # every SM, CUDA events), used only if the live measurement (f2d_fp64_peak)
 # fails: the FP64-ALU roofline of the float64 kernels
 FP64_PEAK_TFLOPS = 1.20
-SMOOTH_DRAM_BYTES_PER_POINT = (17996800 + 0 + 17964288 + 0) / 1060900.
+SMOOTH_DRAM_BYTES_PER_POINT = (20111360 + 0 + 20073472 + 0) / 1060900.
 
 
 def cpu_baseline(n, budget, cores):

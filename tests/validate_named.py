@@ -1,6 +1,6 @@
 """Full-size parity and error reports of the named workloads.
 
-    python -m fluid2d_gb300.validate [dipole|turbulence|shear|all] [--out FILE]
+    python tests/validate_named.py [dipole|turbulence|shear|all] [--out FILE]
 
 * dipole      Euler dipole, closed 128x128, 200 steps: float64 GPU path against
               the CPU oracle at every step (relative L-inf of omega and psi).
@@ -12,12 +12,18 @@
               field relative L2 and L-inf every 100 steps over 1000 steps.
 
 The oracle (CPU restatement of the reference) is the checker here; the GPU
-paths are what is measured.
+paths are what is measured.  A report script beside the parity tests (pytest
+does not collect it).
 """
 import argparse
 import json
+import os
 import sys
 import time
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 
 import numpy as np
 
@@ -32,7 +38,7 @@ def _rel_l2(a, b):
 
 def gpu_vs_oracle(wl, steps, every=1, variant="product", **kw):
     import torch
-    from . import engine
+    from fluid2d_gb300 import engine
     from oracle import stepper
     p, O = stepper.from_workload(wl, **kw)
     dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
@@ -62,7 +68,7 @@ def gpu_vs_oracle(wl, steps, every=1, variant="product", **kw):
 
 def mixed_vs_fp64(wl, steps, every, **kw):
     import torch
-    from . import engine
+    from fluid2d_gb300 import engine
     A = engine.from_workload(wl, **kw)
     A.set_psi_from_vorticity()
     d = A.diagnostics()
@@ -91,7 +97,7 @@ def mixed_vs_fp64(wl, steps, every, **kw):
 
 
 def main(argv=None):
-    from . import workloads as W
+    from fluid2d_gb300 import workloads as W
     ap = argparse.ArgumentParser()
     ap.add_argument("which", nargs="?", default="all")
     ap.add_argument("--out", default=None)

@@ -561,7 +561,13 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
             bet[l] = mem.at<double>(o_bet[l]);
             TRY(mg_tri_factor(d[l], l == 0 ? &an : nullptr, gam[l], bet[l], s));
         }
-    return build_coarse_op(s);
+    // without its coarse operators (no memory for them) the hierarchy runs
+    // the cycle in the coarse CTA: same function, so set-up goes on
+    if (build_coarse_op(s) != OK) {
+        free_coarse_op();
+        (void)cudaGetLastError();
+    }
+    return OK;
 }
 
 template <typename T>
@@ -1976,7 +1982,10 @@ int f2d_model_coarse_level(void *model, int level, int *current, int *first, int
         if (level != g.cs) {
             g.cs = level;
             drop_graphs(M);
-            TRY(rebuild_coarse_op(g));
+            if (rebuild_coarse_op(g) != OK) {  // fall back to the coarse CTA
+                g.free_coarse_op();
+                (void)cudaGetLastError();
+            }
         }
     }
     if (current) *current = g.cs;

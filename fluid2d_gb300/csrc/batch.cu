@@ -31,7 +31,7 @@ Recorder *&recorder() {
 }
 
 bool &pdl_enabled() {
-    static bool on = false;
+    static bool on = true;
     return on;
 }
 
@@ -256,8 +256,8 @@ void batch_destroy(void *b) { delete (Batch *)b; }
 
 extern "C" {
 
-// programmatic dependent launch of the engine kernels: on (1) or off (0, the
-// default); returns the previous setting.  Graphs captured before a change
+// programmatic dependent launch of the engine kernels: on (1, the default) or
+// off (0); returns the previous setting.  Graphs captured before a change
 // keep the launches they were captured with.
 int f2d_set_pdl(int enable) {
     const int prev = f2d::pdl_enabled() ? 1 : 0;

@@ -284,7 +284,7 @@ int f2d_model_reset_graphs(void *model);
 
 /* Programmatic dependent launch of the engine kernels (each kernel may be
  * scheduled while its predecessor runs and waits for it before touching
- * memory): 1 on, 0 off (default), < 0 query; returns the previous setting.
+ * memory): 1 on (default), 0 off, < 0 query; returns the previous setting.
  * Graphs captured before a change keep their launches. */
 int f2d_set_pdl(int enable);
 

@@ -50,7 +50,8 @@ extern "C" {
 int f2d_version(void);
 /* message of the last failing call on this host thread ("" if none) */
 const char *f2d_last_error(void);
-/* 1 if this build rounds every operation separately (no FMA contraction) */
+/* 1 if the library was compiled to round every operation separately (no FMA
+ * contraction) */
 int f2d_exact_arithmetic(void);
 
 /* ------------------------------------------------ fortran_advection ---- */

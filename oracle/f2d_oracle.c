@@ -3,8 +3,9 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the GB300
  * kernels of fluid2d_gb300.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference arm of bench.py may load it, and only as the
- * checker or as the timed CPU baseline -- never as a product code path.
+ * cpu_baseline / reference arm of bench.py may load it, and only as what the
+ * GPU results are compared against or as the timed CPU baseline -- never as a
+ * product code path.
  *
  * Every routine restates the Fortran routine of the same name in
  *   core/fortran_advection.f90, core/fortran_fluxes.f90,

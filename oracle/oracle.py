@@ -1,7 +1,7 @@
 """ctypes view of the C oracle with the f2py calling conventions of Fluid2d.
 
-TEST INFRASTRUCTURE ONLY: the oracle is the checker for the GB300 kernels of
-``fluid2d_gb300``.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+TEST INFRASTRUCTURE ONLY: the oracle is what the GB300 kernels of
+``fluid2d_gb300`` are compared against.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
 baseline / reference arm of ``bench.py`` may import this module.
 
 Each function keeps the Python signature that f2py generates for the Fortran

@@ -1,6 +1,7 @@
 """Restatement of Fluid2d's Python sequencing over the C oracle kernels.
 
-TEST INFRASTRUCTURE ONLY: this is the step-level checker for fluid2d_gb300.
+TEST INFRASTRUCTURE ONLY: the step-level reference the parity tests compare
+fluid2d_gb300 against.
 Only tests/, __graft_entry__.smoke() and the CPU baseline / reference arm of
 bench.py may import it.
 

@@ -27,7 +27,7 @@ from fluid2d_gb300 import workloads as W  # noqa: E402
 from oracle import refshim, stepper  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# where this build found the reference sources (read-only)
+# where the reference sources are read from (read-only)
 DEFAULT_CORE = "/root/reference/core"
 
 

@@ -4,8 +4,8 @@ With the exact build, closed-domain Euler, Boussinesq and QG states after
 several RK3 steps are bit-identical to the oracle (the only reductions that
 feed the state are maxima); the periodic Euler case differs by the rounding
 of the mean of psi (a sum), so it is compared with a tolerance.  The product
-build (FMA contraction) is compared at 1e-10 relative L-inf, the north-star
-parity bar after 10 steps.
+build (FMA contraction) is compared at 1e-10 relative L-inf, the parity bar
+after 10 steps.
 """
 import numpy as np
 import pytest

@@ -2,7 +2,7 @@
 
 Fluxes in float32, multigrid cycles in float32 inside a float64 defect
 correction (float64 residual and psi accumulation), float64 RK accumulation
-and diagnostics.  Bar (the benchmark spec): single-step relative L2 error <= 1e-6
+and diagnostics.  Bar: single-step relative L2 error <= 1e-6
 per field against the float64 oracle from an identical state.
 """
 import numpy as np

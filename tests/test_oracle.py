@@ -1,4 +1,4 @@
-"""CPU tests of the oracle (the parity checker), no GPU needed.
+"""CPU tests of the oracle (the parity reference), no GPU needed.
 
 * golden: the oracle stepper replays the fixtures of tests/golden/ (made by
   running the reference's own Python over the oracle kernels) bit for bit;

@@ -5,13 +5,13 @@
 * dipole      Euler dipole, closed 128x128, 200 steps: float64 GPU path against
               the CPU oracle at every step (relative L-inf of omega and psi).
 * turbulence  Euler turbulence, periodic 1024x1024: float64 GPU path against the
-              CPU oracle over the first 10 steps (the spec parity bar is
-              omega/psi within 1e-10 relative L-inf after 10 steps).
+              CPU oracle over the first 10 steps (the parity bar: omega/psi
+              within 1e-10 relative L-inf after 10 steps).
 * shear       Boussinesq shear layer, 'xchannel' 2048x512, Ri = 0.1: the mixed
               form against the float64 GPU path (itself at oracle parity), per
               field relative L2 and L-inf every 100 steps over 1000 steps.
 
-The oracle (CPU restatement of the reference) is the checker here; the GPU
+The oracle (CPU restatement of the reference) is the reference of comparison; the GPU
 paths are what is measured.  A report script beside the parity tests (pytest
 does not collect it).
 """

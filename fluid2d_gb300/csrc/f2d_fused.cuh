@@ -6,6 +6,33 @@
 namespace f2d {
 
 constexpr int NH = 3;           // halo width (the reference requires 3)
+
+// call f(offset) for the point (J, I) and each of its periodic halo images:
+// rows J, J - m2 (if J is among the last NH interior rows), J + m2 (if among
+// the first NH), likewise for columns, every combination (scalars rather than
+// small indexed arrays, which would live in local memory)
+template <class F>
+F2D_DEV void for_images(int J, int I, int mv, int nv, F &&f) {
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    const int ja = (J >= m2 && J < m2 + NH) ? J - m2 : -1;
+    const int jb = (J >= NH && J < 2 * NH) ? J + m2 : -1;
+    const int ia = (I >= n2 && I < n2 + NH) ? I - n2 : -1;
+    const int ib = (I >= NH && I < 2 * NH) ? I + n2 : -1;
+    f(off(J, I, nv));
+    if (ia >= 0) f(off(J, ia, nv));
+    if (ib >= 0) f(off(J, ib, nv));
+    if (ja >= 0) {
+        f(off(ja, I, nv));
+        if (ia >= 0) f(off(ja, ia, nv));
+        if (ib >= 0) f(off(ja, ib, nv));
+    }
+    if (jb >= 0) {
+        f(off(jb, I, nv));
+        if (ia >= 0) f(off(jb, ia, nv));
+        if (ib >= 0) f(off(jb, ib, nv));
+    }
+}
+
 constexpr int MAX_LEVELS = 24;  // core/gmg/level.py:112-115 aborts beyond 20
 
 // One multigrid level on the device.  Arrays are (mv, nv) row-major with

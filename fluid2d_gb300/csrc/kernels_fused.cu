@@ -168,33 +168,36 @@ F2D_DEV T restrict_value(const int8_t *msk2, int nv2, const T *r, int nv1, int J
 template <typename T>
 F2D_DEV T interp_value(const int8_t *msk1, int nv1, const int8_t *msk2, const T *x2, int nv2,
                        int J1, int I1) {
-    if (msk1[off(J1, I1, nv1)] <= 0) return (T)0;
     const int J2 = (J1 >> 1) + 1, I2 = (I1 >> 1) + 1;
     const int dj = J1 & 1, di = I1 & 1;
     const size_t q = off(J2, I2, nv2);
-    const T c2[3] = {(T)0, (T)1, (T)0.5};
-    if (!dj && !di) return x2[q];
-    if (!dj) return (x2[q] + x2[q + 1]) * c2[msk2[q] + msk2[q + 1]];
-    if (!di) return (x2[q] + x2[q + nv2]) * c2[msk2[q] + msk2[q + nv2]];
-    const T c3[5] = {(T)0, (T)1, (T)0.5, (T)r4(0.3333333333333333333333333333f), (T)0.25};
-    const int s = msk2[q] + msk2[q + 1] + msk2[q + nv2] + msk2[q + nv2 + 1];
-    return c3[s] * (x2[q] + x2[q + 1] + x2[q + nv2] + x2[q + nv2 + 1]);
+    // every operand is read up front (one memory round trip; the four coarse
+    // points exist for every fine point of rows/cols 1..m-2), and the weight
+    // tables are selects rather than indexed local arrays
+    const int m1 = msk1[off(J1, I1, nv1)];
+    const int k00 = msk2[q], k01 = msk2[q + 1], k10 = msk2[q + nv2], k11 = msk2[q + nv2 + 1];
+    const T x00 = x2[q], x01 = x2[q + 1], x10 = x2[q + nv2], x11 = x2[q + nv2 + 1];
+    if (m1 <= 0) return (T)0;
+    if (!dj && !di) return x00;
+    if (!dj || !di) {
+        const int k = dj ? k00 + k10 : k00 + k01;
+        const T c = k == 0 ? (T)0 : (k == 1 ? (T)1 : (T)0.5);
+        return (x00 + (dj ? x10 : x01)) * c;
+    }
+    const int sm4 = k00 + k01 + k10 + k11;
+    const T c = sm4 == 0 ? (T)0
+                         : sm4 == 1 ? (T)1
+                                    : sm4 == 2 ? (T)0.5
+                                               : sm4 == 3 ? (T)r4(0.3333333333333333333333333333f)
+                                                          : (T)0.25;
+    return c * (x00 + x01 + x10 + x11);
 }
 
 // store an interior value and its periodic halo images
 // (core/gmg/fortran_multigrid.f90:365-412)
 template <typename T>
 F2D_DEV void store_images(T *a, int J, int I, int mv, int nv, T v) {
-    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
-    int rows[3], cols[3], nr = 0, nc = 0;
-    rows[nr++] = J;
-    if (J >= m2 && J < m2 + NH) rows[nr++] = J - m2;
-    if (J >= NH && J < 2 * NH) rows[nr++] = J + m2;
-    cols[nc++] = I;
-    if (I >= n2 && I < n2 + NH) cols[nc++] = I - n2;
-    if (I >= NH && I < 2 * NH) cols[nc++] = I + n2;
-    for (int r = 0; r < nr; r++)
-        for (int c = 0; c < nc; c++) a[off(rows[r], cols[c], nv)] = v;
+    for_images(J, I, mv, nv, [&](size_t q) { a[q] = v; });
 }
 
 F2D_DEV bool inactive(const int *active) { return active != nullptr && *active == 0; }
@@ -1448,22 +1451,13 @@ F2D_DEV void stage_adv_body(const AdvStage &a, const VB vb) {
         y = y + a.diff_coef * lap;
     }
     const double dt = a.rk ? *a.dt : 0.;
-    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
-    int rows[3], cols[3], nr = 0, nc = 0;
-    rows[nr++] = J;
-    if (J >= m2 && J < m2 + NH) rows[nr++] = J - m2;
-    if (J >= NH && J < 2 * NH) rows[nr++] = J + m2;
-    cols[nc++] = I;
-    if (I >= n2 && I < n2 + NH) cols[nc++] = I - n2;
-    if (I >= NH && I < 2 * NH) cols[nc++] = I + n2;
-    for (int r = 0; r < nr; r++)
-        for (int k = 0; k < nc; k++) {
-            const size_t q = off(rows[r], cols[k], nv);
-            a.dq[q] = y;
-            if (a.rk)
-                a.out[q] = rk_combine(a.rk, a.base[q], a.d0 ? a.d0[q] : 0., a.d1 ? a.d1[q] : 0., y,
-                                      dt);
-        }
+    // the point and its periodic halo images (store_images' positions)
+    auto put = [&](size_t q) {
+        a.dq[q] = y;
+        if (a.rk)
+            a.out[q] = rk_combine(a.rk, a.base[q], a.d0 ? a.d0[q] : 0., a.d1 ? a.d1[q] : 0., y, dt);
+    };
+    for_images(J, I, mv, nv, put);
 }
 
 template <typename TC>

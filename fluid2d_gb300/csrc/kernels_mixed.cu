@@ -135,25 +135,16 @@ F2D_DEV void stage_adv_mixed_body(const AdvMixed &a, const VB vb) {
         y = y + a.diff_coef * lap;
     }
     const float dt = a.dtf[0];
-    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
-    int rows[3], cols[3], nr = 0, nc = 0;
-    rows[nr++] = J;
-    if (J >= m2 && J < m2 + NH) rows[nr++] = J - m2;
-    if (J >= NH && J < 2 * NH) rows[nr++] = J + m2;
-    cols[nc++] = I;
-    if (I >= n2 && I < n2 + NH) cols[nc++] = I - n2;
-    if (I >= NH && I < 2 * NH) cols[nc++] = I + n2;
-    for (int r = 0; r < nr; r++)
-        for (int k = 0; k < nc; k++) {
-            const size_t q = off(rows[r], cols[k], nv);
-            a.dq[q] = y;
-            if (a.rk < 3) {
-                a.sout[q] = rk_stage_f32(a.rk, a.sbase[q], a.d0 ? a.d0[q] : 0.f, y, dt);
-            } else {
-                const float inc = (dt / 6.f) * (a.d0[q] + a.d1[q] + 4.f * y);
-                a.xout[q] = a.xout[q] + (double)inc;
-            }
+    // the point and its periodic halo images
+    for_images(J, I, mv, nv, [&](size_t q) {
+        a.dq[q] = y;
+        if (a.rk < 3) {
+            a.sout[q] = rk_stage_f32(a.rk, a.sbase[q], a.d0 ? a.d0[q] : 0.f, y, dt);
+        } else {
+            const float inc = (dt / 6.f) * (a.d0[q] + a.d1[q] + 4.f * y);
+            a.xout[q] = a.xout[q] + (double)inc;
         }
+    });
 }
 
 __global__ void __launch_bounds__(256) k_stage_adv_mixed(AdvMixed a) {

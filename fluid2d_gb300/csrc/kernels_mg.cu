@@ -228,8 +228,12 @@ __global__ void k_interpolate(const int8_t *__restrict__ msk1, const int8_t *__r
     int I2 = 1 + blockIdx.x * MG_TX + threadIdx.x;
     int J2 = 1 + blockIdx.y * MG_TY + threadIdx.y;
     if (I2 > n2 - 3 || J2 > m2 - 3) return;
-    const double c2[3] = {0., 1., 0.5};
-    const double c3[5] = {0., 1., 0.5, r4(0.3333333333333333333333333333f), 0.25};
+    // the weight tables as selects (an indexed local array lives in local memory)
+    auto c2 = [](int k) { return k == 0 ? 0. : (k == 1 ? 1. : 0.5); };
+    auto c3 = [](int k) {
+        return k == 0 ? 0. : k == 1 ? 1. : k == 2 ? 0.5 : k == 3 ? r4(0.3333333333333333333333333333f)
+                                                                 : 0.25;
+    };
     int J1 = 2 * J2 - shift, I1 = 2 * I2 - shift;
     size_t q = off(J2, I2, n2);
     double a = x2[q], bx = x2[q + 1], by = x2[q + n2], bxy = x2[q + n2 + 1];
@@ -240,15 +244,15 @@ __global__ void k_interpolate(const int8_t *__restrict__ msk1, const int8_t *__r
     }
     if (J1 < m1 && I1 + 1 < n1) {
         size_t p = off(J1, I1 + 1, n1);
-        x1[p] = msk1[p] > 0 ? (a + bx) * c2[ma + mbx] : 0.;
+        x1[p] = msk1[p] > 0 ? (a + bx) * c2(ma + mbx) : 0.;
     }
     if (J1 + 1 < m1 && I1 < n1) {
         size_t p = off(J1 + 1, I1, n1);
-        x1[p] = msk1[p] > 0 ? (a + by) * c2[ma + mby] : 0.;
+        x1[p] = msk1[p] > 0 ? (a + by) * c2(ma + mby) : 0.;
     }
     if (J1 + 1 < m1 && I1 + 1 < n1) {
         size_t p = off(J1 + 1, I1 + 1, n1);
-        x1[p] = msk1[p] > 0 ? c3[ma + mbx + mby + mbxy] * (a + bx + by + bxy) : 0.;
+        x1[p] = msk1[p] > 0 ? c3(ma + mbx + mby + mbxy) * (a + bx + by + bxy) : 0.;
     }
 }
 

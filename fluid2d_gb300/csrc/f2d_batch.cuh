@@ -90,11 +90,22 @@ struct body_min_blocks<B, std::void_t<decltype(B::MIN_BLOCKS)>> {
 template <class Body>
 __global__ void __launch_bounds__(Body::THREADS, body_min_blocks<Body>::value)
     k_batch(const typename Body::Args *args, BatchGrid g) {
+    using Args = typename Body::Args;
+    static_assert(sizeof(Args) % 4 == 0, "argument blocks are copied as words");
+    // the instance's arguments go to shared memory once per block: the body
+    // then reads them from there as it needs them instead of holding them in
+    // registers (as a kernel's own parameters are held in constant memory)
+    __shared__ __align__(16) unsigned char abuf[sizeof(Args)];
     pdl_prologue();
     const int i = batch_instance(g, (int)blockIdx.x);
+    const int nthr = (int)(blockDim.x * blockDim.y);
+    const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
+    for (int w = tid; w < (int)(sizeof(Args) / 4); w += nthr)
+        ((int *)abuf)[w] = ((const int *)(args + i))[w];
+    __syncthreads();
     const int lb = (int)blockIdx.x - g.start[i];
     const int gx = g.gxy[2 * i];
-    Body::run(args[i], VB{lb % gx, lb / gx, gx, g.gxy[2 * i + 1]});
+    Body::run(*(const Args *)abuf, VB{lb % gx, lb / gx, gx, g.gxy[2 * i + 1]});
 }
 
 // body kinds (the registry in batch.cu maps each to its batched launcher)

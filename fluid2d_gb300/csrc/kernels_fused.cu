@@ -858,7 +858,7 @@ template <typename T>
 struct BSmoothL0 {
     using Args = SmoothFusedArgs<T>;
     static constexpr int THREADS = SL_THREADS;
-    static constexpr int MIN_BLOCKS = 6;
+    static constexpr int MIN_BLOCKS = 5;
     static constexpr int KIND = sizeof(T) == 4 ? BK_SmoothFusedF1 : -1;
     F2D_DEV static void run(const Args &a, VB vb) { smooth_l0_body<T>(a, vb); }
 };

@@ -80,7 +80,7 @@ def tune_level_tiles(model, steps=5, warmup=2, use_cache=True):
     side = torch.cuda.Stream()
     side.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(side):
-        for pair in ((0, 0), (2 * sms, 0), (4 * sms, 0), (0, 1)):
+        for pair in ((0, 0), (2 * sms, 0), (4 * sms, 0), (0, 1), (2 * sms, 1)):
             L.f2d_set_level_tiles(pair[0])
             L.f2d_set_level_threads(pair[1])
             model.reset_graphs()

@@ -135,6 +135,7 @@ SIGNATURES = {
     "f2d_cornertocell": [_P, _P, _I, _I, _P],
     "f2d_add_diffusion": [_P, _P, _D, _I, _D, _P, _I, _I, _P],
     "f2d_add_torque": [_P, _P, _D, _I, _D, _P, _I, _I, _P],
+    "f2d_computenoslipsourceterm": [_P, _P, _P, _D, _D, _I, _I, _I, _P, _P],
     "f2d_computedotprod": [_P, _P, _P, _I, _I, _I, _P, _P],
     "f2d_computemax": [_P, _P, _I, _I, _I, _P, _P],
     "f2d_computesum": [_P, _P, _I, _I, _I, _P, _P],

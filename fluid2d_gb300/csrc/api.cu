@@ -8,6 +8,7 @@
 #include "../../include/fluid2d_gb300.h"
 #include "f2d_common.cuh"
 #include "f2d_kernels.cuh"
+#include "f2d_walls.cuh"
 
 namespace f2d {
 
@@ -149,6 +150,11 @@ int f2d_add_diffusion(const int8_t *msk, const double *trac, double dx, int nh, 
 int f2d_add_torque(const int8_t *msk, const double *buoy, double dx, int nh, double gravity,
                    double *domega, int m, int n, void *stream) {
     return launch_add_torque(msk, buoy, dx, nh, gravity, domega, m, n, STREAM(stream));
+}
+
+int f2d_computenoslipsourceterm(const int8_t *msk, const double *x, double *y, double dx,
+                                double dy, int nh, int m, int n, double *total, void *stream) {
+    return launch_noslip_dropin(msk, x, y, dx, dy, nh, m, n, total, STREAM(stream));
 }
 
 // reduction kinds, see kernels_ops.cu

@@ -9,6 +9,10 @@ namespace f2d {
 // interior cells; the halo is filled by the caller
 int noslip_source(const int8_t *msknoslip, const double *psi, double *src, double dx, double dy,
                   int mv, int nv, cudaStream_t s);
+// the f2py routine on a caller array: every cell its loop writes, and its
+// intent(out) total (to the device double *total, skipped when null)
+int launch_noslip_dropin(const int8_t *msk, const double *x, double *y, double dx, double dy,
+                         int nh, int m, int n, double *total, cudaStream_t s);
 // src -= (sum[0]/bcarea)*mskbc over the whole array
 int noslip_mean(double *src, const double *sum, const int8_t *mskbc, double bcarea, size_t n,
                 cudaStream_t s);

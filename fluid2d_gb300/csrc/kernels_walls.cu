@@ -51,6 +51,133 @@ int noslip_source(const int8_t *msknoslip, const double *psi, double *src, doubl
     return launch_status("noslip_source");
 }
 
+// ---- the f2py routine itself (core/fortran_operators.f90:221-277), for
+// callers of fortran_operators.computenoslipsourceterm (core/operators.py:256).
+// Its loop visits 1-based rows nh+1..m-nh+1 and columns nh+1..n-nh+1, so it
+// also writes the first halo row and column after the interior, and its
+// scatters reach row and column nh.  Written here, 0-based:
+//  * rows [0, nh): 0, except row nh-1 at columns [nh, n-nh], which takes the
+//    south-edge term of the visited cell above it when that cell is solid;
+//  * rows [nh, m-nh]: columns [0, nh-1) are 0; column nh-1 takes the
+//    west-edge term of its solid east neighbour; columns [nh, n-nh] gather
+//    their terms in the loop's order (own west, own south, east neighbour's
+//    west, north neighbour's south), the last visited column and row
+//    receiving nothing from beyond;
+//  * every other cell keeps its value (f2py intent(inplace)).
+__global__ void k_noslip_dropin(const int8_t *m, const double *x, double *y, double cff, int nh,
+                                int mm, int nn) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= nn || j > mm - nh) return;
+    const size_t p = off(j, i, nn);
+    const int ilast = nn - nh, jlast = mm - nh;  // last visited column and row
+    double r = 0.;
+    if (j < nh) {
+        if (j == nh - 1 && i >= nh && i <= ilast && m[p + nn] == 0 && m[p] + m[p + nn] == 1)
+            r = r - edge_u(x, p + nn, nn, cff);
+    } else if (i < nh - 1) {
+        // zeroed by y(j,1:nh)=0
+    } else if (i == nh - 1) {
+        if (m[p + 1] == 0 && m[p] + m[p + 1] == 1) r = r + edge_v(x, p + 1, nn, cff);
+    } else if (i <= ilast) {
+        const int mc = m[p];
+        if (mc != 0) {
+            if (m[p - 1] + mc == 1) r = r - edge_v(x, p, nn, cff);
+            if (m[p - nn] + mc == 1) r = r + edge_u(x, p, nn, cff);
+        }
+        if (i < ilast && m[p + 1] == 0 && mc + m[p + 1] == 1) r = r + edge_v(x, p + 1, nn, cff);
+        if (j < jlast && m[p + nn] == 0 && mc + m[p + nn] == 1)
+            r = r - edge_u(x, p + nn, nn, cff);
+    } else {
+        return;  // beyond the last visited column: untouched
+    }
+    y[p] = r;
+}
+
+// The routine's intent(out) 'total': the terms added in the loop's order,
+// one after the other as the Fortran adds them (one CTA walks the rows; each
+// chunk of a row compacts its terms in column order, then one thread adds
+// them), so the value is the reference's to the last bit.
+constexpr int NS_THREADS = 1024;
+
+__global__ void __launch_bounds__(NS_THREADS)
+    k_noslip_total(const int8_t *m, const double *x, double cff, int nh, int mm, int nn,
+                   double *total) {
+    __shared__ double terms[2 * NS_THREADS];
+    __shared__ int wbase[NS_THREADS / 32];
+    __shared__ int nterms;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int ilast = nn - nh;
+    double acc = 0.;  // thread 0's running sum
+    for (int j = nh; j <= mm - nh; j++) {
+        for (int c0 = nh; c0 <= ilast; c0 += NS_THREADS) {
+            const int i = c0 + t;
+            double a = 0., b = 0.;
+            int na = 0, nb = 0;
+            if (i <= ilast) {
+                const size_t p = off(j, i, nn);
+                const int mc = m[p];
+                if (m[p - 1] + mc == 1) {
+                    const double v = edge_v(x, p, nn, cff);
+                    a = mc != 0 ? -v : v;
+                    na = 1;
+                }
+                if (m[p - nn] + mc == 1) {
+                    const double u = edge_u(x, p, nn, cff);
+                    b = mc != 0 ? u : -u;
+                    nb = 1;
+                }
+            }
+            const int cnt = na + nb;
+            int s = cnt;  // inclusive scan over the warp
+            for (int o = 1; o < 32; o <<= 1) {
+                const int up = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += up;
+            }
+            if (lane == 31) wbase[w] = s;
+            __syncthreads();
+            if (w == 0) {
+                const int own = wbase[lane];
+                int e = own;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int up = __shfl_up_sync(0xffffffffu, e, o);
+                    if (lane >= o) e += up;
+                }
+                wbase[lane] = e - own;
+                if (lane == 31) nterms = e;
+            }
+            __syncthreads();
+            int pos = wbase[w] + s - cnt;
+            if (na) terms[pos++] = a;
+            if (nb) terms[pos] = b;
+            __syncthreads();
+            if (t == 0)
+                for (int q = 0; q < nterms; q++) acc = acc + terms[q];
+            __syncthreads();
+        }
+    }
+    if (t == 0) *total = acc;
+}
+
+int launch_noslip_dropin(const int8_t *msk, const double *x, double *y, double dx, double dy,
+                         int nh, int m, int n, double *total, cudaStream_t s) {
+    if (!msk || !x || !y) {
+        set_error("computenoslipsourceterm: null array");
+        return ERR_ARG;
+    }
+    if (nh < 2 || m < 2 * nh + 1 || n < 2 * nh + 1) {
+        set_error("computenoslipsourceterm: nh=%d with (m, n) = (%d, %d)", nh, m, n);
+        return nh < 2 ? ERR_NH : ERR_SHAPE;
+    }
+    const double cff = 1. / (2 * dx * dy);
+    dim3 b(32, 8);
+    k_noslip_dropin<<<grid2d(m - nh + 1, n, b), b, 0, s>>>(msk, x, y, cff, nh, m, n);
+    int st = launch_status("computenoslipsourceterm");
+    if (st || !total) return st;
+    k_noslip_total<<<1, NS_THREADS, 0, s>>>(msk, x, cff, nh, m, n, total);
+    return launch_status("computenoslipsourceterm total");
+}
+
 // source -= (sum/bcarea)*mskbc over the whole array
 __global__ void k_noslip_mean(double *src, const double *sum, const int8_t *mskbc, double bcarea,
                               size_t n) {

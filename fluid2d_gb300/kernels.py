@@ -10,7 +10,8 @@ place), so Fluid2d's callers need no change:
                      (core/fortran_fluxes.f90, exported there as adv_upwind,
                      adv_centered -- see fluid2d_gb300/f2py_compat)
 * fortran_operators: computeorthogradient, celltocorner, cornertocell,
-                     add_diffusion, add_torque  (core/fortran_operators.f90)
+                     add_diffusion, add_torque, computenoslipsourceterm
+                     (core/fortran_operators.f90)
 * fortran_diag:      computedotprod, computemax, computesum,
                      computesumandnorm, computenormmaxu, computekemaxu,
                      computekemaxuv, computekewithpsi  (core/fortran_diag.f90)
@@ -242,6 +243,18 @@ def add_torque(msk, buoy, dx, nh, gravity, domega):
     _call("f2d_add_torque", M.ptr, B.ptr, float(dx), int(nh), float(gravity), W.ptr, m, n,
           stream_handle())
     W.done()
+
+
+def computenoslipsourceterm(msk, x, y, dx, dy, nh):
+    """core/fortran_operators.f90:221-277 -> total (y updated in place)"""
+    _same(msk, x, y)
+    m, n = _mn(msk)
+    M, X, Y = _i8(msk), _f64(x), _f64(y, True)
+    out = _scalars(1)
+    _call("f2d_computenoslipsourceterm", M.ptr, X.ptr, Y.ptr, float(dx), float(dy), int(nh), m,
+          n, out.data_ptr(), stream_handle())
+    Y.done()
+    return _host(out)[0]
 
 
 # ---------------------------------------------------------------- diagnostics

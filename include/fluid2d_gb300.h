@@ -95,6 +95,14 @@ int f2d_add_diffusion(const int8_t *msk, const double *trac, double dx, int nh, 
  * core/operators.py:312 */
 int f2d_add_torque(const int8_t *msk, const double *buoy, double dx, int nh, double gravity,
                    double *domega, int m, int n, void *stream);
+/* core/fortran_operators.f90:221-277 total=computenoslipsourceterm(msk,x,y,dx,dy,nh),
+ * called from core/operators.py:256 (rhs_noslip).  y is written wherever the
+ * Fortran loop writes it (rows 1..m-nh+1 in 1-based terms, including the
+ * scattered terms in row and column nh); other cells keep their values.
+ * total: DEVICE pointer to one double, the intent(out) sum of the terms in
+ * the Fortran's order (bit-identical), or NULL to skip it.  nh >= 2. */
+int f2d_computenoslipsourceterm(const int8_t *msk, const double *x, double *y, double dx,
+                                double dy, int nh, int m, int n, double *total, void *stream);
 
 /* ------------------------------------------------ fortran_diag --------- */
 /* The f2py intent(out) scalars are written to the DEVICE array "out".

@@ -68,36 +68,98 @@ def _module(name, **attrs):
     return m
 
 
+# the f2py modules the reference imports by bare name (install.sh:44-46) and,
+# for each of their routines, the oracle function that stands in for it
+F2PY_NAMES = {
+    'fortran_advection': {'adv_upwind': 'adv_upwind', 'adv_centered': 'adv_centered'},
+    'fortran_fluxes': {'adv_upwind': 'adv_upwind_flux', 'adv_centered': 'adv_centered_flux'},
+    'fortran_operators': {n: n for n in (
+        'computeorthogradient', 'celltocorner', 'cornertocell', 'add_diffusion', 'add_torque',
+        'computenoslipsourceterm')},
+    'fortran_diag': {n: n for n in (
+        'computedotprod', 'computemax', 'computesum', 'computesumandnorm', 'computenormmaxu',
+        'computekemaxu', 'computekemaxuv', 'computekewithpsi')},
+    'gmg.fortran_multigrid': {n: n for n in (
+        'smoothtwicewitha', 'smoothoncewitha', 'smoothtridiag', 'computeresidualwitha',
+        'fillhalo', 'interpolate', 'restrict', 'coarsenmatrix', 'computenorm',
+        'computeinner')},
+}
+
+
+def arg_kind(a):
+    """How an argument is passed: dtype, rank and memory order of an array
+    (C, F or S for strided), 'scalar' for a number, else the type name."""
+    if isinstance(a, np.ndarray):
+        order = 'C' if a.flags.c_contiguous else ('F' if a.flags.f_contiguous else 'S')
+        return '%s:%dd:%s' % (a.dtype.str, a.ndim, order)
+    if isinstance(a, (int, float, np.integer, np.floating)):
+        return 'scalar'
+    return type(a).__name__
+
+
+class CallTrace(object):
+    """Records every kernel call made through ``traced`` functions as
+    (module.routine, argument kinds)."""
+
+    def __init__(self):
+        self.calls = []
+        self.on = True
+
+    def traced(self, qualname, fn):
+        def call(*args):
+            if self.on:
+                self.calls.append((qualname, tuple(arg_kind(a) for a in args)))
+            return fn(*args)
+        call.__name__ = getattr(fn, '__name__', qualname)
+        return call
+
+    def forms(self):
+        """the distinct calls as text: routine(kind, kind, ...)"""
+        return sorted(set(call_form(c) for c in self.calls))
+
+    def digest(self):
+        """sha256 of the whole call sequence, one call per line"""
+        import hashlib
+        return hashlib.sha256('\n'.join(call_form(c) for c in self.calls).encode()).hexdigest()
+
+
+def call_form(call):
+    return '%s(%s)' % (call[0], ', '.join(call[1]))
+
+
+TRACE = CallTrace()
+TRACE.on = False
+
+
+def kernel_set(modules, trace=None):
+    """A namespace with the oracle's names over the routines of the given
+    f2py-named modules ({module name: module}), optionally traced."""
+    ns = types.SimpleNamespace()
+    for mod, names in F2PY_NAMES.items():
+        m = modules[mod]
+        for routine, oname in names.items():
+            if not hasattr(m, routine):
+                continue
+            fn = getattr(m, routine)
+            if trace is not None:
+                fn = trace.traced(mod + '.' + routine, fn)
+            setattr(ns, oname, fn)
+    return ns
+
+
 def install(core_dir):
-    """Make ``core_dir`` (the reference's core/) importable over the oracle."""
+    """Make ``core_dir`` (the reference's core/) importable over the oracle.
+    Kernel calls are recorded in ``TRACE`` while ``TRACE.on`` is set."""
     if not hasattr(np, 'NaN'):
         np.NaN = np.nan
     mpi = _module('mpi4py.MPI', COMM_WORLD=_Comm(), SUM='sum', MAX='max', MIN='min')
     sys.modules['mpi4py'] = _module('mpi4py', MPI=mpi)
     sys.modules['mpi4py.MPI'] = mpi
     sys.modules['netCDF4'] = _module('netCDF4', Dataset=None)
-    sys.modules['fortran_advection'] = _module(
-        'fortran_advection', adv_upwind=K.adv_upwind, adv_centered=K.adv_centered)
-    sys.modules['fortran_fluxes'] = _module(
-        'fortran_fluxes', adv_upwind=K.adv_upwind_flux, adv_centered=K.adv_centered_flux)
-    sys.modules['fortran_operators'] = _module(
-        'fortran_operators',
-        computeorthogradient=K.computeorthogradient, celltocorner=K.celltocorner,
-        cornertocell=K.cornertocell, add_diffusion=K.add_diffusion,
-        add_torque=K.add_torque, computenoslipsourceterm=K.computenoslipsourceterm)
-    sys.modules['fortran_diag'] = _module(
-        'fortran_diag',
-        computedotprod=K.computedotprod, computemax=K.computemax,
-        computesum=K.computesum, computesumandnorm=K.computesumandnorm,
-        computenormmaxu=K.computenormmaxu, computekemaxu=K.computekemaxu,
-        computekemaxuv=K.computekemaxuv, computekewithpsi=K.computekewithpsi)
-    sys.modules['gmg.fortran_multigrid'] = _module(
-        'gmg.fortran_multigrid',
-        smoothtwicewitha=K.smoothtwicewitha, smoothoncewitha=K.smoothoncewitha,
-        smoothtridiag=K.smoothtridiag, computeresidualwitha=K.computeresidualwitha,
-        fillhalo=K.fillhalo, interpolate=K.interpolate, restrict=K.restrict,
-        coarsenmatrix=K.coarsenmatrix, computenorm=K.computenorm,
-        computeinner=K.computeinner)
+    for mod, names in F2PY_NAMES.items():
+        sys.modules[mod] = _module(mod, **{
+            routine: TRACE.traced(mod + '.' + routine, getattr(K, oname))
+            for routine, oname in names.items()})
     core_dir = os.path.abspath(core_dir)
     if core_dir not in sys.path:
         sys.path.insert(0, core_dir)

@@ -36,6 +36,15 @@ except ImportError:  # imported with oracle/ itself on sys.path
     import oracle as K
 
 
+def use_kernels(kernels):
+    """Run the sequencing over another kernel set with the oracle's names
+    (the tests pass the GPU drop-in modules of fluid2d_gb300.f2py_compat,
+    mapped by ``oracle.refshim.F2PY_NAMES``); returns the previous set."""
+    global K
+    old, K = K, kernels
+    return old
+
+
 class Param(object):
     """The defaults of core/defaults.json that the hot path reads."""
 
@@ -171,7 +180,9 @@ class Level(object):
         self.msk[coef <= 0.5] = 0
         A = K.coarsenmatrix(prev.A, prev.msk, self.msk, prev.nh)
         for k in range(9):
-            c = A[:, :, k].copy()
+            # each plane's halo is filled through a strided view of A, as
+            # core/gmg/level.py:323-327 passes it
+            c = A[:, :, k].squeeze()
             self.fill(c)
             A[:, :, k] = c
         self.A = A
@@ -380,6 +391,16 @@ class Operators(object):
         self.last_solve = (0, 0.)
         self.msknoslip = grid.msknoslip
         self.set_boundary_msk()
+        # the thermal-wind coefficients every model computes at set-up
+        # (core/operators.py:132-145); unused by these models, kept so that the
+        # kernel calls are the reference's, call for call
+        for a, b in (((slice(1, -1), slice(2, None)), (slice(1, -1), slice(0, -2))),
+                     ((slice(2, None), slice(1, -1)), (slice(0, -2), slice(1, -1)))):
+            coef = 0. * np.zeros_like(self.msk)
+            coef[1:-1, 1:-1] = self.msk[a] + self.msk[b]
+            coef[coef < 2] = 0.
+            coef[coef == 2] = 0.5
+            self.fill_halo(coef)
 
     def set_boundary_msk(self):
         """core/operators.py:157-184: the cells along the solid boundary."""
@@ -982,6 +1003,38 @@ def loop(model, param, tend, dt0, out, t=0., kt=0, exacthistime=True,
             reason = 'blowup'
             break
     return t, kt, dts, reason
+
+
+def fixture_param(z):
+    """The Param of a tests/golden step fixture (its recorded overrides)."""
+    import ast
+    prm = ast.literal_eval(str(z["params"][0]))
+    kw = {k: v for k, v in prm.items() if k not in ("model", "nx", "ny", "Lx", "Ly",
+                                                    "geometry", "gravity")}
+    return Param(modelname=prm["model"], nx=prm["nx"], ny=prm["ny"], Lx=prm["Lx"],
+                 Ly=prm["Ly"], geometry=prm["geometry"], gravity=prm["gravity"], **kw)
+
+
+def from_fixture(z, **kw):
+    """A model on the initial state of a tests/golden step fixture, as the
+    fixture's run had it after its set-up: mask, no-slip walls, islands'
+    arrays, the state, the diagnostics (no initial inversion: the state
+    already holds its result).  ``kw`` overrides Param attributes (another
+    time scheme, ...).  Returns (param, model)."""
+    p = fixture_param(z)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    g = Grid(p)
+    g.msk = np.array(z["msk"])
+    if "msknoslip" in z:
+        g.msknoslip = np.array(z["msknoslip"])
+    g.finalize_msk()
+    M = MODELS[p.modelname](p, grid=g)
+    if "rhsp" in z:
+        M.set_islands(z["rhsp"], z["psi_island"])
+    M.state[...] = z["states"][0]
+    M.diagnostics()
+    return p, M
 
 
 def from_workload(wl, **kw):

@@ -13,6 +13,18 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: long-running parity case")
 
 
+# where CPU tests look for the reference's core/ sources (read-only); tests
+# that need them skip themselves when they are absent (on the GPU machine)
+REFERENCE_CORE = os.environ.get("FLUID2D_CORE", "/root/reference/core")
+
+
+def reference_core(marker="fluid2d.py"):
+    """The reference's core/ directory, or skip the calling test."""
+    if not os.path.exists(os.path.join(REFERENCE_CORE, marker)):
+        pytest.skip("reference sources not present")
+    return REFERENCE_CORE
+
+
 def gpu_available():
     try:
         import torch

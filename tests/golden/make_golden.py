@@ -27,8 +27,6 @@ from fluid2d_gb300 import workloads as W  # noqa: E402
 from oracle import refshim, stepper  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# where the reference sources are read from (read-only)
-DEFAULT_CORE = "/root/reference/core"
 
 
 def channel_with_islands(model="euler", nx=64, ny=32, seed=9):
@@ -378,7 +376,11 @@ def main_fluxes(core, steps=2):
 
 
 if __name__ == "__main__":
-    core = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLUID2D_CORE", DEFAULT_CORE)
+    # the reference's core/ directory (read-only), from the command line or
+    # the FLUID2D_CORE environment variable
+    core = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FLUID2D_CORE")
+    if not core:
+        sys.exit("usage: make_golden.py <reference core/ directory> (or FLUID2D_CORE)")
     main(core)
     main_loop(core)
     main_fluxes(core)

@@ -157,6 +157,32 @@ def test_operators(gk, variant, m, n, geom, islands, seed):
 
 
 @pytest.mark.parametrize("m,n,geom,islands,seed", cases())
+def test_computenoslipsourceterm(gk, variant, m, n, geom, islands, seed):
+    """core/fortran_operators.f90:221-277 as core/operators.py:256 calls it:
+    the whole output array (the cells its loop writes, its scatters into row
+    and column nh, the untouched rest) and the returned total, which the
+    Fortran sums in loop order (bit-identical in the exact build)."""
+    msk = C.mask(m, n, geom, islands + 1, seed)
+    psi = C.field(m, n, seed + 5)
+    dx, dy = 1. / (n - 6), 1.3 / (m - 6)
+    y0 = C.field(m, n, seed + 6)
+    yr = y0.copy()
+    tr = K().computenoslipsourceterm(msk, psi, yr, dx, dy, 3)
+    yg = cuda(y0)
+    tg = gk.computenoslipsourceterm(cuda(msk), cuda(psi), yg, dx, dy, 3)
+    check(host(yg), yr, variant)
+    if variant == "exact":
+        assert tg == tr
+    else:
+        assert abs(tg - tr) <= 1e-12 * max(np.abs(yr).sum(), 1e-300)
+    # numpy arrays (the reference's own call) take the host-buffer path
+    yh = y0.copy()
+    th = gk.computenoslipsourceterm(msk, psi, yh, dx, dy, 3)
+    check(yh, yr, variant)
+    assert th == tg
+
+
+@pytest.mark.parametrize("m,n,geom,islands,seed", cases())
 def test_diagnostics(gk, variant, m, n, geom, islands, seed):
     msk = C.mask(m, n, geom, islands, seed)
     u, v, x = C.field(m, n, seed), C.field(m, n, seed + 1), C.field(m, n, seed + 2)

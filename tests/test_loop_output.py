@@ -31,10 +31,8 @@ def make_golden():
 
 
 def reference_core():
-    core = os.environ.get("FLUID2D_CORE", make_golden().DEFAULT_CORE)
-    if not os.path.exists(os.path.join(core, "fluid2d.py")):
-        pytest.skip("reference sources not present")
-    return core
+    from tests.conftest import reference_core as core
+    return core()
 
 
 def load_loop(path):

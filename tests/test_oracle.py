@@ -79,9 +79,8 @@ def test_reference_python_pin():
         "make_golden", os.path.join(HERE, "golden", "make_golden.py"))
     mg = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mg)
-    core = os.environ.get("FLUID2D_CORE", mg.DEFAULT_CORE)
-    if not os.path.exists(os.path.join(core, "operators.py")):
-        pytest.skip("reference sources not present")
+    from tests.conftest import reference_core
+    core = reference_core("operators.py")
     from oracle import stepper
     wl, kw = mg.cases()["euler_closed_32"]
     R = mg.reference_model(core, wl, kw)

@@ -210,6 +210,8 @@ SIGNATURES.update({
     "f2d_model_step_graph": [_P, _I, _P],
     "f2d_model_set_dt": [_P, _D],
     "f2d_model_solve_stats": [_P, _PI, _PDd, _PI],
+    "f2d_model_status": [_P, _I, _PI, _P],
+    "f2d_models_status": [ctypes.POINTER(ctypes.c_void_p), _I, _I, _PI, _P],
     "f2d_model_probe": [_P, _I, _PI, _PDd],
     "f2d_model_bytes": [_P, ctypes.POINTER(ctypes.c_size_t)],
     "f2d_model_graph_kernels": [_P, _PI],

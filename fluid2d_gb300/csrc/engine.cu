@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <mutex>
 #include <vector>
 
 #include "../../include/fluid2d_gb300.h"
@@ -762,7 +763,10 @@ static const char *VARNAMES[3][6] = {
     {"vorticity", "psi", "u", "v", "buoyancy", "banom"},
     {"pv", "psi", "u", "v", "pvanom", "vorticity"}};
 static const int NVAR[3] = {5, 6, 6};
-static const int NDIAG[3] = {8, 8, 6};
+__host__ __device__ constexpr int ndiag_of(int kind) { return kind == 2 ? 6 : 8; }
+static const int NDIAG[3] = {ndiag_of(0), ndiag_of(1), ndiag_of(2)};
+// status word bits (include/fluid2d_gb300.h F2D_STATUS_*)
+enum { STATUS_NONFINITE = 1, STATUS_BLOWUP = 2, STATUS_DIVERGED = 4, STATUS_BAD_DT = 8 };
 
 struct DiagArgs {
     int kind;
@@ -775,6 +779,9 @@ struct DiagArgs {
     double *part;      // partials
     double *out;       // NDIAG values
     int nr;            // partial kernel: rows per block; final kernel: partial blocks
+    int *status;              // the model's status word (F2D_STATUS_* bits, sticky)
+    const SolveState *solve;  // the last full solve's state (divergence)
+    const double *dt;         // the step's dt
 };
 
 // diagnostics of core/euler.py:185-223, core/boussinesq.py:123-153,
@@ -900,6 +907,20 @@ F2D_DEV void diag_final_body(const DiagArgs &a, const VB) {
         a.out[4] = ape / area;
         a.out[5] = (ke + ape) / area;
     }
+    if (a.status) {
+        // what stops the reference's run, per instance: a blow-up
+        // (maxspeed > 1e3, core/fluid2d.py:309-314), a diverged solve
+        // (core/gmg/hierarchy.py:182-188), and any non-finite value: a NaN or
+        // Inf anywhere in u, v or the tracers reaches these sums
+        int st = 0;
+        bool finite = isfinite(acc[0]) && isfinite(acc[1]);
+        for (int k = 0; k < ndiag_of(a.kind); k++) finite = finite && isfinite(a.out[k]);
+        if (!finite) st |= STATUS_NONFINITE;
+        if (maxu > 1e3) st |= STATUS_BLOWUP;
+        if (a.solve && a.solve->status == ERR_DIVERGED) st |= STATUS_DIVERGED;
+        if (a.dt && !(isfinite(*a.dt) && *a.dt > 0.)) st |= STATUS_BAD_DT;
+        if (st) *a.status |= st;
+    }
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_diag_final(DiagArgs a) {
@@ -1012,6 +1033,7 @@ struct Model {
     Arena mem;
     int8_t *msk = nullptr, *mskp = nullptr, *ones = nullptr;
     double *X, *D[3], *S1, *S2, *B, *cst, *advc, *dt, *diag, *pvback, *bref, *part;
+    int *status = nullptr;  // F2D_STATUS_* bits, set by the diagnostics, sticky
     // mixed form: float stage states, float tendencies, float split constants
     float *Xf = nullptr, *S1f = nullptr, *S2f = nullptr, *Df[3] = {nullptr, nullptr, nullptr};
     float *dtf = nullptr;
@@ -1125,6 +1147,16 @@ int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t 
         set_error("model: unknown kind %d", kind);
         return ERR_ARG;
     }
+    if (d->nx < 4 || d->ny < 4 || d->nx > (1 << 15) || d->ny > (1 << 15) ||
+        !(d->Lx > 0. && d->Ly > 0.) || !isfinite(d->Lx) || !isfinite(d->Ly)) {
+        set_error("model: bad grid nx=%d ny=%d Lx=%g Ly=%g", d->nx, d->ny, d->Lx, d->Ly);
+        return ERR_SHAPE;
+    }
+    if (d->order < 1 || d->order > 6 || d->precision < 0 || d->precision > 1 ||
+        !(d->dt > 0.) || !isfinite(d->dt)) {
+        set_error("model: bad order %d, precision %d or dt %g", d->order, d->precision, d->dt);
+        return ERR_ARG;
+    }
     nvar = NVAR[kind];
     nv = d->nx + 2 * NH;
     mv = d->ny + 2 * NH;
@@ -1157,7 +1189,7 @@ int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t 
            o_cst = mem.add(8 * 8), o_advc = mem.add(sizeof(SplitConst)), o_dt = mem.add(8),
            o_diag = mem.add(8 * 8),
            o_pvb = mem.add(kind == M_QG ? pl * 8 : 8), o_bref = mem.add(kind == M_BOUSSINESQ ? pl * 8 : 8),
-           o_part = mem.add(8 * RED_MAX_BLOCKS * 8);
+           o_part = mem.add(8 * RED_MAX_BLOCKS * 8), o_status = mem.add(16);
     const bool mixed = d->precision != 0;
     size_t o_f[6] = {0, 0, 0, 0, 0, 0}, o_advf = 0, o_dtf = 0;
     if (mixed) {
@@ -1192,6 +1224,8 @@ int Model::create(const f2d_model_desc *d, const int8_t *msk_host, cudaStream_t 
     pvback = mem.at<double>(o_pvb);
     bref = mem.at<double>(o_bref);
     part = mem.at<double>(o_part);
+    status = mem.at<int>(o_status);
+    TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int), s), "status"));
     TRY(cuda_status(cudaMemcpyAsync(msk, msk_host, pl, cudaMemcpyHostToDevice, s), "msk"));
     TRY(cuda_status(cudaMemcpyAsync(mskp, mp.data(), pl, cudaMemcpyHostToDevice, s), "mskp"));
     // cst (core/operators.py:99-119)
@@ -1443,6 +1477,9 @@ int Model::diagnostics(cudaStream_t s) {
     a.area = area;
     a.part = part;
     a.out = diag;
+    a.status = status;
+    a.solve = gmg.solve_state;
+    a.dt = dt;
     int rows = mv - 2 * NH;
     int nb = reduce_blocks(rows);
     int rpb = (rows + nb - 1) / nb;
@@ -2399,6 +2436,60 @@ int f2d_model_graph_kernels(void *model, int *nkernels) {
         if (t == cudaGraphNodeTypeKernel) k++;
     }
     *nkernels = k;
+    return OK;
+}
+
+int f2d_model_status(void *model, int clear, int *status, void *stream) {
+    Model *M = (Model *)model;
+    if (!M || !status) {
+        set_error("f2d_model_status: null argument");
+        return ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int v = 0;
+    TRY(cuda_status(cudaMemcpyAsync(&v, M->status, sizeof(int), cudaMemcpyDeviceToHost, s),
+                    "status read"));
+    if (clear) TRY(cuda_status(cudaMemsetAsync(M->status, 0, sizeof(int), s), "status clear"));
+    TRY(cuda_status(cudaStreamSynchronize(s), "status sync"));
+    *status = v;
+    return OK;
+}
+
+// the status words of many models with one synchronisation: every word is
+// copied into a pinned host buffer owned by the library, then the stream is
+// synchronised once
+int f2d_models_status(void **models, int n, int clear, int *status, void *stream) {
+    if (n < 0 || (n > 0 && (!models || !status))) {
+        set_error("f2d_models_status: bad argument");
+        return ERR_ARG;
+    }
+    static std::mutex mu;
+    static int *pinned = nullptr;
+    static int cap = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (n > cap) {
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        cap = 0;
+        const int want = n < 1024 ? 1024 : n;
+        TRY(cuda_status(cudaHostAlloc((void **)&pinned, want * sizeof(int), cudaHostAllocDefault),
+                        "status buffer"));
+        cap = want;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int k = 0; k < n; k++) {
+        Model *M = (Model *)models[k];
+        if (!M) {
+            set_error("f2d_models_status: null model %d", k);
+            return ERR_ARG;
+        }
+        TRY(cuda_status(cudaMemcpyAsync(pinned + k, M->status, sizeof(int),
+                                        cudaMemcpyDeviceToHost, s), "status read"));
+        if (clear)
+            TRY(cuda_status(cudaMemsetAsync(M->status, 0, sizeof(int), s), "status clear"));
+    }
+    TRY(cuda_status(cudaStreamSynchronize(s), "status sync"));
+    for (int k = 0; k < n; k++) status[k] = pinned[k];
     return OK;
 }
 

@@ -107,6 +107,26 @@ class Gmg(object):
             pass
 
 
+# status word bits (include/fluid2d_gb300.h F2D_STATUS_*)
+STATUS_NAMES = {1: "non-finite values", 2: "blow-up (maxspeed > 1e3)",
+                4: "multigrid solve diverged", 8: "bad time step"}
+
+
+def status_text(bits):
+    return ", ".join(v for k, v in sorted(STATUS_NAMES.items()) if bits & k) or "ok"
+
+
+def statuses(models, clear=False):
+    """The status words of many models, read with one synchronisation."""
+    if not models:
+        return []
+    arr = (ctypes.c_void_p * len(models))(*[m.h.value for m in models])
+    out = (ctypes.c_int * len(models))()
+    _lib.call("f2d_models_status", arr, len(models), int(bool(clear)), out, _stream(),
+              variant=models[0].variant)
+    return list(out)
+
+
 class _Var(object):
     def __init__(self, state, names):
         self.state = state
@@ -248,6 +268,13 @@ class Model(object):
     @property
     def cells(self):
         return self.desc.nx * self.desc.ny
+
+    def status(self, clear=False):
+        """The device status word (STATUS_* bits; 0 = healthy), read
+        synchronously on the current stream; cleared afterwards if asked."""
+        v = ctypes.c_int()
+        self._call("f2d_model_status", self.h, int(bool(clear)), ctypes.byref(v), _stream())
+        return v.value
 
     def solve_stats(self):
         nite, res, st = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
@@ -471,6 +498,7 @@ class Ensemble(object):
         self.models = list(models)
         self.streams = [torch.cuda.Stream() for _ in range(max(1, nstreams))]
         self.batch = None
+        self.failed = []  # (model, status bits) of retired instances
         if batched:
             self.build_batch(groups, policy)
 
@@ -539,8 +567,38 @@ class Ensemble(object):
     def cells(self):
         return sum(m.cells for m in self.models)
 
-    def run(self, nsteps, lockstep=False):
-        """Advance every instance by nsteps (asynchronous)."""
+    def retire_failed(self):
+        """Read every instance's status word (synchronous).  Instances whose
+        run failed -- a non-finite value, a blow-up (maxspeed > 1e3,
+        core/fluid2d.py:309-314), a diverged solve -- leave the ensemble:
+        their graphs no longer run (batched launches are merged again without
+        them) and they go to ``failed`` with their status bits.  The other
+        instances never shared data with them and go on unchanged.  Returns
+        the instances retired now."""
+        now = list(zip(self.models, statuses(self.models)))
+        bad = [(m, st) for m, st in now if st]
+        if not bad:
+            return []
+        self.failed.extend(bad)
+        gone = set(id(m) for m, _ in bad)
+        self.models = [m for m in self.models if id(m) not in gone]
+        if self.batch is not None:
+            args = getattr(self, "_batch_args", (1, 1, False))
+            self.free_batch()
+            if self.models:
+                self.build_batch(*args)
+        return bad
+
+    def run(self, nsteps, lockstep=False, check=False):
+        """Advance every instance by nsteps (asynchronous unless ``check``:
+        then the instances that failed are retired, see retire_failed, and
+        returned)."""
+        self._run(nsteps, lockstep)
+        return self.retire_failed() if check else []
+
+    def _run(self, nsteps, lockstep=False):
+        if not self.models:
+            return
         cur = torch.cuda.current_stream()
         if self.batch is not None:
             streams = self.streams[:len(self.batch)]

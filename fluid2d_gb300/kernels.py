@@ -379,8 +379,9 @@ def restrict(msk2, x1, nh, x2):
 def coarsenmatrix(Afine, msk1, msk2, nh):
     """core/gmg/fortran_multigrid.f90:706-811 -> Acoarse (m2, n2, 9)
 
-    Returned in the reference layout: a numpy array for numpy inputs, else a
-    CUDA tensor view (m2, n2, 9).  Cells the Fortran does not write are 0.
+    Returned in the reference layout: a C-ordered numpy array for numpy
+    inputs, else a CUDA tensor view (m2, n2, 9).  Cells the Fortran does not
+    write are 0.
     """
     m1, n1 = _mn(msk1)
     m2, n2 = _mn(msk2)
@@ -391,7 +392,7 @@ def coarsenmatrix(Afine, msk1, msk2, nh):
           out.data_ptr(), stream_handle())
     res = out.permute(1, 2, 0)
     if isinstance(msk2, np.ndarray):
-        return res.cpu().numpy()
+        return np.ascontiguousarray(res.cpu().numpy())
     return res
 
 

@@ -1,9 +1,15 @@
 """Serving loop: simulations arrive as requests and are stepped together.
 
 A request is (model, grid, mask, initial fields, step count).  The server
-keeps a FIFO of arrived requests and admits the head whenever its estimated
-device memory fits in the HBM budget beside the running ones; every admitted
-simulation keeps its state resident on the GPU.  Each tick advances every
+keeps a FIFO of arrived requests and admits the head whenever its device
+memory fits in the HBM budget beside the running ones -- estimated from the
+bytes per grid point measured on the models already built (nbytes()), and
+checked against the built model's own nbytes() before it runs; every
+admitted simulation keeps its state resident on the GPU.  A request the
+engine cannot serve (unknown model, bad grid, too large) is rejected with
+its reason; a simulation whose run fails (non-finite values, blow-up,
+diverged solve: the model's device status word, read after every tick) is
+retired alone with its reason, and the others go on unchanged.  Each tick advances every
 running simulation by one step -- its captured step graph replayed on one of
 `nstreams` CUDA streams, so the kernels of different simulations overlap --
 and retires the ones that have done all their steps, which frees memory for
@@ -19,13 +25,33 @@ import time
 import numpy as np
 
 # device bytes per grid point (halo included) of a model and its multigrid
-# hierarchy, measured from the engine's allocations, with a margin
+# hierarchy, with a margin: the first estimate for a (model, precision) whose
+# size the server has not measured yet; afterwards the largest measured
+# nbytes()/point of that kind is used
 BYTES_PER_POINT = {"fp64": 560., "mixed": 760.}
+MODELS = ("euler", "boussinesq", "quasigeostrophic")
 
 
-def estimate_bytes(wl, precision):
+def estimate_bytes(wl, precision, per_point=None):
     pts = (wl["nx"] + 6) * (wl["ny"] + 6)
-    return int(BYTES_PER_POINT[precision] * pts) + (4 << 20)
+    return int((per_point or BYTES_PER_POINT[precision]) * pts) + (4 << 20)
+
+
+def check_request(wl, steps):
+    """Why a request cannot be served (None if it can): unknown model, grid
+    sides that are not integers in [4, 32768], a mask of the wrong shape, a
+    step count below 1."""
+    if wl.get("model") not in MODELS:
+        return "unknown model %r" % (wl.get("model"),)
+    nx, ny = wl.get("nx"), wl.get("ny")
+    if not all(isinstance(v, (int, np.integer)) and 4 <= v <= 32768 for v in (nx, ny)):
+        return "bad grid size %r x %r" % (nx, ny)
+    msk = wl.get("msk")
+    if msk is not None and tuple(np.shape(msk)) != (ny + 6, nx + 6):
+        return "mask shape %s is not (ny+6, nx+6)" % (np.shape(msk),)
+    if not (isinstance(steps, (int, np.integer)) and steps >= 1):
+        return "bad step count %r" % (steps,)
+    return None
 
 
 class Request(object):
@@ -40,6 +66,7 @@ class Request(object):
         self.admitted = None
         self.finished = None
         self.latencies = []
+        self.error = None  # why it was rejected or retired early
 
     @property
     def cells(self):
@@ -61,6 +88,7 @@ class Server(object):
         self.nstreams = nstreams
         self.make_model = make_model or _gpu_make_model
         self.step_models = step_models or _GpuStepper(nstreams).step
+        self.read_status = _read_status
         self.max_active = max_active
         self.clock = clock
         self.on_finish = on_finish
@@ -69,12 +97,24 @@ class Server(object):
         self.active = []
         self.finished = []
         self.rejected = []
+        self.failed = []
         self.ticks = []
+        self.per_point = {}  # measured device bytes per grid point, per model
+
+    def _estimate(self, wl):
+        return estimate_bytes(wl, self.precision, self.per_point.get(wl["model"]))
+
+    def _reject(self, req, why):
+        req.error = why
+        self.rejected.append(req)
+        return False
 
     def submit(self, req):
-        if estimate_bytes(req.wl, self.precision) > self.budget:
-            self.rejected.append(req)  # can never fit
-            return False
+        why = check_request(req.wl, req.steps)
+        if why:
+            return self._reject(req, why)
+        if self._estimate(req.wl) > self.budget:
+            return self._reject(req, "needs more than the HBM budget")  # can never fit
         self.queue.append(req)
         return True
 
@@ -83,12 +123,28 @@ class Server(object):
             if self.max_active is not None and len(self.active) >= self.max_active:
                 break
             req = self.queue[0]
-            need = estimate_bytes(req.wl, self.precision)
+            need = self._estimate(req.wl)
             if self.used + need > self.budget:
                 break
             self.queue.pop(0)
-            req.model = self.make_model(req.wl, self.precision)
-            req.nbytes = max(need, _model_bytes(req.model))
+            try:
+                req.model = self.make_model(req.wl, self.precision)
+            except Exception as exc:  # a request the engine refuses fails alone
+                self._reject(req, "model set-up failed: %s" % exc)
+                continue
+            got = _model_bytes(req.model)
+            if got:
+                # admission on measured sizes: the largest bytes per point seen
+                pp = (got - (4 << 20)) / float((req.wl["nx"] + 6) * (req.wl["ny"] + 6))
+                kind = req.wl["model"]
+                self.per_point[kind] = max(self.per_point.get(kind, 0.), pp)
+            req.nbytes = got or need
+            if self.used + req.nbytes > self.budget:
+                # larger than estimated: back to the head of the queue until
+                # memory frees up
+                req.model = None
+                self.queue.insert(0, req)
+                break
             self.used += req.nbytes
             req.admitted = now
             self.active.append(req)
@@ -99,20 +155,29 @@ class Server(object):
         dt = self.step_models([r.model for r in self.active])
         self.ticks.append((now, len(self.active), sum(r.cells for r in self.active), dt))
         keep = []
-        for r in self.active:
+        status = self.read_status([r.model for r in self.active])
+        for r, bits in zip(self.active, status):
             r.done += 1
             r.latencies.append(dt)
-            if r.done >= r.steps:
-                r.finished = now + dt
+            if bits:
+                # this instance alone leaves: the others share nothing with it
+                r.error = "retired after step %d: %s" % (r.done, _status_text(bits))
+                self._release(r, now + dt)
+                self.failed.append(r)
+            elif r.done >= r.steps:
+                self._release(r, now + dt)
                 if self.on_finish is not None:
                     self.on_finish(r)
-                self.used -= r.nbytes
-                r.model = None  # frees the device memory
                 self.finished.append(r)
             else:
                 keep.append(r)
         self.active = keep
         return dt
+
+    def _release(self, r, when):
+        r.finished = when
+        self.used -= r.nbytes
+        r.model = None  # frees the device memory
 
     def run(self, stream, time_scale=1.0):
         """Serve (arrival, wl, steps) tuples; arrival times are honoured in
@@ -135,15 +200,16 @@ class Server(object):
                     time.sleep(min(wait, 0.05))
             elif self.queue and not self.active:
                 # head cannot be admitted even with nothing running
-                self.rejected.append(self.queue.pop(0))
+                self._reject(self.queue.pop(0), "does not fit the HBM budget alone")
         wall = self.clock() - t0
-        return metrics(self.finished, wall, busy, self.rejected)
+        return metrics(self.finished, wall, busy, self.rejected, self.failed)
 
 
-def metrics(finished, wall, busy, rejected=()):
+def metrics(finished, wall, busy, rejected=(), failed=()):
     lat = np.array([x for r in finished for x in r.latencies]) if finished else np.zeros(1)
     cell_steps = float(sum(r.cells * r.steps for r in finished))
-    return {"requests": len(finished), "rejected": len(rejected), "cell_steps": cell_steps,
+    return {"requests": len(finished), "rejected": len(rejected), "failed": len(failed),
+            "cell_steps": cell_steps,
             "wall_s": wall, "busy_s": busy,
             "cell_steps_per_s": cell_steps / busy if busy > 0 else 0.,
             "cell_steps_per_s_wall": cell_steps / wall if wall > 0 else 0.,
@@ -156,6 +222,20 @@ def _model_bytes(m):
         return int(m.nbytes())
     except Exception:
         return 0
+
+
+def _read_status(models):
+    """Status words of the models (0 = healthy): engine models in one
+    synchronisation, others (host fakes) through their own status()."""
+    from . import engine
+    if models and all(isinstance(m, engine.Model) for m in models):
+        return engine.statuses(models)
+    return [int(m.status()) if hasattr(m, "status") else 0 for m in models]
+
+
+def _status_text(bits):
+    from .engine import status_text
+    return status_text(bits)
 
 
 def _gpu_make_model(wl, precision):

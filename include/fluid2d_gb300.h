@@ -256,6 +256,20 @@ int f2d_model_step(void *model, int nsteps, void *stream);
 int f2d_model_step_graph(void *model, int nsteps, void *stream);
 int f2d_model_set_dt(void *model, double dt);
 int f2d_model_solve_stats(void *model, int *nite, double *res, int *status);
+/* The model's status word: F2D_STATUS_* bits that the diagnostics set after
+ * every step (and after set_psi) and that stay set until cleared -- what
+ * stops the reference's run (core/fluid2d.py:309-314 maxspeed > 1e3,
+ * core/gmg/hierarchy.py:182-188 divergence) plus any non-finite value.
+ * Reads it on `stream` (synchronous), then clears it if `clear`.  Batched
+ * and served runs use it to retire a failing instance alone. */
+#define F2D_STATUS_NONFINITE 1 /* NaN or Inf in the fields (diagnostic sums) */
+#define F2D_STATUS_BLOWUP 2    /* maxspeed > 1e3 */
+#define F2D_STATUS_DIVERGED 4  /* the last full solve diverged */
+#define F2D_STATUS_BAD_DT 8    /* dt not a positive finite number */
+int f2d_model_status(void *model, int clear, int *status, void *stream);
+/* f2d_model_status of n models at once (one synchronisation of `stream`):
+ * status[k] for models[k] */
+int f2d_models_status(void **models, int n, int clear, int *status, void *stream);
 /* Timing probe of the finest-level smoother (one smoothtwicewitha call =
  * the engine's two sweep kernels): enable >= 0 switches it on/off (and drops
  * a captured graph); enable < 0 reads the mean duration in ms over the

@@ -278,17 +278,18 @@ def test_level_tiles_change_nothing_but_launches(eng, precision):
 
 
 def test_fp64_peak_and_profile_step(eng, capsys):
-    """The live float64 FMA peak is a plausible figure for this part, and the
-    profiling module runs an NVTX-bracketed step (single model and batched
-    ensemble)."""
+    """The live float64 FMA peak is a plausible figure for this part, and
+    bench.py's profiling mode runs an NVTX-bracketed step (single model and
+    batched ensemble)."""
     import ctypes
-    from fluid2d_gb300 import _lib, profile_step
+    import bench
+    from fluid2d_gb300 import _lib
     v = ctypes.c_double()
     assert _lib.lib().f2d_fp64_peak(ctypes.byref(v)) == 0
     assert 0.05 < v.value < 100., v.value
-    profile_step.main(["--n", "64", "--coarse-level", "3"])
-    profile_step.main(["--n", "64", "--precision", "mixed", "--no-coarse-operator"])
-    profile_step.main(["--ensemble", "3", "--precision", "mixed", "--groups", "2",
-                       "--coarse-offset", "1", "--balanced"])
+    bench.profile_step(["--n", "64", "--coarse-level", "3"])
+    bench.profile_step(["--n", "64", "--precision", "mixed", "--no-coarse-operator"])
+    bench.profile_step(["--ensemble", "3", "--precision", "mixed", "--groups", "2",
+                        "--coarse-offset", "1", "--balanced"])
     out = capsys.readouterr().out
     assert "coarse operator 0 points" in out and "batched launches per step" in out

@@ -92,3 +92,39 @@ def test_batched_product_with_coarse_operators(precision):
         for v in range(a.shape[0]):
             err = np.abs(a[v] - b[v]).max() / max(1e-300, np.abs(a[v]).max())
             assert err <= 1e-10, (k, v, err)
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_failing_instances_are_retired_alone(batched):
+    """One instance starts with a NaN in its vorticity, another with a
+    velocity beyond the reference's blow-up threshold (maxspeed > 1e3,
+    core/fluid2d.py:309-314): the status words retire exactly those two, and
+    the others go on bit for bit as they do alone (exact build)."""
+    import torch
+    from fluid2d_gb300 import engine, workloads as W
+    wls = W.ensemble(5, seed=24, nmin=64, nmax=192)
+    E = engine.ensemble_from_workloads(wls, batched=batched, groups=2, variant="exact",
+                                       nstreams=4)
+    bad_nan, bad_fast = E.models[1], E.models[3]
+    w = bad_nan.get("vorticity")
+    w[10, 10] = float("nan")
+    bad_fast.get("psi").mul_(1e7)
+    bad_fast.get("u").mul_(1e7)
+    bad_fast.get("v").mul_(1e7)
+    torch.cuda.synchronize()
+    if batched:  # record the batch after the states were changed (no effect on it)
+        E.build_batch(2, 1)
+    gone = E.run(2, check=True)
+    assert sorted(id(m) for m, _ in gone) == sorted([id(bad_nan), id(bad_fast)])
+    bits = {id(m): st for m, st in gone}
+    assert bits[id(bad_nan)] & 1
+    assert bits[id(bad_fast)] & 2
+    assert len(E.models) == 3 and not E.run(2, check=True)
+    torch.cuda.synchronize()
+    keep = [0, 2, 4]
+    for k, m in zip(keep, E.models):
+        alone = engine.ensemble_from_workloads([wls[k]], nstreams=1, variant="exact")
+        alone.models[0].run(4)
+        torch.cuda.synchronize()
+        assert torch.equal(alone.models[0].var.state, m.var.state), k
+        assert m.status() == 0

@@ -1,12 +1,12 @@
 #!/usr/bin/env python
 """Throughput of the Fluid2d time step on GB300: cell-steps/s per RK3 step.
 
-Workload (the headline configuration): Euler 2D decaying turbulence on a
-doubly periodic 1024 x 1024 unit box, random-phase vorticity with
-E(k) ~ k^3 exp(-(k/10)^2), rms 1 (seeded synthetic data: the reference
-publishes no dataset), 5th-order upwind advection, RK3-SSP, multigrid
-Poisson inversion (two V-cycles per inverting stage, full F-cycle solve after
-every step), float64, fixed dt from CFL 0.8 on the initial max|u|.
+Headline workload: Euler 2D decaying turbulence on a doubly periodic
+1024 x 1024 unit box, random-phase vorticity with E(k) ~ k^3 exp(-(k/10)^2),
+rms 1 (seeded synthetic data: the reference publishes no dataset), 5th-order
+upwind advection, RK3-SSP, multigrid Poisson inversion (two V-cycles per
+inverting stage, full F-cycle solve after every step), float64, fixed dt from
+CFL 0.8 on the initial max|u|.
 
 One bench "step" is one iteration of the reference's time loop
 (core/fluid2d.py:237-268): set_dt, model.step (3 RK stages + solve),
@@ -14,7 +14,15 @@ diagnostics.  value = interior cells x steps / device time.  The working set
 (state, RK tendencies, stage states, multigrid hierarchy, ~0.3 GB) is larger
 than the 129 MB L2, so no flush is needed between steps.
 
+The same JSON line carries the other named workloads under "configs":
+the closed 128^2 dipole (200 steps, with its CPU path on one core and on
+every core), the 2048x512 Boussinesq shear layer (1000 steps of the float64
+and the mixed form, the mixed form's error every 100 steps), the
+96-instance batched ensemble (100 steps) and a sample of the served stream
+(requests with U[50, 500] steps, Poisson arrivals at 40/s).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --profile-step [...]      one NVTX-bracketed step for ncu
 
 --impl reference times the reference's own CPU implementation of the path
 (its Fortran kernels restated in C, driven by a restatement of its Python
@@ -45,7 +53,7 @@ NX = NY = 1024
 WORKLOAD = "euler-decaying-turbulence-1024x1024-perio-fp64"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
@@ -55,11 +63,26 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-sample-s", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ensemble-steps", type=int, default=20)
-    ap.add_argument("--served-requests", type=int, default=24)
-    ap.add_argument("--no-extra", action="store_true",
-                    help="skip the ensemble and served-stream measurements")
-    return ap.parse_args()
+    ap.add_argument("--dipole-steps", type=int, default=200)
+    ap.add_argument("--shear-steps", type=int, default=1000)
+    ap.add_argument("--shear-cpu-steps", type=int, default=5)
+    ap.add_argument("--ensemble-steps", type=int, default=100)
+    ap.add_argument("--ensemble-cpu-steps", type=int, default=3)
+    ap.add_argument("--served-requests", type=int, default=200)
+    ap.add_argument("--served-slots", type=int, default=0,
+                    help="requests stepped together at most (0: the budget alone decides)")
+    ap.add_argument("--alone-steps", type=int, default=20,
+                    help="steps timed per request when run alone (the rest extrapolated)")
+    ap.add_argument("--only", default="",
+                    help="comma list of extra measurements to run: "
+                         "mixed,dipole,shear,ensemble,served (default all; 'none')")
+    return ap.parse_args(argv)
+
+
+def wanted(a, key):
+    if not a.only:
+        return True
+    return key in a.only.split(",")
 
 
 def dist_info():
@@ -67,6 +90,32 @@ def dist_info():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def host_info():
+    """CPU model and logical core count of this host."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k = line.split(":")[0].strip().lower()
+                if k in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if not model:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    import platform
+    return {"cpu": model or platform.processor() or "unknown", "arch": platform.machine(),
+            "nproc": os.cpu_count() or 1}
 
 
 # ------------------------------------------------------------------ clocks
@@ -127,24 +176,39 @@ class ClockSampler(object):
 
 
 # ------------------------------------------------------------------ CPU side
-def _cpu_worker(args):
-    """Step the oracle (the reference's CPU path restated) for a time budget."""
-    n, budget, seed = args
-    sys.path.insert(0, ROOT)
+def _workload(kind, n=None, index=None):
     from fluid2d_gb300 import workloads as W
+    if kind == "turbulence":
+        return W.turbulence(n, n, seed=2)
+    if kind == "dipole":
+        return W.dipole(128, 128)
+    if kind == "shear":
+        return W.shear(2048, 512)
+    if kind == "ensemble":
+        return W.ensemble(96, seed=4)[index]
+    raise ValueError(kind)
+
+
+def _cpu_worker(args):
+    """Step the oracle (the reference's CPU path restated, timing build) on
+    one workload, for `steps` steps or until `budget` seconds have passed."""
+    kind, n, index, budget, steps = args
+    os.environ["F2D_ORACLE_VARIANT"] = "timing"
+    sys.path.insert(0, ROOT)
     from oracle import stepper
-    wl = W.turbulence(n, n, seed=2)
+    wl = _workload(kind, n, index)
     p, M = stepper.from_workload(wl)
     dt = 0.8 * min(M.grid.dx, M.grid.dy) / M.diags["maxspeed"]
     t0 = time.perf_counter()
-    steps = 0
+    done = 0
     t = 0.
     while True:
         t = stepper.run(M, p, 1, dt, t=t)
-        steps += 1
-        if time.perf_counter() - t0 >= budget:
+        done += 1
+        el = time.perf_counter() - t0
+        if (steps and done >= steps) or (not steps and el >= budget):
             break
-    return steps, time.perf_counter() - t0
+    return done, time.perf_counter() - t0, wl["nx"] * wl["ny"]
 
 
 # float64 FMA throughput of a GB300 of this pool (independent DFMA chains on
@@ -154,31 +218,53 @@ FP64_PEAK_TFLOPS = 1.20
 SMOOTH_DRAM_BYTES_PER_POINT = (20111360 + 0 + 20073472 + 0) / 1060900.
 
 
-def cpu_baseline(n, budget, cores):
-    """Cell-steps/s of the oracle path on `cores` host processes."""
+def cpu_run(jobs, cores):
+    """Run oracle jobs (see _cpu_worker) on `cores` processes; returns
+    cell-steps/s over the slowest process's wall time and the per-job
+    results.  The pool is started with 'spawn'."""
     from oracle import oracle
     oracle.build()
+    if cores == 1 and len(jobs) == 1:
+        res = [_cpu_worker(jobs[0])]
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(_cpu_worker, jobs)
+    total = sum(d * c for d, _, c in res)
     if cores == 1:
-        steps, wall = _cpu_worker((n, budget, 0))
-        return n * n * steps / wall, "1 process, %d steps of the %dx%d workload in %.1f s" % (
-            steps, n, n, wall)
-    import multiprocessing as mp
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(n, budget, k) for k in range(cores)])
-    wall = time.perf_counter() - t0
-    total = sum(s for s, _ in res)
-    slowest = max(w for _, w in res)
-    return n * n * total / slowest, (
-        "%d processes, each stepping its own %dx%d copy for ~%.0f s (%d steps in total)"
-        % (cores, n, n, budget, total))
+        wall = sum(w for _, w, _ in res)
+    elif len(jobs) <= cores:
+        wall = max(w for _, w, _ in res)  # one job per process, all at once
+    else:
+        # more jobs than processes: the stepping time shared evenly over the
+        # cores (set-up between jobs not counted) -- the CPU's best case
+        wall = sum(w for _, w, _ in res) / cores
+    return total / wall, res
+
+
+def cpu_baseline(n, budget, cores):
+    """Cell-steps/s of the oracle path on `cores` host processes, each on its
+    own copy of the n x n turbulence workload for about `budget` seconds."""
+    val, res = cpu_run([("turbulence", n, None, budget, 0)] * cores, cores)
+    steps = sum(d for d, _, _ in res)
+    if cores == 1:
+        return val, "1 process, %d steps of the %dx%d workload in %.1f s" % (
+            steps, n, n, res[0][1])
+    return val, ("%d processes, each stepping its own %dx%d copy for ~%.0f s (%d steps in total)"
+                 % (cores, n, n, budget, steps))
+
+
+def cpu_descr(cores, sample, val, host):
+    return {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "build": "C restatement of the Fortran, gcc -O3 -ffp-contract=fast (FMA)",
+            "host_cpu": host["cpu"], "host_nproc": host["nproc"]}
 
 
 def run_reference(a, rank, world):
     if rank != 0:
         return
-    cores = os.cpu_count() or 1
+    host = host_info()
+    cores = host["nproc"]
     K, W = a.steps, a.warmup
     # the whole --steps/--warmup run is one bounded sample per core
     val, sample = cpu_baseline(a.n, a.cpu_sample_s, cores)
@@ -187,8 +273,7 @@ def run_reference(a, rank, world):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": "euler-decaying-turbulence-%dx%d-perio-fp64"
                                             % (a.n, a.n), "nx": a.n, "ny": a.n},
-            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+            "cpu_baseline": cpu_descr(cores, sample, val, host),
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -254,14 +339,7 @@ def run_ours(a, rank, world, local):
     value = world * n * n * a.steps / (ms * 1e-3)
     nite, res, st = M.solve_stats()
     diags = M.read_diags()
-
-    # ---- the mixed form on the same workload (FP32 fluxes and multigrid
-    # cycles inside an FP64 defect correction; FP64 state, RK and diagnostics)
-    mixed = None
-    try:
-        mixed = bench_mixed(engine, wl, dt, s0, a, stream, world)
-    except Exception as exc:
-        print("mixed form failed: %s" % exc, file=sys.stderr)
+    nlevs, coarse_level, coarse_points = M.nlevs, M.coarse_level, M.coarse_operator()
 
     # ---- roofline of the dominant kernel (the finest-level smoother, timed
     # with CUDA events around every call inside the replayed step graph)
@@ -275,35 +353,7 @@ def run_ours(a, rank, world, local):
         M.probe(False)
     except Exception as exc:  # keep the bench line even if the probe fails
         print("probe failed: %s" % exc, file=sys.stderr)
-    pts = (n + 6) * (n + 6)
-    # one smoothtwicewitha call reads x, b, msk and writes x: 8+8+1+8 = 25 B/point
-    alg_bytes = 25 * pts
-    import json as _json
-    peaks = {}
-    try:
-        peaks = _json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = alg_bytes / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None
-    # dram__bytes_read.sum + dram__bytes_write.sum of one smoothtwicewitha call
-    # (k_sweep1 + k_sweep2) per grid point, from the ncu capture summarised in
-    # profiles/k_sweep_turbulence_1024_fp64_dram.md (1024^2, 1060900 points)
-    traffic = SMOOTH_DRAM_BYTES_PER_POINT * pts
-    # the same kernel against the float64 pipe, its real bound on this part:
-    # one damped-Jacobi update is 1 mul + 7 fma + 1 sub + 1 mul + 1 fma =
-    # 19 flops, two sweeps per call
-    fp64_flops = 2 * 19 * pts
-    fp64_achieved = fp64_flops / (probe_ms * 1e-3) / 1e12 if probe_ms > 0 else None
-    fp64_peak, fp64_src = FP64_PEAK_TFLOPS, "earlier FMA-chain measurement on this pool"
-    try:
-        import ctypes as _ct
-        from fluid2d_gb300 import _lib as _l
-        _v = _ct.c_double()
-        if _l.lib().f2d_fp64_peak(_ct.byref(_v)) == 0 and _v.value > 0:
-            fp64_peak, fp64_src = _v.value, "f2d_fp64_peak: FMA chains measured live on this GPU"
-    except Exception as exc:
-        print("fp64 peak failed: %s" % exc, file=sys.stderr)
+    roofline = smoother_roofline(n, probe_ms, nprobe)
 
     # ---- e2e through the public API with host buffers: every step uploads
     # the state (Var.state) from pinned memory, steps, reads it back
@@ -332,22 +382,35 @@ def run_ours(a, rank, world, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_val = world * n * n * a.e2e_steps / (e2e_ms * 1e-3)
+    del M
+    torch.cuda.synchronize()
 
-    extra = {}
-    # the ensemble and the served stream tune their own launch structure;
-    # the level kernels go back to their default tiles and block sizes
+    # the other workloads tune their own launch structure; the level kernels
+    # go back to their default tiles and block sizes
     try:
         from fluid2d_gb300 import _lib as _l
         _l.lib().f2d_set_level_tiles(0)
         _l.lib().f2d_set_level_threads(0)
     except Exception as exc:
         print("level tiles reset failed: %s" % exc, file=sys.stderr)
-    if not a.no_extra and rank == 0:
-        for key, fn in (("ensemble", bench_ensemble), ("served", bench_served)):
+    host = host_info()
+    extra = {}
+    if rank == 0:
+        todo = [("mixed", lambda: bench_mixed(engine, wl, dt, s0, a, stream, world)),
+                ("dipole", lambda: bench_dipole(a, host)),
+                ("shear", lambda: bench_shear(a, host)),
+                ("ensemble", lambda: bench_ensemble(a, host)),
+                ("served", lambda: bench_served(a))]
+        for key, fn in todo:
+            if not wanted(a, key):
+                continue
             try:
-                extra[key] = fn(a)
+                extra[key] = fn()
             except Exception as exc:
+                import traceback
+                traceback.print_exc()
                 print("%s failed: %s" % (key, exc), file=sys.stderr)
+            torch.cuda.synchronize()
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -355,7 +418,7 @@ def run_ours(a, rank, world, local):
     cpu = None
     if not a.no_cpu_baseline:
         v, sample = cpu_baseline(n, a.cpu_sample_s, 1)
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+        cpu = cpu_descr(1, sample, v, host)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -363,32 +426,25 @@ def run_ours(a, rank, world, local):
         "data": "synthetic: seeded random-phase vorticity, E(k)~k^3 exp(-(k/10)^2), rms 1",
         "config": {"workload": "euler-decaying-turbulence-%dx%d-perio-fp64" % (n, n),
                    "nx": n, "ny": n, "precision": "fp64", "cuda_graph": True,
-                   "multigrid_levels": M.nlevs, "coarse_cta_from_level": M.coarse_level,
-                   "coarse_operator_points": M.coarse_operator(),
+                   "multigrid_levels": nlevs, "coarse_cta_from_level": coarse_level,
+                   "coarse_operator_points": coarse_points,
                    "level_tiles": {"cta_target": tiles[0], "one_pass_threads": tiles[1]},
                    "solve_iterations_last_step": nite, "solve_residual_last_step": res,
                    "dt": dt, "maxspeed": diags.get("maxspeed"),
                    "l2": "working set > L2 (state, tendencies, hierarchy ~0.3 GB); no flush",
                    "parallelism": "replicas" if world > 1 else "single"},
-        "roofline": {"kernel": "finest-level smoother (smoothtwicewitha: sweep1+sweep2)",
-                     "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic, "launches_probed": nprobe,
-                     "avg_launch_ms": probe_ms,
-                     "alg_bytes_per_launch": alg_bytes,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                     "fp64": {"achieved": fp64_achieved, "peak": fp64_peak,
-                              "unit": "TFLOP/s",
-                              "frac": (fp64_achieved / fp64_peak) if fp64_achieved else None,
-                              "flops_per_launch": fp64_flops, "peak_source": fp64_src}},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": a.e2e_steps},
-        "mixed": mixed,
-        "ensemble": extra.get("ensemble"),
-        "served": extra.get("served"),
         "gpu_launches": kernels_per_step * a.steps,
         "clocks": clk.summary(),
+        "host": host,
+        "mixed": extra.get("mixed"),
+        "configs": {"dipole_128_closed_fp64": extra.get("dipole"),
+                    "shear_2048x512_boussinesq": extra.get("shear"),
+                    "ensemble_96": extra.get("ensemble"),
+                    "served_stream": extra.get("served")},
         "libraries": [os.path.basename(so_path("product"))],
     }
     print(json.dumps(line), flush=True)
@@ -396,10 +452,77 @@ def run_ours(a, rank, world, local):
         dist.destroy_process_group()
 
 
-def bench_mixed(engine, wl, dt, s0, a, stream, world):
-    """Throughput of the mixed form, and its single-step error against the
-    float64 path from the same state (per field, relative L2)."""
+def smoother_roofline(n, probe_ms, nprobe):
+    """The finest-level smoother (one smoothtwicewitha call: the two float64
+    Jacobi sweeps of core/gmg/fortran_multigrid.f90:2-127) against its bound,
+    the float64 pipe: 19 flops per point per sweep (1 mul, 7 fma, 1 sub,
+    1 mul, 1 fma), two sweeps per call, over the call's mean CUDA-event
+    duration inside the replayed step graph; peak = float64 FMA chains
+    measured live on this GPU (f2d_fp64_peak).  Beside it, the same call
+    against HBM: x, b read, x written (8 B each) and the mask (1 B) = 25 B
+    per point, with the DRAM traffic of an ncu capture of the same kernels."""
+    pts = (n + 6) * (n + 6)
+    fp64_flops = 2 * 19 * pts
+    achieved = fp64_flops / (probe_ms * 1e-3) / 1e12 if probe_ms > 0 else None
+    fp64_peak, fp64_src = FP64_PEAK_TFLOPS, "fallback: earlier FMA-chain measurement on this pool"
+    try:
+        import ctypes as _ct
+        from fluid2d_gb300 import _lib as _l
+        _v = _ct.c_double()
+        if _l.lib().f2d_fp64_peak(_ct.byref(_v)) == 0 and _v.value > 0:
+            fp64_peak, fp64_src = _v.value, "measured live: f2d_fp64_peak (float64 FMA chains)"
+    except Exception as exc:
+        print("fp64 peak failed: %s" % exc, file=sys.stderr)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg_bytes = 25 * pts
+    hbm = alg_bytes / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None
+    # dram__bytes_read.sum + dram__bytes_write.sum of one call per grid point
+    # (ncu capture of the 1024^2 turbulence step)
+    traffic = SMOOTH_DRAM_BYTES_PER_POINT * pts
+    return {"kernel": "finest-level smoother (smoothtwicewitha: the two float64 sweeps)",
+            "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": (achieved / fp64_peak) if achieved else None,
+            "flops_per_launch": fp64_flops, "peak_source": fp64_src,
+            "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
+            "launches_probed": nprobe, "avg_launch_ms": probe_ms,
+            "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": (hbm / hbm_peak) if hbm else None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}}
+
+
+def _timed_graph(model, steps, stream):
+    """ms of `steps` graph replays of the model's step (CUDA events)."""
     import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        model.run(steps, graph=True)
+        e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def _rel(a, b):
+    import numpy as np
+    nb = float(np.sqrt((b ** 2).sum()))
+    mb = float(np.abs(b).max())
+    return {"rel_l2": float(np.sqrt(((a - b) ** 2).sum())) / nb if nb > 0 else None,
+            "rel_linf": float(np.abs(a - b).max()) / mb if mb > 0 else None}
+
+
+def bench_mixed(engine, wl, dt, s0, a, stream, world):
+    """Throughput of the mixed form on the headline workload, and its
+    single-step error against the float64 oracle from the oracle's state
+    (per field, relative L2 and L-inf)."""
+    import torch
+    from oracle import stepper
     n = wl["nx"]
     Mm = engine.from_workload(wl, dt=dt, precision="mixed")
     Mm.var.state.copy_(s0)
@@ -411,35 +534,140 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
     with torch.cuda.stream(stream):
         Mm.run(a.warmup, graph=True)
     stream.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        Mm.run(a.steps, graph=True)
-        e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = _timed_graph(Mm, a.steps, stream)
     nite, res, st = Mm.solve_stats()
     del Mm
-    # one step of each form from the same (fresh) state
-    A = engine.from_workload(wl, dt=dt)
-    B = engine.from_workload(wl, dt=dt, precision="mixed")
-    for M in (A, B):
-        M.var.state.copy_(s0)
-        M.diagnostics()
-        M.run(1)
-    torch.cuda.synchronize()
+    # one step of the mixed form and of the oracle from the oracle's state
+    p, O = stepper.from_workload(wl)
+    odt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
+    B = engine.from_workload(wl, dt=odt, precision="mixed")
+    B.var.state.copy_(torch.from_numpy(O.state).cuda())
+    B.diagnostics()
+    stepper.run(O, p, 1, odt)
+    B.run(1)
+    got = B.var.state.cpu().numpy()
     err = {}
-    for k, nm in enumerate(A.var.varname_list):
-        ref = A.var.state[k]
-        nrm = float(torch.linalg.vector_norm(ref))
-        if nrm > 0:
-            err[nm] = float(torch.linalg.vector_norm(B.var.state[k] - ref)) / nrm
+    for k, nm in enumerate(B.var.varname_list):
+        if abs(O.state[k]).max() > 0:
+            err[nm] = _rel(got[k], O.state[k])
     return {"value": world * n * n * a.steps / (ms * 1e-3), "unit": UNIT,
             "ms_per_step": ms / a.steps, "dtype": "f32 fluxes and multigrid, f64 defect "
             "correction, RK accumulation and diagnostics",
-            "single_step_rel_l2_vs_f64": err, "solve_iterations_last_step": nite,
+            "single_step_error_vs_f64_oracle": err, "solve_iterations_last_step": nite,
             "solve_residual_last_step": res}
+
+
+def bench_dipole(a, host):
+    """Euler dipole, closed 128x128, 200 steps (the reference's CPU-runnable
+    case): the float64 GPU path from the oracle's initial state, timed as a
+    graph; the oracle's own 200 steps on one core give the CPU rate and the
+    parity of the final state; the CPU path on every core (one copy each)
+    gives the host's aggregate rate."""
+    import numpy as np
+    import torch
+    from fluid2d_gb300 import engine, workloads as W
+    from oracle import stepper
+    steps = a.dipole_steps
+    wl = W.dipole(128, 128)
+    p, O = stepper.from_workload(wl)
+    dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
+    G = engine.from_workload(wl, dt=dt)
+    G.var.state.copy_(torch.from_numpy(O.state).cuda())
+    G.diagnostics()
+    stream = torch.cuda.Stream()
+    ms = _timed_graph(G, steps, stream)  # the first replay captures the graph
+    final = G.var.state.cpu().numpy()
+    G.var.state.copy_(torch.from_numpy(O.state).cuda())
+    G.diagnostics()
+    with torch.cuda.stream(stream):
+        G.run(5, graph=True)
+    stream.synchronize()
+    ms = _timed_graph(G, steps, stream)
+    stepper.run(O, p, steps, dt)
+    parity = {nm: _rel(final[k], O.state[k])["rel_linf"]
+              for k, nm in enumerate(G.var.varname_list) if nm in ("vorticity", "psi", "u", "v")}
+    one, res1 = cpu_run([("dipole", None, None, 0, steps)], 1)
+    cores = host["nproc"]
+    allc, _ = cpu_run([("dipole", None, None, 0, steps)] * cores, cores)
+    value = 128 * 128 * steps / (ms * 1e-3)
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "precision": "fp64", "dt": dt,
+            "parity_rel_linf_after_%d_steps_vs_oracle" % steps: parity,
+            "cpu_baseline_1core": cpu_descr(1, "the %d steps on one core" % steps, one, host),
+            "cpu_baseline_all_cores": cpu_descr(cores, "%d copies, one per core, %d steps each"
+                                                % (cores, steps), allc, host),
+            "gpu_vs_cpu_1core": value / one, "gpu_vs_cpu_all_cores": value / allc}
+
+
+def bench_shear(a, host):
+    """Boussinesq shear layer, 'xchannel' 2048x512, Ri = 0.1: 1000 steps of
+    the float64 form and of the mixed form from the same state, each timed
+    (graph replays, 100 steps at a time), with the mixed form's per-field
+    error against the float64 path every 100 steps.  The float64 GPU path is
+    compared with the oracle over the first --shear-cpu-steps steps, which
+    also time the CPU path on one core (rate extrapolated to the run)."""
+    import numpy as np
+    import torch
+    from fluid2d_gb300 import engine, workloads as W
+    from oracle import stepper
+    wl = W.shear(2048, 512)
+    cells = 2048 * 512
+    p, O = stepper.from_workload(wl)
+    dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
+    s0 = torch.from_numpy(O.state).cuda()
+    A = engine.from_workload(wl, dt=dt)
+    B = engine.from_workload(wl, dt=dt, precision="mixed")
+    stream = torch.cuda.Stream()
+    # parity of the float64 form with the oracle over the first steps
+    A.var.state.copy_(s0)
+    A.diagnostics()
+    ncpu = a.shear_cpu_steps
+    A.run(ncpu)
+    t0 = time.perf_counter()
+    stepper.run(O, p, ncpu, dt)
+    t_oracle = time.perf_counter() - t0
+    got = A.var.state.cpu().numpy()
+    parity = {nm: _rel(got[k], O.state[k])["rel_linf"]
+              for k, nm in enumerate(A.var.varname_list)
+              if nm in ("vorticity", "psi", "u", "v", "buoyancy")}
+    # 1000 steps of each form, 100 at a time
+    for M in (A, B):
+        M.var.state.copy_(s0)
+        M.diagnostics()
+        with torch.cuda.stream(stream):
+            M.run(1, graph=True)  # capture
+        stream.synchronize()
+        M.var.state.copy_(s0)
+        M.diagnostics()
+    every = 100
+    ms = {"fp64": 0., "mixed": 0.}
+    rows = []
+    for k in range(every, a.shear_steps + 1, every):
+        ms["fp64"] += _timed_graph(A, every, stream)
+        ms["mixed"] += _timed_graph(B, every, stream)
+        fa, fb = A.var.state.cpu().numpy(), B.var.state.cpu().numpy()
+        row = {"step": k}
+        for q, nm in enumerate(A.var.varname_list):
+            if nm in ("vorticity", "psi", "u", "v", "buoyancy"):
+                row[nm] = _rel(fb[q], fa[q])
+        iu, iv = A.var.varname_list.index("u"), A.var.varname_list.index("v")
+        nrm = float(np.sqrt((fa[iu] ** 2).sum() + (fa[iv] ** 2).sum()))
+        row["velocity_rel_l2"] = float(np.sqrt(((fb[iu] - fa[iu]) ** 2).sum()
+                                               + ((fb[iv] - fa[iv]) ** 2).sum())) / nrm
+        rows.append(row)
+    n = a.shear_steps
+    cpu = cells * ncpu / t_oracle
+    return {"fp64": {"value": cells * n / (ms["fp64"] * 1e-3), "unit": UNIT,
+                     "ms_per_step": ms["fp64"] / n},
+            "mixed": {"value": cells * n / (ms["mixed"] * 1e-3), "unit": UNIT,
+                      "ms_per_step": ms["mixed"] / n},
+            "steps": n, "dt": dt, "gravity": wl["gravity"], "richardson": 0.1,
+            "parity_fp64_rel_linf_vs_oracle_after_%d_steps" % ncpu: parity,
+            "mixed_error_vs_fp64_every_100_steps": rows,
+            "cpu_baseline_1core": cpu_descr(1, "first %d steps of the oracle (parity build) "
+                                            "on one core, rate extrapolated to the run" % ncpu,
+                                            cpu, host),
+            "gpu_fp64_vs_cpu_1core": cells * n / (ms["fp64"] * 1e-3) / cpu}
 
 
 def _structure(choice):
@@ -450,20 +678,22 @@ def _structure(choice):
     return "batched groups=%d policy=%d, %s" % (groups, policy, lev)
 
 
-def bench_ensemble(a):
+def bench_ensemble(a, host):
     """Config: 96 independent Euler instances (sides log-uniform 64-768,
-    multiples of 64, islands, 3-12 vortices; seed 4).  Batched = the launch
-    structure the autotuner picks (fluid2d_gb300.autotune.tune_ensemble):
-    groups of instances whose steps are merged into one launch per kernel,
-    one graph per group on its own stream, or every instance's own step graph
-    replayed on 32 streams; comparator = the plain float64 path, one instance
-    at a time."""
+    multiples of 64, islands, 3-12 vortices; seed 4), 100 steps.  Batched =
+    the launch structure the autotuner picks (fluid2d_gb300.autotune.
+    tune_ensemble): groups of instances whose steps are merged into one
+    launch per kernel, one graph per group on its own stream, or every
+    instance's own step graph replayed on 32 streams; comparators = the plain
+    float64 path one instance at a time, and the CPU path with the 96
+    instances spread over every host core (a few steps each)."""
     import torch
     from fluid2d_gb300 import engine, workloads as W
     from fluid2d_gb300.autotune import tune_ensemble
     wls = W.ensemble(96, seed=4)
     cells = sum(w["nx"] * w["ny"] for w in wls)
-    out = {"instances": len(wls), "cells": cells, "steps": a.ensemble_steps}
+    steps = a.ensemble_steps
+    out = {"instances": len(wls), "cells": cells, "steps": steps}
     for prec in ("mixed", "fp64"):
         E = engine.ensemble_from_workloads(wls, precision=prec, nstreams=32)
         choice, times = tune_ensemble(E, steps=3, warmup=1)
@@ -471,13 +701,15 @@ def bench_ensemble(a):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        E.run(a.ensemble_steps)
+        E.run(steps)
         e1.record()
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        out[prec + "_batched"] = {"cell_steps_per_s": cells * a.ensemble_steps / (ms * 1e-3),
-                                  "ms_per_ensemble_step": ms / a.ensemble_steps,
+        failed = E.retire_failed()
+        out[prec + "_batched"] = {"cell_steps_per_s": cells * steps / (ms * 1e-3),
+                                  "ms_per_ensemble_step": ms / steps,
                                   "launch_structure": _structure(choice),
+                                  "failed_instances": len(failed),
                                   "tuning_ms_per_step": {_structure(k): round(v, 3)
                                                          for k, v in times.items()}}
         E.free_batch()
@@ -485,7 +717,7 @@ def bench_ensemble(a):
         torch.cuda.synchronize()
     # one at a time, plain float64
     tot_ms = 0.
-    nst = max(2, a.ensemble_steps // 4)
+    nst = 10
     s = torch.cuda.Stream()
     for w in wls:
         E = engine.ensemble_from_workloads([w], precision="fp64", nstreams=1)
@@ -504,26 +736,42 @@ def bench_ensemble(a):
                                  "ms_per_ensemble_step": tot_ms, "steps_timed_each": nst}
     out["mixed_batched_vs_fp64_one_at_a_time"] = (
         out["mixed_batched"]["cell_steps_per_s"] / out["fp64_one_at_a_time"]["cell_steps_per_s"])
+    cores = host["nproc"]
+    k = a.ensemble_cpu_steps
+    cpu, _ = cpu_run([("ensemble", None, i, 0, k) for i in range(len(wls))], cores)
+    out["cpu_baseline"] = cpu_descr(cores, "the 96 instances over %d processes, %d steps each "
+                                    "(stepping time shared evenly over the cores)" % (cores, k),
+                                    cpu, host)
+    out["mixed_batched_vs_cpu"] = out["mixed_batched"]["cell_steps_per_s"] / cpu
     return out
 
 
 def bench_served(a):
     """Config: served stream with Poisson arrivals at 40/s, 70 % Euler /
-    30 % Boussinesq, sides 128-2048 (multiples of 128), HBM budget 150 GB.
-    Bounded sample: the first --served-requests requests, step counts drawn
-    from U[5, 50] (the full stream draws U[50, 500])."""
+    30 % Boussinesq, sides 128-2048 (multiples of 128), HBM budget 150 GB,
+    steps U[50, 500].  Sample: the first --served-requests requests of the
+    2000-request stream.  Comparator: the same requests one at a time on the
+    plain float64 path, each timed over --alone-steps steps after its graph
+    capture (a fixed-dt step costs the same every step; the request's time is
+    its step count times that)."""
     from fluid2d_gb300 import serve, workloads as W
-    stream = W.served_stream(count=a.served_requests, rate=40., seed=5, steps_min=5,
-                             steps_max=50)
-    srv = serve.Server(150e9, precision="mixed", nstreams=32)
+    full = 2000
+    stream = W.served_stream(count=a.served_requests, rate=40., seed=5)
+    srv = serve.Server(150e9, precision="mixed", nstreams=32,
+                       max_active=a.served_slots or None)
     served = srv.run(stream)
-    alone = serve.run_one_at_a_time(stream, precision="fp64")
-    return {"sample": "%d requests, steps U[5,50], sides 128-2048, 70%% Euler / 30%% "
-                      "Boussinesq, Poisson 40/s, budget 150 GB" % len(stream),
+    alone = serve.run_one_at_a_time(stream, precision="fp64", timed_steps=a.alone_steps)
+    busy = served["cell_steps_per_s"] / max(1e-300, alone["cell_steps_per_s"])
+    wall = served["cell_steps_per_s_wall"] / max(1e-300, alone["cell_steps_per_s"])
+    return {"sample": "%d of the %d requests (%.0f %%), steps U[50,500], sides 128-2048, "
+                      "70%% Euler / 30%% Boussinesq, Poisson 40/s, budget 150 GB"
+                      % (len(stream), full, 100. * len(stream) / full),
+            "slots": a.served_slots or None,
             "served_mixed_continuous_batching": served,
             "fp64_one_at_a_time": alone,
-            "throughput_ratio": served["cell_steps_per_s"] / max(1e-300,
-                                                                 alone["cell_steps_per_s"])}
+            "throughput_ratio_busy": busy, "throughput_ratio_wall": wall,
+            "p50_ratio_served_vs_alone": served["p50_step_ms"] / max(1e-300,
+                                                                      alone["p50_step_ms"])}
 
 
 def profile_step(argv=None):

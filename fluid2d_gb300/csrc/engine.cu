@@ -781,7 +781,6 @@ struct DiagArgs {
     int nr;            // partial kernel: rows per block; final kernel: partial blocks
     int *status;              // the model's status word (F2D_STATUS_* bits, sticky)
     const SolveState *solve;  // the last full solve's state (divergence)
-    const double *dt;         // the step's dt
 };
 
 // diagnostics of core/euler.py:185-223, core/boussinesq.py:123-153,
@@ -918,7 +917,6 @@ F2D_DEV void diag_final_body(const DiagArgs &a, const VB) {
         if (!finite) st |= STATUS_NONFINITE;
         if (maxu > 1e3) st |= STATUS_BLOWUP;
         if (a.solve && a.solve->status == ERR_DIVERGED) st |= STATUS_DIVERGED;
-        if (a.dt && !(isfinite(*a.dt) && *a.dt > 0.)) st |= STATUS_BAD_DT;
         if (st) *a.status |= st;
     }
 }
@@ -955,6 +953,7 @@ struct SetDtArgs {
     const double *diag;
     int adaptable;
     double dt0, cfl, hmin, dtmax;
+    int *status;  // STATUS_BAD_DT when the step's dt is not a positive finite number
 };
 
 F2D_DEV void set_dt_body(const SetDtArgs &a, const VB) {
@@ -972,6 +971,7 @@ F2D_DEV void set_dt_body(const SetDtArgs &a, const VB) {
     *dt = d;
     cst[3] = maxspeed;
     *advc = split_const(cst);
+    if (a.status && !(isfinite(d) && d > 0.)) *a.status |= STATUS_BAD_DT;
 }
 
 __global__ void k_set_dt(SetDtArgs a) { pdl_prologue();
@@ -985,9 +985,11 @@ struct BSetDt {
 F2D_BATCH_ENTRY(SetDt, BSetDt)
 
 static int set_dt(double *dt, double *cst, void *advc, const double *diag, int adaptable,
-                  double dt0, double cfl, double hmin, double dtmax, cudaStream_t s) {
+                  double dt0, double cfl, double hmin, double dtmax, int *status,
+                  cudaStream_t s) {
     return launch_body<BSetDt>(
-        k_set_dt, SetDtArgs{dt, cst, (SplitConst *)advc, diag, adaptable, dt0, cfl, hmin, dtmax},
+        k_set_dt,
+        SetDtArgs{dt, cst, (SplitConst *)advc, diag, adaptable, dt0, cfl, hmin, dtmax, status},
         dim3(1), dim3(1), 0, s, "set_dt");
 }
 
@@ -1479,7 +1481,6 @@ int Model::diagnostics(cudaStream_t s) {
     a.out = diag;
     a.status = status;
     a.solve = gmg.solve_state;
-    a.dt = dt;
     int rows = mv - 2 * NH;
     int nb = reduce_blocks(rows);
     int rpb = (rows + nb - 1) / nb;
@@ -1494,7 +1495,7 @@ int Model::diagnostics(cudaStream_t s) {
 int Model::step(cudaStream_t s) {
     gmg.nprobe = 0;
     TRY(set_dt(dt, cst, advc, diag, desc.adaptable_dt, desc.dt, desc.cfl, dx < dy ? dx : dy,
-               desc.dtmax, s));
+               desc.dtmax, status, s));
     TRY(advance(s));
     return diagnostics(s);
 }
@@ -2283,7 +2284,7 @@ int f2d_model_loop_start(void *model, void *stream) {
     if (M->loop->k.fluxes) {
         // set_dt then the flux diagnostic (core/fluid2d.py:203-210)
         TRY(set_dt(M->dt, M->cst, M->advc, M->diag, M->desc.adaptable_dt, M->desc.dt,
-                   M->desc.cfl, M->dx < M->dy ? M->dx : M->dy, M->desc.dtmax, s));
+                   M->desc.cfl, M->dx < M->dy ? M->dx : M->dy, M->desc.dtmax, M->status, s));
         TRY(M->diag_fluxes(s));
     }
     TRY(loop_record(M->loop->clock, M->loop->k, M->diag, M->loop->r, s));

@@ -165,9 +165,9 @@ class Server(object):
                 self._release(r, now + dt)
                 self.failed.append(r)
             elif r.done >= r.steps:
-                self._release(r, now + dt)
                 if self.on_finish is not None:
                     self.on_finish(r)
+                self._release(r, now + dt)
                 self.finished.append(r)
             else:
                 keep.append(r)
@@ -272,9 +272,12 @@ class _GpuStepper(object):
         return e0.elapsed_time(e1) * 1e-3
 
 
-def run_one_at_a_time(stream, precision="fp64", make_model=None):
+def run_one_at_a_time(stream, precision="fp64", make_model=None, timed_steps=None):
     """The comparator: every request alone on the GPU, in arrival order;
-    per-step latency is that request's own step time."""
+    per-step latency is that request's own step time.  With `timed_steps`,
+    each request is timed over that many steps after its graph capture and
+    its time is its step count times the mean (a fixed-dt step costs the same
+    every step); otherwise every step runs."""
     import torch
     make_model = make_model or _gpu_make_model
     fin = []
@@ -284,19 +287,23 @@ def run_one_at_a_time(stream, precision="fp64", make_model=None):
     for k, (t, wl, steps) in enumerate(stream):
         r = Request(k, t, wl, steps)
         m = make_model(wl, precision)
+        n = steps - 1 if timed_steps is None else max(1, min(steps - 1, int(timed_steps)))
         with torch.cuda.stream(s):
             m.run(1, graph=True)  # capture
             s.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(s)
-            m.run(steps - 1, graph=True)
+            m.run(n, graph=True)
             e1.record(s)
             e1.synchronize()
-        ms = e0.elapsed_time(e1) / max(1, steps - 1)
+        ms = e0.elapsed_time(e1) / max(1, n)
         r.latencies = [ms * 1e-3] * steps
         r.done = steps
         busy += ms * 1e-3 * steps
         fin.append(r)
         del m
-    return metrics(fin, time.perf_counter() - t0, busy)
+    out = metrics(fin, time.perf_counter() - t0, busy)
+    if timed_steps is not None:
+        out["steps_timed_per_request"] = int(timed_steps)
+    return out

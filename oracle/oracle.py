@@ -36,22 +36,41 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "f2d_oracle.c")
 _BUILD = os.path.join(_HERE, "_build")
-_SO = os.path.join(_BUILD, "liboracle.so")
 
-# -ffp-contract=off: no fused multiply-add, so every product and sum is
-# rounded as the Fortran statement writes it.
+# parity: -ffp-contract=off, no fused multiply-add, so every product and sum
+# is rounded as the Fortran statement writes it.
 CFLAGS = ["-O3", "-ffp-contract=off", "-fPIC", "-shared", "-fno-math-errno"]
+# timing (the CPU baseline): what the reference's own build does for speed
+# (build.py:13, -O3 -march=native): full optimisation with multiply-adds
+# contracted into FMA.  -march=native itself is not used: the host code
+# builds the same on the x86-64 and aarch64 machines, and FMA is part of the
+# aarch64 base instruction set.
+TIMING_CFLAGS = ["-O3", "-ffp-contract=fast", "-funroll-loops", "-fPIC", "-shared",
+                 "-fno-math-errno"]
+VARIANTS = {"parity": ("liboracle.so", CFLAGS),
+            "timing": ("liboracle_timing.so", TIMING_CFLAGS)}
+_SO = os.path.join(_BUILD, VARIANTS["parity"][0])
 
 
-def build(force=False):
-    """Compile the oracle shared library (gcc, a second or two)."""
+def variant():
+    """The build this process loads: 'parity' unless F2D_ORACLE_VARIANT says
+    'timing' (set by bench.py's CPU-baseline workers before they load it)."""
+    v = os.environ.get("F2D_ORACLE_VARIANT", "parity")
+    return v if v in VARIANTS else "parity"
+
+
+def build(force=False, variants=("parity", "timing")):
+    """Compile the oracle shared libraries (gcc, a second or two each)."""
     os.makedirs(_BUILD, exist_ok=True)
-    if (not force and os.path.exists(_SO)
-            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
-        return _SO
-    tmp = _SO + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc"] + CFLAGS + ["-o", tmp, _SRC, "-lm"])
-    os.replace(tmp, _SO)
+    for v in variants:
+        so, flags = VARIANTS[v]
+        so = os.path.join(_BUILD, so)
+        if (not force and os.path.exists(so)
+                and os.path.getmtime(so) >= os.path.getmtime(_SRC)):
+            continue
+        tmp = so + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc"] + flags + ["-o", tmp, _SRC, "-lm"])
+        os.replace(tmp, so)
     return _SO
 
 
@@ -61,7 +80,9 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        _lib = ctypes.CDLL(build())
+        v = variant()
+        build(variants=(v,))
+        _lib = ctypes.CDLL(os.path.join(_BUILD, VARIANTS[v][0]))
         _declare(_lib)
     return _lib
 

@@ -69,8 +69,10 @@ def parse(argv=None):
     ap.add_argument("--ensemble-steps", type=int, default=100)
     ap.add_argument("--ensemble-cpu-steps", type=int, default=3)
     ap.add_argument("--served-requests", type=int, default=200)
-    ap.add_argument("--served-slots", type=int, default=0,
-                    help="requests stepped together at most (0: the budget alone decides)")
+    ap.add_argument("--served-slots", type=int, default=16,
+                    help="simulations running at once at most (0: the budget alone decides)")
+    ap.add_argument("--served-chunk", type=int, default=16,
+                    help="steps queued at a time for each served simulation")
     ap.add_argument("--alone-steps", type=int, default=20,
                     help="steps timed per request when run alone (the rest extrapolated)")
     ap.add_argument("--only", default="",
@@ -750,28 +752,37 @@ def bench_served(a):
     """Config: served stream with Poisson arrivals at 40/s, 70 % Euler /
     30 % Boussinesq, sides 128-2048 (multiples of 128), HBM budget 150 GB,
     steps U[50, 500].  Sample: the first --served-requests requests of the
-    2000-request stream.  Comparator: the same requests one at a time on the
-    plain float64 path, each timed over --alone-steps steps after its graph
-    capture (a fixed-dt step costs the same every step; the request's time is
-    its step count times that)."""
+    2000-request stream, served in the mixed form with every admitted
+    simulation running free on its own stream (chunks of --served-chunk
+    steps), at two slot counts: --served-slots (throughput) and 4
+    (latency).  Comparator: the same requests one at a time on the plain
+    float64 path, each timed over --alone-steps steps after its graph capture
+    (a fixed-dt step costs the same every step; the request's time is its
+    step count times that)."""
     from fluid2d_gb300 import serve, workloads as W
     full = 2000
     stream = W.served_stream(count=a.served_requests, rate=40., seed=5)
-    srv = serve.Server(150e9, precision="mixed", nstreams=32,
-                       max_active=a.served_slots or None)
-    served = srv.run(stream)
     alone = serve.run_one_at_a_time(stream, precision="fp64", timed_steps=a.alone_steps)
-    busy = served["cell_steps_per_s"] / max(1e-300, alone["cell_steps_per_s"])
-    wall = served["cell_steps_per_s_wall"] / max(1e-300, alone["cell_steps_per_s"])
-    return {"sample": "%d of the %d requests (%.0f %%), steps U[50,500], sides 128-2048, "
-                      "70%% Euler / 30%% Boussinesq, Poisson 40/s, budget 150 GB"
-                      % (len(stream), full, 100. * len(stream) / full),
-            "slots": a.served_slots or None,
-            "served_mixed_continuous_batching": served,
-            "fp64_one_at_a_time": alone,
-            "throughput_ratio_busy": busy, "throughput_ratio_wall": wall,
-            "p50_ratio_served_vs_alone": served["p50_step_ms"] / max(1e-300,
-                                                                      alone["p50_step_ms"])}
+    out = {"sample": "%d of the %d requests (%.0f %%), steps U[50,500], sides 128-2048, "
+                     "70%% Euler / 30%% Boussinesq, Poisson 40/s, budget 150 GB"
+                     % (len(stream), full, 100. * len(stream) / full),
+           "fp64_one_at_a_time": alone}
+    for key, slots in (("served_mixed_free_running", a.served_slots),
+                       ("served_mixed_free_running_4_slots", 4)):
+        srv = serve.Server(150e9, precision="mixed", nstreams=32, max_active=slots or None)
+        m = srv.run_free(stream, chunk=a.served_chunk)
+        m["slots"] = slots or None
+        m["chunk_steps"] = a.served_chunk
+        m["peak_active"] = srv.peak_active
+        m["peak_bytes"] = srv.peak_used
+        m["throughput_ratio_busy"] = m["cell_steps_per_s"] / max(1e-300, alone["cell_steps_per_s"])
+        m["throughput_ratio_wall"] = (m["cell_steps_per_s_wall"]
+                                      / max(1e-300, alone["cell_steps_per_s"]))
+        m["p50_ratio_vs_alone"] = m["p50_step_ms"] / max(1e-300, alone["p50_step_ms"])
+        m["p99_ratio_vs_alone"] = m["p99_step_ms"] / max(1e-300, alone["p99_step_ms"])
+        out[key] = m
+        del srv
+    return out
 
 
 def profile_step(argv=None):

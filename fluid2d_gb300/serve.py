@@ -17,6 +17,10 @@ the next admissions (continuous batching: requests join and leave between
 ticks).  Per-step latency of a request is the duration of the tick that
 advanced it.
 
+`run_free` serves the same stream with every admitted simulation running free
+on its own stream (chunks of steps queued as the previous chunk finishes)
+instead of in lockstep ticks.
+
 `run_one_at_a_time` is the comparator: the same requests, one after the
 other, each alone on the GPU.
 """
@@ -82,12 +86,14 @@ class Server(object):
     """
 
     def __init__(self, hbm_budget, precision="mixed", nstreams=32, make_model=None,
-                 step_models=None, max_active=None, clock=time.perf_counter, on_finish=None):
+                 step_models=None, max_active=None, clock=time.perf_counter, on_finish=None,
+                 chunks=None):
         self.budget = int(hbm_budget)
         self.precision = precision
         self.nstreams = nstreams
         self.make_model = make_model or _gpu_make_model
-        self.step_models = step_models or _GpuStepper(nstreams).step
+        self._step_models = step_models
+        self._chunks = chunks
         self.read_status = _read_status
         self.max_active = max_active
         self.clock = clock
@@ -99,7 +105,20 @@ class Server(object):
         self.rejected = []
         self.failed = []
         self.ticks = []
+        self.peak_used = 0    # the most device memory admitted at once
+        self.peak_active = 0  # the most simulations running at once
         self.per_point = {}  # measured device bytes per grid point, per model
+
+    def step_models(self, models):
+        if self._step_models is None:
+            self._step_models = _GpuStepper(self.nstreams).step
+        return self._step_models(models)
+
+    @property
+    def chunks(self):
+        if self._chunks is None:
+            self._chunks = _GpuChunks(self.nstreams)
+        return self._chunks
 
     def _estimate(self, wl):
         return estimate_bytes(wl, self.precision, self.per_point.get(wl["model"]))
@@ -148,6 +167,8 @@ class Server(object):
             self.used += req.nbytes
             req.admitted = now
             self.active.append(req)
+            self.peak_used = max(self.peak_used, self.used)
+            self.peak_active = max(self.peak_active, len(self.active))
 
     def tick(self, now):
         if not self.active:
@@ -201,6 +222,70 @@ class Server(object):
             elif self.queue and not self.active:
                 # head cannot be admitted even with nothing running
                 self._reject(self.queue.pop(0), "does not fit the HBM budget alone")
+        wall = self.clock() - t0
+        return metrics(self.finished, wall, busy, self.rejected, self.failed)
+
+
+    def run_free(self, stream, chunk=8, time_scale=1.0):
+        """Serve (arrival, wl, steps) tuples with every admitted simulation
+        running free on its own CUDA stream: `chunk` steps (its captured step
+        graph replayed) are queued at a time, and the next chunk as soon as
+        the last one has finished, so a small simulation is not held back by
+        a large one as in the lockstep ticks of run(); the per-step latency of
+        a step is its chunk's duration on the device over the chunk's steps.
+        Admission, retirement, failure isolation (status words read after
+        each chunk) and the budget are those of run().  Returns the metrics."""
+        reqs = [Request(k, t, wl, st) for k, (t, wl, st) in enumerate(stream)]
+        t0 = self.clock()
+        nxt = 0
+        busy = 0.
+        last = t0
+        while nxt < len(reqs) or self.queue or self.active:
+            tnow = self.clock()
+            if self.active:
+                busy += tnow - last
+            last = tnow
+            now = (tnow - t0) * time_scale
+            while nxt < len(reqs) and reqs[nxt].arrival <= now:
+                self.submit(reqs[nxt])
+                nxt += 1
+            before = len(self.active)
+            self.admit(now)
+            for r in self.active[before:]:
+                self.chunks.launch(r, min(chunk, r.steps - r.done))
+            # chunks that have finished: account, check, go on or retire
+            done = [(r, self.chunks.poll(r)) for r in self.active]
+            done = [(r, sec) for r, sec in done if sec is not None]
+            if done:
+                status = self.read_status([r.model for r, _ in done])
+                gone = set()
+                for (r, sec), bits in zip(done, status):
+                    n = r.inflight
+                    r.done += n
+                    r.latencies.extend([sec / n] * n)
+                    if bits:
+                        r.error = "retired after step %d: %s" % (r.done, _status_text(bits))
+                        self._release(r, now)
+                        self.failed.append(r)
+                        gone.add(id(r))
+                    elif r.done >= r.steps:
+                        if self.on_finish is not None:
+                            self.on_finish(r)
+                        self._release(r, now)
+                        self.finished.append(r)
+                        gone.add(id(r))
+                    else:
+                        self.chunks.launch(r, min(chunk, r.steps - r.done))
+                self.active = [r for r in self.active if id(r) not in gone]
+            elif not self.active:
+                if nxt < len(reqs):
+                    wait = (reqs[nxt].arrival - now) / time_scale
+                    if wait > 0:
+                        time.sleep(min(wait, 0.05))
+                elif self.queue:
+                    self._reject(self.queue.pop(0), "does not fit the HBM budget alone")
+            else:
+                self.chunks.wait()
         wall = self.clock() - t0
         return metrics(self.finished, wall, busy, self.rejected, self.failed)
 
@@ -270,6 +355,39 @@ class _GpuStepper(object):
         e1.record(cur)
         e1.synchronize()
         return e0.elapsed_time(e1) * 1e-3
+
+
+class _GpuChunks(object):
+    """Chunks of steps of each request on its own stream (free-running
+    serving): launch() queues a chunk bracketed by CUDA events, poll() gives
+    its device duration in seconds once it has finished, else None."""
+
+    def __init__(self, nstreams):
+        import torch
+        self.torch = torch
+        self.streams = [torch.cuda.Stream() for _ in range(max(1, nstreams))]
+        self.next = 0
+
+    def launch(self, r, n):
+        torch = self.torch
+        if getattr(r, "stream", None) is None:
+            r.stream = self.streams[self.next % len(self.streams)]
+            self.next += 1
+            r.ev0 = torch.cuda.Event(enable_timing=True)
+            r.ev1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(r.stream):
+            r.ev0.record(r.stream)
+            r.model.run(n, graph=True)
+            r.ev1.record(r.stream)
+        r.inflight = n
+
+    def poll(self, r):
+        if not r.ev1.query():
+            return None
+        return r.ev0.elapsed_time(r.ev1) * 1e-3
+
+    def wait(self):
+        time.sleep(50e-6)
 
 
 def run_one_at_a_time(stream, precision="fp64", make_model=None, timed_steps=None):

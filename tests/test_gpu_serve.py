@@ -6,8 +6,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("mode", ["lockstep", "free"])
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_served_results_equal_alone(precision):
+def test_served_results_equal_alone(precision, mode):
     import torch
     from fluid2d_gb300 import serve, workloads as W
     stream = W.served_stream(count=6, rate=1000., seed=31, side_min=128, side_max=256,
@@ -20,9 +21,12 @@ def test_served_results_equal_alone(precision):
         finals[req.rid] = req.model.var.state.cpu().numpy()
 
     srv = serve.Server(budget, precision=precision, nstreams=4, on_finish=keep)
-    m = srv.run(stream, time_scale=1.0)
+    if mode == "free":
+        m = srv.run_free(stream, chunk=2, time_scale=1.0)
+    else:
+        m = srv.run(stream, time_scale=1.0)
     assert m["requests"] == 6 and m["rejected"] == 0
-    assert max(n for _, n, _, _ in srv.ticks) <= 2 or srv.used <= budget
+    assert srv.peak_used <= budget and 1 <= srv.peak_active <= 6
     for k, (t, wl, steps) in enumerate(stream):
         alone = serve._gpu_make_model(wl, precision)
         alone.run(steps, graph=False)
@@ -30,7 +34,8 @@ def test_served_results_equal_alone(precision):
         assert np.array_equal(alone.var.state.cpu().numpy(), finals[k]), k
 
 
-def test_a_failing_request_is_retired_alone():
+@pytest.mark.parametrize("mode", ["lockstep", "free"])
+def test_a_failing_request_is_retired_alone(mode):
     """A request whose initial vorticity holds a NaN is retired after its
     first step with the reason; the requests beside it finish with the
     results they give alone; bogus requests are rejected at submission."""
@@ -49,7 +54,10 @@ def test_a_failing_request_is_retired_alone():
         finals[req.rid] = req.model.var.state.cpu().numpy()
 
     srv = serve.Server(100e9, precision="fp64", nstreams=4, on_finish=keep)
-    m = srv.run(stream, time_scale=1.0)
+    if mode == "free":
+        m = srv.run_free(stream, chunk=1, time_scale=1.0)
+    else:
+        m = srv.run(stream, time_scale=1.0)
     assert m["requests"] == 3 and m["failed"] == 1 and m["rejected"] == 1
     assert srv.failed[0].rid == 2 and "non-finite" in srv.failed[0].error
     assert srv.failed[0].done == 1

@@ -164,3 +164,33 @@ def test_admission_uses_measured_sizes():
         s.admit(0.)
         s.tick(0.)
     assert [r.rid for r in s.finished] == [0, 1, 2]
+
+
+class FakeChunks(object):
+    """Free-running chunks on the host: a chunk of n steps finishes at the
+    next poll, after n ms; the model counts its steps."""
+
+    def launch(self, r, n):
+        r.inflight = n
+        r.model.steps += n
+
+    def poll(self, r):
+        return 1e-3 * r.inflight
+
+    def wait(self):
+        pass
+
+
+def test_free_running_serving_admits_retires_and_isolates():
+    budget = serve.estimate_bytes(wl(128), "fp64") * 2 + 1
+    s = serve.Server(budget, precision="fp64", make_model=FakeModel, chunks=FakeChunks(),
+                     max_active=2)
+    stream = [(0., wl(128), 20), (0., dict(wl(128), fail_after=5), 20), (0., wl(128), 7),
+              (0., {"nx": 3, "ny": 64, "model": "euler"}, 5)]
+    m = s.run_free(stream, chunk=4, time_scale=100.)
+    assert m["requests"] == 2 and m["failed"] == 1 and m["rejected"] == 1
+    assert sorted(r.rid for r in s.finished) == [0, 2]
+    assert s.failed[0].rid == 1 and "blow-up" in s.failed[0].error
+    assert all(len(r.latencies) == r.steps for r in s.finished)
+    assert all(abs(x - 1e-3) < 1e-12 for r in s.finished for x in r.latencies)
+    assert s.used == 0

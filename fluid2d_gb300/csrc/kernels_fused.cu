@@ -757,6 +757,17 @@ F2D_DEV T jacobi_bits(unsigned bits, const T *x, int W, T bq, const AnalyticT<T>
                              - bq);
 }
 
+// one damped-Jacobi update of a point whose 3x3 block is fluid, through the
+// separable form of the analytic 9-point operator (x: the point in a row-major
+// array of row width W)
+template <typename T>
+F2D_DEV T separable9(const T *x, int W, T bq, T c3, T k0, T k1) {
+    const T corners = (x[-W - 1] + x[-W + 1]) + (x[W - 1] + x[W + 1]);
+    const T edges = (x[-W] + x[W]) + (x[-1] + x[1]);
+    const T V = fma((T)4, x[0], fma((T)2, edges, corners));
+    return fma(k1, V, fma(k0, x[0], -c3 * bq));
+}
+
 template <typename T>
 F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
@@ -796,6 +807,7 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
         }
     }
     // bits, mask and b of the first sweep's points (rows/cols 2..m-3)
+    int mine = 1;  // every point this thread staged has its 3x3 block fluid
     {
         const size_t o1 = off(j0 - 1, i0 - 1, nv);
         const uint16_t *nbg = L.nb + o1;
@@ -806,12 +818,28 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
             const int j = j0 - 1 + r, i = i0 - 1 + c;
             if (j < 2 || j > mv - 3 || i < 2 || i > nv - 3) continue;
             const int o = r * nv + c;
-            nbs[q] = nbg[o];
+            const uint16_t bits = nbg[o];
+            nbs[q] = bits;
             ms[q] = mg[o];
             bs[q] = bg[o];
+            mine &= bits == 511u;
         }
     }
+#ifdef F2D_EXACT
     __syncthreads();
+    const bool uni = false;
+#else
+    // A tile whose first-sweep points all have fluid 3x3 blocks takes the
+    // separable form of the 9-point operator (product build): (c/4)(V - 4x)
+    // with V the [1 2 1] x [1 2 1] sum, so a sweep is k0 x + k1 V - c3 b
+    // (k1 = c3 c/4, k0 = c2 - 4 k1): no coefficient selects, 8 operations
+    // for the operator instead of 8 products and 16 selects.  The same
+    // function, another rounding; the exact build keeps jacobi_bits().
+    const T e = an.sc[1];
+    const bool nine = e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e && an.sc[2] == an.sc[0];
+    const bool uni = __syncthreads_and(mine && nine) != 0;
+    const T k1 = an.c3 * e * (T)0.5, k0 = c2 - (T)4 * k1;
+#endif
     // first sweep
     for (int q = tid; q < SL_TW * SL_TW; q += SL_THREADS) {
         const int r = q / SL_TW, c = q - r * SL_TW;
@@ -823,7 +851,13 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
         } else if (xmode == X_ZERO) {
             v = ((nbs[q] & 256u) ? an.c3 : c3z) * (-bs[q]);
         } else {
-            v = jacobi_bits<T>(nbs[q], xs + (r + 1) * SL_XW + (c + 1), SL_XW, bs[q], an, c2, c3z);
+            const T *x = xs + (r + 1) * SL_XW + (c + 1);
+#ifndef F2D_EXACT
+            if (uni)
+                v = separable9<T>(x, SL_XW, bs[q], an.c3, k0, k1);
+            else
+#endif
+                v = jacobi_bits<T>(nbs[q], x, SL_XW, bs[q], an, c2, c3z);
         }
         ts[q] = v;
     }
@@ -840,7 +874,12 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
         const int q = (r + 1) * SL_TW + (tx + 1);
         T v = (T)0;
         if (ms[q] != 0)
-            v = jacobi_bits<T>(nbs[q], ts + q, SL_TW, bs[q], an, c2, c3z);
+#ifndef F2D_EXACT
+            if (uni)
+                v = separable9<T>(ts + q, SL_TW, bs[q], an.c3, k0, k1);
+            else
+#endif
+                v = jacobi_bits<T>(nbs[q], ts + q, SL_TW, bs[q], an, c2, c3z);
         if (direct)
             out[off(j, i, nv)] = v;
         else

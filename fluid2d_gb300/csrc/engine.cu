@@ -612,8 +612,15 @@ int Gmg::smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream
     } else {
         if (xmode == X_PLUS_INTERP || xmode == X_INTERP)
             TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, xmode == X_INTERP, active, s));
-        TRY(mg_sweep1<T>(L[l], a0, c1, c2, xmode == X_ZERO, active, s));
-        TRY(mg_sweep2<T>(L[l], a0, c1, c2, active, s));
+        // the column form where it applies (float64 product build), else the
+        // sweeps in the reference's order of operations
+        bool done = false;
+        if constexpr (sizeof(T) == 8)
+            if (a0) TRY(mg_sweeps_column<T>(L[l], *a0, c1, c2, xmode == X_ZERO, active, s, &done));
+        if (!done) {
+            TRY(mg_sweep1<T>(L[l], a0, c1, c2, xmode == X_ZERO, active, s));
+            TRY(mg_sweep2<T>(L[l], a0, c1, c2, active, s));
+        }
     }
     if (pr) {
         TRY(cuda_status(cudaEventRecordWithFlags(ev[nprobe][1], s, cudaEventRecordExternal),

@@ -110,6 +110,12 @@ int mg_coarse_apply(const T *op, int n, const LevelView<T> &L, const int *active
 template <typename T>
 int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, int xmode,
                     const LevelView<T> *coarse, T *out, const int *active, cudaStream_t s);
+// the float64 finest level's two sweeps (x or zero -> t -> x and its images)
+// in column form (product build); *done = false (nothing launched) when it
+// does not apply
+template <typename T>
+int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, bool zero_x,
+                     const int *active, cudaStream_t s, bool *done);
 // residual of L (x, b) restricted into the coarse b2
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,

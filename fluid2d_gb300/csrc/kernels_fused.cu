@@ -97,26 +97,36 @@ F2D_DEV T diag_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i)
     return L.A[4 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
 }
 
+// omega/|A5| of point (j, i); c3z is its value where A5 = 0, c1/|0|, which
+// the host computes once (a division per point costs more than the point)
 template <typename T, bool L0>
-F2D_DEV T c3_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T c1) {
+F2D_DEV T c3_coef(const LevelView<T> &L, const AnalyticT<T> *an, int j, int i, T c3z) {
     if (L0 && L.nb) {  // the diagonal's bit decides a5 != 0 without a float64 compare
-        return (L.nb[off(j, i, L.nv)] & 256u) ? an->c3 : c1 / fabs((T)0);
+        return (L.nb[off(j, i, L.nv)] & 256u) ? an->c3 : c3z;
     }
     if (L0) {
         const T a5 = diag_coef<T, L0>(L, an, j, i);
-        return a5 != (T)0 ? an->c3 : c1 / fabs(a5);
+        return a5 != (T)0 ? an->c3 : c3z;
     }
     return L.A[5 * (size_t)L.mv * L.nv + off(j, i, L.nv)];
+}
+
+// c1/|0|: the relaxation factor over a zero diagonal, as the reference's
+// smoother computes it for a point without an operator
+template <typename T>
+inline T c3_zero(T c1) {
+    const T zero = (T)0;
+    return c1 / fabs(zero);
 }
 
 // damped Jacobi (core/gmg/fortran_multigrid.f90:66-85); q == null: x = 0
 template <typename T, bool L0>
 F2D_DEV T jacobi(const LevelView<T> &L, const AnalyticT<T> *an, const T *q, const T *b, int j,
-                 int i, T c1, T c2) {
+                 int i, T c3z, T c2) {
     const int nv = L.nv;
     const size_t p = off(j, i, nv);
     if (L.msk[p] == 0) return (T)0;
-    const T c3 = c3_coef<T, L0>(L, an, j, i, c1);
+    const T c3 = c3_coef<T, L0>(L, an, j, i, c3z);
     if (q == nullptr) return c3 * (-b[p]);
     T a[8];
     offdiag<T, L0>(L, an, j, i, a);
@@ -260,6 +270,7 @@ struct SweepArgs {
     T c1, c2;
     int zero_x;
     const int *active;
+    T c3z;  // c1/|0| (c3_zero)
 };
 
 template <typename T, bool L0>
@@ -269,7 +280,7 @@ F2D_DEV void sweep1_body(const SweepArgs<T> &A, const VB vb) {
     const int i = 2 + vb.x * LV_TX + threadIdx.x;
     const int j = 2 + vb.y * LV_TY + threadIdx.y;
     if (i > L.nv - 3 || j > L.mv - 3) return;
-    L.t[off(j, i, L.nv)] = jacobi<T, L0>(L, &A.an, A.zero_x ? nullptr : L.x, L.b, j, i, A.c1, A.c2);
+    L.t[off(j, i, L.nv)] = jacobi<T, L0>(L, &A.an, A.zero_x ? nullptr : L.x, L.b, j, i, A.c3z, A.c2);
 }
 
 template <typename T, bool L0>
@@ -279,7 +290,7 @@ F2D_DEV void sweep2_body(const SweepArgs<T> &A, const VB vb) {
     const int i = NH + vb.x * LV_TX + threadIdx.x;
     const int j = NH + vb.y * LV_TY + threadIdx.y;
     if (i > L.nv - NH - 1 || j > L.mv - NH - 1) return;
-    T v = jacobi<T, L0>(L, &A.an, L.t, L.b, j, i, A.c1, A.c2);
+    T v = jacobi<T, L0>(L, &A.an, L.t, L.b, j, i, A.c3z, A.c2);
     store_images(L.x, j, i, L.mv, L.nv, v);
 }
 
@@ -497,7 +508,7 @@ template <typename T>
 int mg_sweep1(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, bool zero_x,
               const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 4, L.nv - 4), b(LV_TX, LV_TY);
-    SweepArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, zero_x ? 1 : 0, active};
+    SweepArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, zero_x ? 1 : 0, active, c3_zero(c1)};
     if (an) return launch_body<BSweep1<T, true>>(k_sweep1<T, true>, a, g, b, 0, s, "mg_sweep1");
     return launch_body<BSweep1<T, false>>(k_sweep1<T, false>, a, g, b, 0, s, "mg_sweep1");
 }
@@ -506,7 +517,7 @@ template <typename T>
 int mg_sweep2(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, const int *active,
               cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), b(LV_TX, LV_TY);
-    SweepArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, 0, active};
+    SweepArgs<T> a{L, an ? *an : AnalyticT<T>{}, c1, c2, 0, active, c3_zero(c1)};
     if (an) return launch_body<BSweep2<T, true>>(k_sweep2<T, true>, a, g, b, 0, s, "mg_sweep2");
     return launch_body<BSweep2<T, false>>(k_sweep2<T, false>, a, g, b, 0, s, "mg_sweep2");
 }
@@ -603,6 +614,7 @@ struct SmoothFusedArgs {
     T *out;
     const int *active;
     int tx, ty;  // the tile
+    T c3z;       // c3 where the diagonal is 0 (c1/|0|), computed on the host
 };
 
 template <typename T, bool L0>
@@ -652,7 +664,7 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
         if (L.msk[p] == 0) {
             v = (T)0;
         } else {
-            const T c3 = c3_coef<T, L0>(L, &an, j, i, c1);
+            const T c3 = c3_coef<T, L0>(L, &an, j, i, A.c3z);
             if (xmode == X_ZERO) {
                 v = c3 * (-L.b[p]);
             } else {
@@ -682,7 +694,7 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
         const size_t p = off(j, i, nv);
         T v = (T)0;
         if (L.msk[p] != 0) {
-            const T c3 = c3_coef<T, L0>(L, &an, j, i, c1);
+            const T c3 = c3_coef<T, L0>(L, &an, j, i, A.c3z);
             T a[8];
             offdiag<T, L0>(L, &an, j, i, a);
             const T *t = ts + (j - (j0 - 1)) * TW + (i - (i0 - 1));
@@ -768,6 +780,200 @@ F2D_DEV T separable9(const T *x, int W, T bq, T c3, T k0, T k1) {
     return fma(k1, V, fma(k0, x[0], -c3 * bq));
 }
 
+// ------------------------------------------------------------ finest-level sweeps, column form
+// The float64 finest level's two damped-Jacobi sweeps (product build) with
+// each thread taking a column of SC_K = 4 consecutive points: the 3 x
+// (SC_K + 2) input values around them (and their b, coefficient bits and
+// mask) are loaded up front, one memory round trip, and every point's
+// neighbours come from registers.  Where a point's 3x3 block is fluid the
+// analytic 9-point operator is (c/4)(V - 4x), V the [1 2 1] x [1 2 1] sum,
+// built from row sums shared by three points, so a sweep is
+//     x' = k0 x + k1 V - c3 b,   k1 = c3 c/4,  k0 = c2 - 4 k1
+// (8 float64 operations a point instead of 11); other points take the
+// reference's expression (jacobi_bits).  The same function, another
+// rounding: the exact build keeps the sweep kernels.  Same points, inputs and
+// outputs as sweep1_body / sweep2_body.
+constexpr int SC_K = 4;
+
+template <typename T>
+struct SweepCArgs {
+    LevelView<T> L;
+    AnalyticT<T> an;
+    T c1, c2;
+    T c3z;         // c3 where the diagonal is 0: c1/|0|, computed on the host
+    T k0, k1;      // separable update constants
+    int second;    // 0: first sweep (x or zero -> t), 1: second (t -> x and its images)
+    int zero_x;
+    const int *active;
+};
+
+template <typename T>
+F2D_DEV void sweepc_body(const SweepCArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<T> L = A.L;
+    const AnalyticT<T> an = A.an;
+    const int mv = L.mv, nv = L.nv, second = A.second;
+    const int lo = second ? NH : 2, hj = second ? mv - NH - 1 : mv - 3,
+              hi = second ? nv - NH - 1 : nv - 3;
+    const int i = lo + vb.x * LV_TX + (int)threadIdx.x;
+    const int jb = lo + (vb.y * LV_TY + (int)threadIdx.y) * SC_K;
+    if (i > hi || jb > hj) return;
+    const T c2 = A.c2, c3z = A.c3z;
+    // b, bits and mask of the column's points (mk < 0: beyond the last row)
+    T bq[SC_K];
+    unsigned bt[SC_K];
+    int mk[SC_K];
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) {
+        const int j = jb + k;
+        bq[k] = (T)0;
+        bt[k] = 0u;
+        mk[k] = -1;
+        if (j <= hj) {
+            const size_t p = off(j, i, nv);
+            bq[k] = L.b[p];
+            bt[k] = L.nb[p];
+            mk[k] = L.msk[p];
+        }
+    }
+    T v[SC_K];
+    if (!second && A.zero_x) {
+#pragma unroll
+        for (int k = 0; k < SC_K; k++)
+            v[k] = mk[k] <= 0 ? (T)0 : ((bt[k] & 256u) ? an.c3 : c3z) * (-bq[k]);
+    } else {
+        const T *__restrict__ q = second ? L.t : L.x;
+        // rows jb-1 .. jb+SC_K, columns i-1 .. i+1 (rows past hj + 1 are not needed)
+        T w[SC_K + 2][3];
+#pragma unroll
+        for (int r = 0; r < SC_K + 2; r++) {
+            const int j = jb - 1 + r;
+            w[r][0] = w[r][1] = w[r][2] = (T)0;
+            if (j <= hj + 1) {
+                const T *row = q + off(j, i, nv);
+                w[r][0] = row[-1];
+                w[r][1] = row[0];
+                w[r][2] = row[1];
+            }
+        }
+        T h[SC_K + 2];
+#pragma unroll
+        for (int r = 0; r < SC_K + 2; r++) h[r] = fma((T)2, w[r][1], w[r][0] + w[r][2]);
+        bool full = true;
+#pragma unroll
+        for (int k = 0; k < SC_K; k++) full = full && (mk[k] <= 0 || bt[k] == 511u);
+        // the separable form alone for a warp whose points all have fluid
+        // blocks (no second expression for the compiler to predicate in)
+        if (__all_sync(__activemask(), full)) {
+#pragma unroll
+            for (int k = 0; k < SC_K; k++) {
+                const T V = fma((T)2, h[k + 1], h[k] + h[k + 2]);
+                const T u = fma(A.k1, V, fma(A.k0, w[k + 1][1], -an.c3 * bq[k]));
+                v[k] = mk[k] > 0 ? u : (T)0;
+            }
+        } else {
+#pragma unroll
+        for (int k = 0; k < SC_K; k++) {
+            v[k] = (T)0;
+            if (mk[k] <= 0) continue;
+            const unsigned bits = bt[k];
+            if (bits == 511u) {
+                const T V = fma((T)2, h[k + 1], h[k] + h[k + 2]);
+                v[k] = fma(A.k1, V, fma(A.k0, w[k + 1][1], -an.c3 * bq[k]));
+            } else {
+                const T c3 = (bits & 256u) ? an.c3 : c3z;
+                const T a0 = (bits & 1u) ? an.sc[0] : (T)0, a1 = (bits & 2u) ? an.sc[1] : (T)0,
+                        a2 = (bits & 4u) ? an.sc[2] : (T)0, a3 = (bits & 8u) ? an.sc[3] : (T)0,
+                        a4 = (bits & 16u) ? an.sc[3] : (T)0, a5 = (bits & 32u) ? an.sc[2] : (T)0,
+                        a6 = (bits & 64u) ? an.sc[1] : (T)0, a7 = (bits & 128u) ? an.sc[0] : (T)0;
+                v[k] = w[k + 1][1] * c2 + c3 * (+a0 * w[k][0]
+                                               + a1 * w[k][1]
+                                               + a2 * w[k][2]
+                                               + a3 * w[k + 1][0]
+                                               + a4 * w[k + 1][2]
+                                               + a5 * w[k + 2][0]
+                                               + a6 * w[k + 2][1]
+                                               + a7 * w[k + 2][2]
+                                               - bq[k]);
+            }
+        }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) {
+        if (mk[k] < 0) break;
+        const int j = jb + k;
+        if (second)
+            store_images(L.x, j, i, mv, nv, v[k]);
+        else
+            L.t[off(j, i, nv)] = v[k];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_sweepc(SweepCArgs<T> a) {
+    pdl_prologue();
+    sweepc_body<T>(a, F2D_VB_NATIVE);
+}
+
+// 1 (the product build's default): the float64 finest level's sweeps take
+// the column form where the operator is the 9-point one; 0: the sweep kernels
+int &separable_mode() {
+#ifdef F2D_EXACT
+    static int m = 0;
+#else
+    static int m = 1;
+#endif
+    return m;
+}
+
+// The finest level's two sweeps in column form; *done = false and nothing
+// launched when the mode is off, the operator is not the 9-point form with
+// corners = edges / 2, the level has no coefficient bits, or a step is being
+// recorded (a batch takes the sweep kernels: this kernel is not a batched
+// body).
+template <typename T>
+int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, bool zero_x,
+                     const int *active, cudaStream_t s, bool *done) {
+    *done = false;
+    if (!separable_mode() || recorder() != nullptr || !L.nb) return OK;
+    const T e = an.sc[1];
+    if (!(e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e && an.sc[2] == an.sc[0]))
+        return OK;
+    SweepCArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.L = L;
+    a.an = an;
+    a.c1 = c1;
+    a.c2 = c2;
+    a.c3z = c3_zero(c1);
+    a.k1 = an.c3 * e * (T)0.5;
+    a.k0 = c2 - (T)4 * a.k1;
+    a.zero_x = zero_x ? 1 : 0;
+    a.active = active;
+    const dim3 b(LV_TX, LV_TY);
+    // a grid of fewer CTAs than SMs is latency bound: four points a thread
+    // lose there to the sweep kernels' one
+    if ((long long)((L.nv - 4 + LV_TX - 1) / LV_TX) * ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K)) <
+        sm_count())
+        return OK;
+    for (int second = 0; second < 2; second++) {
+        a.second = second;
+        const int lo = second ? NH : 2;
+        const int rows = (second ? L.mv - NH - 1 : L.mv - 3) - lo + 1;
+        const int cols = (second ? L.nv - NH - 1 : L.nv - 3) - lo + 1;
+        const dim3 g((unsigned)((cols + LV_TX - 1) / LV_TX),
+                     (unsigned)((rows + LV_TY * SC_K - 1) / (LV_TY * SC_K)));
+        const int st = cuda_status((cudaError_t)launch_pdl(k_sweepc<T>, a, g, b, 0, s),
+                                   "mg_sweeps_column");
+        if (st) return st;
+    }
+    *done = true;
+    return OK;
+}
+template int mg_sweeps_column<double>(const LevelView<double> &, const AnalyticT<double> &, double,
+                                      double, bool, const int *, cudaStream_t, bool *);
+
 template <typename T>
 F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
@@ -779,7 +985,7 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
     int8_t *ms = (int8_t *)(nbs + SL_TW * SL_TW);
     const LevelView<T> L = A.L;
     const AnalyticT<T> an = A.an;
-    const T c2 = A.c2, c3z = A.c1 / fabs((T)0);  // c3 where the diagonal is 0
+    const T c2 = A.c2, c3z = A.c3z;  // c3 where the diagonal is 0
     const int xmode = A.xmode;
     const int mv = L.mv, nv = L.nv;
     const int i0 = NH + vb.x * SL_T, j0 = NH + vb.y * SL_T;
@@ -910,7 +1116,7 @@ int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, i
     if (an && L.nb && sizeof(T) == 4) {  // the float finest level
         CoarseSrc<T> cs{nullptr, nullptr, 0};
         if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
-        SmoothFusedArgs<T> a{L, *an, c1, c2, xmode, cs, out, active, SL_T, SL_T};
+        SmoothFusedArgs<T> a{L, *an, c1, c2, xmode, cs, out, active, SL_T, SL_T, c3_zero(c1)};
         const dim3 g = grid2d(L.mv - 2 * NH, L.nv - 2 * NH, dim3(SL_T, SL_T));
         return launch_body<BSmoothL0<T>>(k_smooth_l0<T>, a, g, dim3(SL_THREADS),
                                          smooth_l0_smem<T>(), s, "mg_smooth_l0");
@@ -922,7 +1128,7 @@ int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, i
     CoarseSrc<T> cs{nullptr, nullptr, 0};
     if (coarse) cs = CoarseSrc<T>{coarse->msk, coarse->x, coarse->nv};
     SmoothFusedArgs<T> a{L,   an ? *an : AnalyticT<T>{}, c1, c2, xmode, cs, out, active,
-                         (int)tile.x, (int)tile.y};
+                         (int)tile.x, (int)tile.y, c3_zero(c1)};
     if (an)
         return launch_body<BSmoothFused<T, true>>(k_smooth_fused<T, true>, a, g, b, smem, s,
                                                   "mg_smooth_fused");
@@ -1123,7 +1329,7 @@ F2D_DEV void co_smooth(unsigned char *sm, const CoLv &d, T c1, T c2, bool zero_x
     if (co_enter(sc, L.mv * L.nv, nt)) {
         CO_FOR(2, L.mv - 3, 2, L.nv - 3, nt)
         L.t[off(j, i, L.nv)] = jacobi<T, false>(L, nullptr, zero_x ? nullptr : L.x, L.b, j, i,
-                                                c1, c2);
+                                                c1, c2);  // stored level: c3 from its A plane
         co_leave(nt);
         CO_FOR(NH, L.mv - NH - 1, NH, L.nv - NH - 1, nt)
         store_images(L.x, j, i, L.mv, L.nv, jacobi<T, false>(L, nullptr, L.t, L.b, j, i, c1, c2));
@@ -1782,6 +1988,18 @@ extern "C" {
 int f2d_set_level_tiles(int target) {
     const int prev = f2d::level_tile_target();
     if (target >= -1) f2d::level_tile_target() = target;
+    return prev;
+}
+
+// the float64 finest level's sweeps: 1 the column form where the operator
+// allows (the product build's default), 0 the sweep kernels in the
+// reference's order; < 0 only queries; returns the previous setting.  The
+// exact build always takes the sweeps (0).
+int f2d_set_separable(int mode) {
+    const int prev = f2d::separable_mode();
+#ifndef F2D_EXACT
+    if (mode == 0 || mode == 1) f2d::separable_mode() = mode;
+#endif
     return prev;
 }
 

@@ -319,6 +319,16 @@ int f2d_set_pdl(int enable);
  * graphs captured before a change keep their tiles. */
 int f2d_set_level_tiles(int target);
 
+/* The float64 finest level's smoother (no counterpart in the reference: an
+ * arithmetic form): 1 (the product build's default) each thread takes a
+ * column of four points with their neighbourhood in registers, and a point
+ * whose 3x3 block is fluid goes through the separable form of the analytic
+ * 9-point operator (8 float64 operations instead of 11; the same function,
+ * other rounding); 0 the sweep kernels in the reference's order of
+ * operations.  < 0 queries; returns the previous setting.  The exact build
+ * always uses 0; graphs captured before a change keep their kernels. */
+int f2d_set_separable(int mode);
+
 /* Threads of the fused level smoother's CTA: 0 one per tile point (the
  * input ring and the first sweep's ring take a second pass; default), 1 one
  * per input point, so that every phase is one pass, for grids of fewer than

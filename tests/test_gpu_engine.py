@@ -241,6 +241,56 @@ def test_coarse_operator_matches_the_cycle(eng, name, precision):
             assert relerr(on[k], off[k]) <= max(1e-12, 10 * fma), (level, k, fma)
 
 
+@pytest.mark.parametrize("name", ["euler-perio-turb", "euler-closed-dipole", "euler-closed-islands",
+                                  "boussinesq-xchannel", "qg-closed", "euler-closed-5point"])
+def test_column_sweeps_match_the_sweep_kernels(eng, name):
+    """The float64 finest level's sweeps in column form (four points a
+    thread, neighbourhoods in registers, fluid 3x3 blocks through the
+    separable form of the 9-point operator) compute the reference's function
+    in another order of operations: the states after four steps agree with
+    the sweep kernels (reference order) to the product build's rounding, on
+    periodic and closed domains, islands, the Helmholtz operator of QG and a
+    5-point operator (dx != dy: the sweep kernels run); a replayed graph
+    gives the eager steps' bits."""
+    import torch
+    from fluid2d_gb300 import _lib
+    from fluid2d_gb300 import workloads as W
+    wls = dict(_workloads())
+    wls["euler-closed-5point"] = W.dipole(64, 48, seed=2)
+    wl = wls[name]
+    P = _lib.lib("product")
+
+    def run(mode, graph=False):
+        old = P.f2d_set_separable(mode)
+        try:
+            kw = {"Rd": 0.3, "beta": 2.0} if wl["model"] == "quasigeostrophic" else {}
+            M = eng.from_workload(wl, dt=1e-3, **kw)
+            M.set_psi_from_vorticity()
+            M.diagnostics()
+            if graph:
+                s = torch.cuda.Stream()
+                with torch.cuda.stream(s):
+                    M.run(4, graph=True)
+                s.synchronize()
+            else:
+                M.run(4)
+            torch.cuda.synchronize()
+            return M.var.state.cpu().numpy()
+        finally:
+            P.f2d_set_separable(old)
+
+    assert P.f2d_set_separable(-1) == 1
+    a, b, g = run(1), run(0), run(1, graph=True)
+    # u and v (planes 2 and 3 of every model) against the velocity's scale:
+    # v is ~0 in the parallel shear flow
+    vel = max(np.abs(b[2]).max(), np.abs(b[3]).max())
+    for k in range(a.shape[0]):
+        scale = vel if k in (2, 3) else max(np.abs(b[k]).max(), 1e-300)
+        assert np.abs(a[k] - b[k]).max() <= 1e-12 * scale, k
+        assert np.array_equal(a[k], g[k]), k
+    assert _lib.lib("exact").f2d_set_separable(-1) == 0
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_level_tiles_change_nothing_but_launches(eng, precision):
     """Every CTA tile target and smoother block size of the level kernels

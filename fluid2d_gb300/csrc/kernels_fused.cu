@@ -316,6 +316,12 @@ struct ResidualArgs {
     const int *active;
 };
 
+// the finest level's residual in column form; false: not launched (the
+// residual kernels apply)
+template <typename T>
+bool residual_column(const LevelView<T> &L, const AnalyticT<T> &an, const T *x, const T *b, T *r,
+                     float *rf, const int *active, cudaStream_t s, int *st);
+
 template <typename T, bool L0>
 F2D_DEV void residual_body(const ResidualArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
@@ -359,6 +365,8 @@ F2D_BATCH_ENTRY(ResidualMixed, BResidualMixed)
 
 int mg_residual_mixed(const LevelView<double> &L, const Analytic &an, const double *x,
                       const double *b, double *r, float *rf, const int *active, cudaStream_t s) {
+    int st = OK;
+    if (residual_column<double>(L, an, x, b, r, rf, active, s, &st)) return st;
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
     return launch_body<BResidualMixed>(k_residual_mixed, ResidualArgs<double>{L, an, x, b, r, rf,
                                                                               active},
@@ -527,6 +535,10 @@ int mg_residual(const LevelView<T> &L, const AnalyticT<T> *an, const T *x, const
                 const int *active, cudaStream_t s) {
     dim3 g = lv_grid(L.mv - 2 * NH, L.nv - 2 * NH), bl(LV_TX, LV_TY);
     ResidualArgs<T> a{L, an ? *an : AnalyticT<T>{}, x, b, r, nullptr, active};
+    if constexpr (sizeof(T) == 8) {
+        int st = OK;
+        if (an && residual_column<T>(L, *an, x, b, r, nullptr, active, s, &st)) return st;
+    }
     if (an)
         return launch_body<BResidual<T, true>>(k_residual<T, true>, a, g, bl, 0, s, "mg_residual");
     return launch_body<BResidual<T, false>>(k_residual<T, false>, a, g, bl, 0, s, "mg_residual");
@@ -916,8 +928,156 @@ __global__ void __launch_bounds__(LV_TX *LV_TY) k_sweepc(SweepCArgs<T> a) {
     sweepc_body<T>(a, F2D_VB_NATIVE);
 }
 
-// 1 (the product build's default): the float64 finest level's sweeps take
-// the column form where the operator is the 9-point one; 0: the sweep kernels
+int &separable_mode();
+// The finest level's residual r = b - A x (core/gmg/fortran_multigrid.f90:
+// 340-357) in the same column form: with corners e/2 and edges e, on a fluid
+// block A x = (e/2) V + (a5 - 2e) x, so r = b + kv V + kx x with kv = -e/2,
+// kx = 2e - a5 (7 float64 operations a point instead of 10); other points
+// take the reference's expression.  r is written with its periodic images
+// and, for the mixed form, a float copy rf.  Same points, inputs and outputs
+// as residual_body / residual_mixed_body.
+template <typename T>
+struct ResidualCArgs {
+    LevelView<T> L;
+    AnalyticT<T> an;
+    const T *x, *b;
+    T *r;
+    float *rf;
+    T kv, kx;  // on a fluid block: r = b + kv V + kx x
+    const int *active;
+};
+
+template <typename T>
+F2D_DEV void residualc_body(const ResidualCArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<T> L = A.L;
+    const AnalyticT<T> an = A.an;
+    const int mv = L.mv, nv = L.nv;
+    const int hj = mv - NH - 1, hi = nv - NH - 1;
+    const int i = NH + vb.x * LV_TX + (int)threadIdx.x;
+    const int jb = NH + (vb.y * LV_TY + (int)threadIdx.y) * SC_K;
+    if (i > hi || jb > hj) return;
+    const T *__restrict__ q = A.x;
+    T bq[SC_K];
+    unsigned bt[SC_K];
+    int mk[SC_K];
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) {
+        const int j = jb + k;
+        bq[k] = (T)0;
+        bt[k] = 0u;
+        mk[k] = -1;
+        if (j <= hj) {
+            const size_t p = off(j, i, nv);
+            bq[k] = A.b[p];
+            bt[k] = L.nb[p];
+            mk[k] = L.msk[p];
+        }
+    }
+    T w[SC_K + 2][3];
+#pragma unroll
+    for (int r = 0; r < SC_K + 2; r++) {
+        const int j = jb - 1 + r;
+        w[r][0] = w[r][1] = w[r][2] = (T)0;
+        if (j <= hj + 1) {
+            const T *row = q + off(j, i, nv);
+            w[r][0] = row[-1];
+            w[r][1] = row[0];
+            w[r][2] = row[1];
+        }
+    }
+    T h[SC_K + 2];
+#pragma unroll
+    for (int r = 0; r < SC_K + 2; r++) h[r] = fma((T)2, w[r][1], w[r][0] + w[r][2]);
+    bool full = true;
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) full = full && (mk[k] <= 0 || bt[k] == 511u);
+    T v[SC_K];
+    if (__all_sync(__activemask(), full)) {
+#pragma unroll
+        for (int k = 0; k < SC_K; k++) {
+            const T V = fma((T)2, h[k + 1], h[k] + h[k + 2]);
+            const T u = fma(A.kv, V, fma(A.kx, w[k + 1][1], bq[k]));
+            v[k] = mk[k] > 0 ? u : (T)0;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < SC_K; k++) {
+            v[k] = (T)0;
+            if (mk[k] <= 0) continue;
+            const unsigned bits = bt[k];
+            if (bits == 511u) {
+                const T V = fma((T)2, h[k + 1], h[k] + h[k + 2]);
+                v[k] = fma(A.kv, V, fma(A.kx, w[k + 1][1], bq[k]));
+            } else {
+                const T a0 = (bits & 1u) ? an.sc[0] : (T)0, a1 = (bits & 2u) ? an.sc[1] : (T)0,
+                        a2 = (bits & 4u) ? an.sc[2] : (T)0, a3 = (bits & 8u) ? an.sc[3] : (T)0,
+                        a4 = (bits & 16u) ? an.sc[3] : (T)0, a5 = (bits & 32u) ? an.sc[2] : (T)0,
+                        a6 = (bits & 64u) ? an.sc[1] : (T)0, a7 = (bits & 128u) ? an.sc[0] : (T)0;
+                const T d = (bits & 256u) ? an.a5 : (T)0;
+                v[k] = bq[k]
+                    - a0 * w[k][0]
+                    - a1 * w[k][1]
+                    - a2 * w[k][2]
+                    - a3 * w[k + 1][0]
+                    - d * w[k + 1][1]
+                    - a4 * w[k + 1][2]
+                    - a5 * w[k + 2][0]
+                    - a6 * w[k + 2][1]
+                    - a7 * w[k + 2][2];
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) {
+        if (mk[k] < 0) break;
+        const int j = jb + k;
+        store_images(A.r, j, i, mv, nv, v[k]);
+        if (A.rf) store_images(A.rf, j, i, mv, nv, (float)v[k]);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_residualc(ResidualCArgs<T> a) {
+    pdl_prologue();
+    residualc_body<T>(a, F2D_VB_NATIVE);
+}
+
+// false (nothing launched) where the column form does not apply: the
+// separable mode off, no coefficient bits, not the 9-point operator with
+// corners = edges / 2, a step being recorded, a grid of fewer CTAs than SMs
+template <typename T>
+bool residual_column(const LevelView<T> &L, const AnalyticT<T> &an, const T *x, const T *b, T *r,
+                     float *rf, const int *active, cudaStream_t s, int *st) {
+    *st = OK;
+    if (!separable_mode() || recorder() != nullptr || !L.nb) return false;
+    const T e = an.sc[1];
+    if (!(e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e && an.sc[2] == an.sc[0]))
+        return false;
+    const int rows = L.mv - 2 * NH, cols = L.nv - 2 * NH;
+    const dim3 g((unsigned)((cols + LV_TX - 1) / LV_TX),
+                 (unsigned)((rows + LV_TY * SC_K - 1) / (LV_TY * SC_K)));
+    if (separable_mode() == 1 && (long long)g.x * g.y < sm_count()) return false;
+    ResidualCArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.L = L;
+    a.an = an;
+    a.x = x;
+    a.b = b;
+    a.r = r;
+    a.rf = rf;
+    a.kv = -an.sc[0];                // -e/2
+    a.kx = (T)4 * an.sc[0] - an.a5;  // 2e - a5
+    a.active = active;
+    *st = cuda_status((cudaError_t)launch_pdl(k_residualc<T>, a, g, dim3(LV_TX, LV_TY), 0, s),
+                      "mg_residual column");
+    return true;
+}
+
+// 1 (the product build's default): the float64 finest level's sweeps and
+// residual take the column form where the operator is the 9-point one and
+// the grid has at least one CTA per SM; 2: at every grid size; 0: the sweep
+// and residual kernels
 int &separable_mode() {
 #ifdef F2D_EXACT
     static int m = 0;
@@ -954,8 +1114,9 @@ int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, 
     const dim3 b(LV_TX, LV_TY);
     // a grid of fewer CTAs than SMs is latency bound: four points a thread
     // lose there to the sweep kernels' one
-    if ((long long)((L.nv - 4 + LV_TX - 1) / LV_TX) * ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K)) <
-        sm_count())
+    if (separable_mode() == 1 &&
+        (long long)((L.nv - 4 + LV_TX - 1) / LV_TX) * ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K)) <
+            sm_count())
         return OK;
     for (int second = 0; second < 2; second++) {
         a.second = second;
@@ -971,6 +1132,9 @@ int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, 
     *done = true;
     return OK;
 }
+template bool residual_column<double>(const LevelView<double> &, const AnalyticT<double> &,
+                                     const double *, const double *, double *, float *,
+                                     const int *, cudaStream_t, int *);
 template int mg_sweeps_column<double>(const LevelView<double> &, const AnalyticT<double> &, double,
                                       double, bool, const int *, cudaStream_t, bool *);
 
@@ -1991,14 +2155,15 @@ int f2d_set_level_tiles(int target) {
     return prev;
 }
 
-// the float64 finest level's sweeps: 1 the column form where the operator
-// allows (the product build's default), 0 the sweep kernels in the
-// reference's order; < 0 only queries; returns the previous setting.  The
-// exact build always takes the sweeps (0).
+// the float64 finest level's sweeps and residual: 1 the column form where
+// the operator allows on grids of at least one CTA per SM (the product
+// build's default), 2 at every grid size, 0 the sweep and residual kernels
+// in the reference's order; < 0 only queries; returns the previous setting.
+// The exact build always takes the reference's order (0).
 int f2d_set_separable(int mode) {
     const int prev = f2d::separable_mode();
 #ifndef F2D_EXACT
-    if (mode == 0 || mode == 1) f2d::separable_mode() = mode;
+    if (mode >= 0 && mode <= 2) f2d::separable_mode() = mode;
 #endif
     return prev;
 }

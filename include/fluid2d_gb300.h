@@ -319,12 +319,14 @@ int f2d_set_pdl(int enable);
  * graphs captured before a change keep their tiles. */
 int f2d_set_level_tiles(int target);
 
-/* The float64 finest level's smoother (no counterpart in the reference: an
- * arithmetic form): 1 (the product build's default) each thread takes a
- * column of four points with their neighbourhood in registers, and a point
- * whose 3x3 block is fluid goes through the separable form of the analytic
- * 9-point operator (8 float64 operations instead of 11; the same function,
- * other rounding); 0 the sweep kernels in the reference's order of
+/* The float64 finest level's smoother sweeps and residual (no counterpart in
+ * the reference: an arithmetic form): 1 (the product build's default) on
+ * grids of at least one CTA per SM, each thread takes a column of four points
+ * with their neighbourhood in registers, and a point whose 3x3 block is
+ * fluid goes through the separable form of the analytic 9-point operator
+ * (8 float64 operations instead of 11 a sweep point, 7 instead of 10 a
+ * residual point; the same function, other rounding); 2 the same at every
+ * grid size; 0 the sweep and residual kernels in the reference's order of
  * operations.  < 0 queries; returns the previous setting.  The exact build
  * always uses 0; graphs captured before a change keep their kernels. */
 int f2d_set_separable(int mode);

@@ -1801,10 +1801,13 @@ int mg_coarse_apply(const T *op, int n, const LevelView<T> &L, const int *active
 }
 
 // ------------------------------------------------------------ stage kernels
-F2D_DEV double rk_combine(int rk, double base, double d0, double d1, double dq, double dt) {
+// dt6 = dt/6, divided once a CTA (a float64 division costs a point's worth
+// of FMAs, and a warp pays it whatever its active lanes)
+F2D_DEV double rk_combine(int rk, double base, double d0, double d1, double dq, double dt,
+                          double dt6) {
     if (rk == 1) return base + dt * dq;                                  // x + dt*dx0
     if (rk == 2) return base + (0.25 * dt) * (d0 + dq);                  // x + (dt/4)(dx0+dx1)
-    return base + (dt / 6.) * (d0 + d1 + 4 * dq);                        // x + (dt/6)(...)
+    return base + dt6 * (d0 + d1 + 4 * dq);                              // x + (dt/6)(...)
 }
 
 // Advection of one tracer with the halo fill, the Boussinesq torque and the
@@ -1816,7 +1819,9 @@ template <typename TC>
 F2D_DEV void stage_adv_body(const AdvStage &a, const VB vb) {
     __shared__ TC sfx[8][33];
     __shared__ TC sfy[9][32];
+    __shared__ double sdt6;
     const int tx = threadIdx.x, ty = threadIdx.y;
+    if (tx == 0 && ty == 0 && a.rk == 3) sdt6 = *a.dt / 6.;
     const int nv = a.nv, mv = a.mv;
     const int I = NH + vb.x * 32 + tx;
     const int J = NH + vb.y * 8 + ty;
@@ -1859,12 +1864,13 @@ F2D_DEV void stage_adv_body(const AdvStage &a, const VB vb) {
                            (double)a.msk[p + nv] * (a.q[p + nv] - t);
         y = y + a.diff_coef * lap;
     }
-    const double dt = a.rk ? *a.dt : 0.;
+    const double dt = a.rk ? *a.dt : 0., dt6 = a.rk == 3 ? sdt6 : 0.;
     // the point and its periodic halo images (store_images' positions)
     auto put = [&](size_t q) {
         a.dq[q] = y;
         if (a.rk)
-            a.out[q] = rk_combine(a.rk, a.base[q], a.d0 ? a.d0[q] : 0., a.d1 ? a.d1[q] : 0., y, dt);
+            a.out[q] = rk_combine(a.rk, a.base[q], a.d0 ? a.d0[q] : 0., a.d1 ? a.d1[q] : 0., y, dt,
+                                  dt6);
     };
     for_images(J, I, mv, nv, put);
 }
@@ -1899,6 +1905,9 @@ int stage_advection(const AdvStage &a, cudaStream_t s) {
 // u,v = orthogradient(psi) (core/fortran_operators.f90:22-37), with the RK
 // combinations of u, v (rows/cols 1..m-2) and of psi fused.
 F2D_DEV void stage_ortho_body(const OrthoStage &a, const VB vb) {
+    __shared__ double sdt6;
+    if (threadIdx.x == 0 && threadIdx.y == 0 && (a.rk == 3 || a.psi_rk)) sdt6 = *a.dt / 6.;
+    __syncthreads();
     const int i = vb.x * 32 + threadIdx.x;
     const int j = vb.y * 8 + threadIdx.y;
     const int nv = a.nv, mv = a.mv;
@@ -1908,12 +1917,13 @@ F2D_DEV void stage_ortho_body(const OrthoStage &a, const VB vb) {
     // thread masks them give the same value
     const double pc = (a.premasked || a.mskp[p]) ? a.psi[p] : 0.;
     const double dt = (a.rk || a.psi_rk) ? *a.dt : 0.;
+    const double dt6 = (a.rk == 3 || a.psi_rk) ? sdt6 : 0.;
     if (!a.premasked) a.psi[p] = pc;
     if (a.psi_rk) {
         // x += (dt/6)*(dx0 + dx1 + 4*dx2) (core/timescheme.py:180)
         const double d1 = a.psi1 ? a.psi1[p] : pc;
         const double d2 = a.psi1 ? pc : 0.;
-        a.psiout[p] = a.psibase[p] + (dt / 6.) * (a.psi0[p] + d1 + 4 * d2);
+        a.psiout[p] = a.psibase[p] + dt6 * (a.psi0[p] + d1 + 4 * d2);
     }
     if (i < 1 || j < 1 || i > nv - 2 || j > mv - 2) return;
     const double ps = (a.premasked || a.mskp[p - nv]) ? a.psi[p - nv] : 0.;
@@ -1924,8 +1934,10 @@ F2D_DEV void stage_ortho_body(const OrthoStage &a, const VB vb) {
     a.u[p] = u;
     a.v[p] = v;
     if (a.rk) {
-        a.uout[p] = rk_combine(a.rk, a.ubase[p], a.u0 ? a.u0[p] : 0., a.u1 ? a.u1[p] : 0., u, dt);
-        a.vout[p] = rk_combine(a.rk, a.vbase[p], a.v0 ? a.v0[p] : 0., a.v1 ? a.v1[p] : 0., v, dt);
+        a.uout[p] = rk_combine(a.rk, a.ubase[p], a.u0 ? a.u0[p] : 0., a.u1 ? a.u1[p] : 0., u, dt,
+                               dt6);
+        a.vout[p] = rk_combine(a.rk, a.vbase[p], a.v0 ? a.v0[p] : 0., a.v1 ? a.v1[p] : 0., v, dt,
+                               dt6);
     }
 }
 

@@ -95,7 +95,9 @@ F2D_DEV float rk_stage_f32(int rk, float base, float d0, float dq, float dt) {
 F2D_DEV void stage_adv_mixed_body(const AdvMixed &a, const VB vb) {
     __shared__ float sfx[8][33];
     __shared__ float sfy[9][32];
+    __shared__ float sdt6;  // dt/6 of the final combination, divided once a CTA
     const int tx = threadIdx.x, ty = threadIdx.y;
+    if (tx == 0 && ty == 0 && a.rk == 3) sdt6 = a.dtf[0] / 6.f;
     const int nv = a.nv, mv = a.mv;
     const int I = NH + vb.x * 32 + tx;
     const int J = NH + vb.y * 8 + ty;
@@ -134,14 +136,14 @@ F2D_DEV void stage_adv_mixed_body(const AdvMixed &a, const VB vb) {
                           (float)a.msk[p + nv] * (a.q[p + nv] - t);
         y = y + a.diff_coef * lap;
     }
-    const float dt = a.dtf[0];
+    const float dt = a.dtf[0], dt6 = a.rk == 3 ? sdt6 : 0.f;
     // the point and its periodic halo images
     for_images(J, I, mv, nv, [&](size_t q) {
         a.dq[q] = y;
         if (a.rk < 3) {
             a.sout[q] = rk_stage_f32(a.rk, a.sbase[q], a.d0 ? a.d0[q] : 0.f, y, dt);
         } else {
-            const float inc = (dt / 6.f) * (a.d0[q] + a.d1[q] + 4.f * y);
+            const float inc = dt6 * (a.d0[q] + a.d1[q] + 4.f * y);
             a.xout[q] = a.xout[q] + (double)inc;
         }
     });
@@ -169,6 +171,14 @@ int stage_advection_mixed(const AdvMixed &a, cudaStream_t s) {
 // (the differences of psi need it) stored as float tendencies, and the
 // stage-state / final combinations.
 F2D_DEV void stage_ortho_mixed_body(const OrthoMixed &a, const VB vb) {
+    // dt/6 in float64 (psi) and float (u, v), divided once a CTA
+    __shared__ double sdt6;
+    __shared__ float sdt6f;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        if (a.psi_rk) sdt6 = *a.dt / 6.;
+        if (a.rk == 3) sdt6f = a.dtf[0] / 6.f;
+    }
+    __syncthreads();
     const int i = vb.x * 32 + threadIdx.x;
     const int j = vb.y * 8 + threadIdx.y;
     const int nv = a.nv, mv = a.mv;
@@ -177,10 +187,9 @@ F2D_DEV void stage_ortho_mixed_body(const OrthoMixed &a, const VB vb) {
     const double pc = a.mskp[p] ? a.psi[p] : 0.;
     a.psi[p] = pc;
     if (a.psi_rk) {
-        const double dt = *a.dt;
         const double d1 = a.psi1 ? a.psi1[p] : pc;
         const double d2 = a.psi1 ? pc : 0.;
-        a.psiout[p] = a.psibase[p] + (dt / 6.) * (a.psi0[p] + d1 + 4 * d2);
+        a.psiout[p] = a.psibase[p] + sdt6 * (a.psi0[p] + d1 + 4 * d2);
     }
     if (i < 1 || j < 1 || i > nv - 2 || j > mv - 2) return;
     const double ps = a.mskp[p - nv] ? a.psi[p - nv] : 0.;
@@ -195,8 +204,8 @@ F2D_DEV void stage_ortho_mixed_body(const OrthoMixed &a, const VB vb) {
         a.su[p] = rk_stage_f32(a.rk, a.ubase[p], a.u0 ? a.u0[p] : 0.f, u, dt);
         a.sv[p] = rk_stage_f32(a.rk, a.vbase[p], a.v0 ? a.v0[p] : 0.f, v, dt);
     } else if (a.rk == 3) {
-        a.xu[p] = a.xu[p] + (double)((dt / 6.f) * (a.u0[p] + a.u1[p] + 4.f * u));
-        a.xv[p] = a.xv[p] + (double)((dt / 6.f) * (a.v0[p] + a.v1[p] + 4.f * v));
+        a.xu[p] = a.xu[p] + (double)(sdt6f * (a.u0[p] + a.u1[p] + 4.f * u));
+        a.xv[p] = a.xv[p] + (double)(sdt6f * (a.v0[p] + a.v1[p] + 4.f * v));
     }
 }
 

@@ -217,7 +217,7 @@ def _cpu_worker(args):
 # every SM, CUDA events), used only if the live measurement (f2d_fp64_peak)
 # fails: the FP64-ALU roofline of the float64 kernels
 FP64_PEAK_TFLOPS = 1.20
-SMOOTH_DRAM_BYTES_PER_POINT = (20111360 + 0 + 20073472 + 0) / 1060900.
+SMOOTH_DRAM_BYTES_PER_POINT = (20118016 + 0 + 20078848 + 0) / 1060900.
 
 
 def cpu_run(jobs, cores):
@@ -460,7 +460,9 @@ def smoother_roofline(n, probe_ms, nprobe):
     the float64 pipe: 19 flops per point per sweep (1 mul, 7 fma, 1 sub,
     1 mul, 1 fma), two sweeps per call, over the call's mean CUDA-event
     duration inside the replayed step graph; peak = float64 FMA chains
-    measured live on this GPU (f2d_fp64_peak).  Beside it, the same call
+    measured live on this GPU (f2d_fp64_peak).  The flops are the
+    algorithm's: the column form (k_sweepc) executes fewer float64
+    instructions for the same sweep.  Beside it, the same call
     against HBM: x, b read, x written (8 B each) and the mask (1 B) = 25 B
     per point, with the DRAM traffic of an ncu capture of the same kernels."""
     pts = (n + 6) * (n + 6)
@@ -485,7 +487,7 @@ def smoother_roofline(n, probe_ms, nprobe):
     alg_bytes = 25 * pts
     hbm = alg_bytes / (probe_ms * 1e-3) / 1e9 if probe_ms > 0 else None
     # dram__bytes_read.sum + dram__bytes_write.sum of one call per grid point
-    # (ncu capture of the 1024^2 turbulence step)
+    # (ncu capture of k_sweepc, the column form, in the 1024^2 turbulence step)
     traffic = SMOOTH_DRAM_BYTES_PER_POINT * pts
     return {"kernel": "finest-level smoother (smoothtwicewitha: the two float64 sweeps)",
             "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",

@@ -306,6 +306,11 @@ struct Gmg {
     // core/gmg/level.py:153-163): elimination factors per level
     bool tri = false;
     double *gam[MAX_LEVELS] = {}, *bet[MAX_LEVELS] = {};
+    // levels >= 1 (float64 product build): flags of the points whose stored
+    // stencil is the level's uniform one (null: none) and that stencil
+    // (c, ey, ex, c3), for the column-form sweeps
+    uint8_t *ufl[MAX_LEVELS] = {};
+    double ust[MAX_LEVELS][4] = {};
     template <typename T>
     int smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream_t s);
     template <typename T>
@@ -460,6 +465,13 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
             o_gam[l] = mem.add(sizeof(double) * (size_t)mv[l] * nv[l]);
             o_bet[l] = mem.add(sizeof(double) * (size_t)mv[l] * nv[l]);
         }
+    size_t o_uf[MAX_LEVELS] = {}, o_smp = 0;
+#ifndef F2D_EXACT
+    if (!tri) {
+        for (int l = 1; l < nlev; l++) o_uf[l] = mem.add((size_t)mv[l] * nv[l]);
+        o_smp = mem.add(sizeof(double) * 80 * MAX_LEVELS);
+    }
+#endif
     TRY(mem.alloc());
     work = mem.at<double>(o_work);
     sums = mem.at<double>(o_sums);
@@ -552,6 +564,24 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
                                                     f32 ? (float *)f[l].A : nullptr, pl);
         TRY(launch_status("finalize A"));
     }
+#ifndef F2D_EXACT
+    // the stored levels' uniform stencils (product build, column-form sweeps)
+    if (!tri && nlev > 1) {
+        double *smp = mem.at<double>(o_smp);
+        for (int l = 1; l < nlev; l++) TRY(mg_stencil_samples(d[l], smp + 80 * l, s));
+        double h[80 * MAX_LEVELS];
+        TRY(cuda_status(cudaMemcpyAsync(h, smp, sizeof(double) * 80 * nlev,
+                                        cudaMemcpyDeviceToHost, s),
+                        "stencil samples copy"));
+        TRY(cuda_status(cudaStreamSynchronize(s), "stencil samples sync"));
+        for (int l = 1; l < nlev; l++) {
+            ufl[l] = nullptr;
+            if (!mg_uniform_choose(h + 80 * l, ust[l])) continue;
+            ufl[l] = mem.at<uint8_t>(o_uf[l]);
+            TRY(mg_uniform_flags(d[l], ust[l], ufl[l], s));
+        }
+    }
+#endif
     for (int l = 0; l < nlev; l++) {
         size_t pl = (size_t)mv[l] * nv[l];
         TRY(cuda_status(cudaMemsetAsync(d[l].r, 0, pl * sizeof(double), s), "clear"));
@@ -604,11 +634,24 @@ int Gmg::smooth(LevelView<T> *L, int l, int xmode, const int *active, cudaStream
             }
         }
     } else if (fused<T>(l)) {
-        TRY(mg_smooth_fused<T>(L[l], a0, c1, c2, xmode, xmode >= X_PLUS_INTERP ? &L[l + 1] : nullptr,
-                               L[l].t, active, s));
-        T *tmp = L[l].x;
-        L[l].x = L[l].t;
-        L[l].t = tmp;
+        // a float64 stored level large enough for the column form (product
+        // build): prolongation, then the two sweeps
+        bool col = false;
+        if constexpr (sizeof(T) == 8) col = ufl[l] != nullptr && column_applies<T>(L[l]);
+        if (col) {
+            if constexpr (sizeof(T) == 8) {
+                if (xmode == X_PLUS_INTERP || xmode == X_INTERP)
+                    TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, xmode == X_INTERP, active,
+                                     s));
+                TRY(mg_sweeps_uniform<T>(L[l], ufl[l], ust[l], c1, c2, xmode == X_ZERO, active, s));
+            }
+        } else {
+            TRY(mg_smooth_fused<T>(L[l], a0, c1, c2, xmode,
+                                   xmode >= X_PLUS_INTERP ? &L[l + 1] : nullptr, L[l].t, active, s));
+            T *tmp = L[l].x;
+            L[l].x = L[l].t;
+            L[l].t = tmp;
+        }
     } else {
         if (xmode == X_PLUS_INTERP || xmode == X_INTERP)
             TRY(mg_interp<T>(L[l + 1], L[l + 1].x, L[l], L[l].x, xmode == X_INTERP, active, s));

@@ -116,6 +116,19 @@ int mg_smooth_fused(const LevelView<T> &L, const AnalyticT<T> *an, T c1, T c2, i
 template <typename T>
 int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, bool zero_x,
                      const int *active, cudaStream_t s, bool *done);
+// a stored level's two sweeps in column form on its uniform-stencil points
+// (flags uf, stencil st = (c, ey, ex, c3) from mg_uniform_setup; float64
+// product build); call where column_applies(L)
+template <typename T>
+int mg_sweeps_uniform(const LevelView<T> &L, const uint8_t *uf, const T *st, T c1, T c2,
+                      bool zero_x, const int *active, cudaStream_t s);
+template <typename T>
+bool column_applies(const LevelView<T> &L);
+// set-up of a stored level's uniform stencil: 16 samples (5 doubles each)
+// of its stencil into out, the choice on the host, the flags on the device
+int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s);
+bool mg_uniform_choose(const double *h, double *st);
+int mg_uniform_flags(const LevelView<double> &L, const double *st, uint8_t *uf, cudaStream_t s);
 // residual of L (x, b) restricted into the coarse b2
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,

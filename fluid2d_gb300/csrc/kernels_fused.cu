@@ -1138,6 +1138,222 @@ template bool residual_column<double>(const LevelView<double> &, const AnalyticT
 template int mg_sweeps_column<double>(const LevelView<double> &, const AnalyticT<double> &, double,
                                       double, bool, const int *, cudaStream_t, bool *);
 
+// ---- the same column form on a stored level (levels >= 1, float64 product
+// build).  Where the stored stencil of a point is the level's uniform one
+// (flag uf = 1: corners c, vertical edges ey, horizontal edges ex and c3 as
+// chosen at set-up), the sum of its 8 neighbours is
+//     c (s[j-1] + s[j+1]) + ey (x[j-1][i] + x[j+1][i]) + ex s[j],
+// s[r] = x[r][i-1] + x[r][i+1] shared down the column, and the damped
+// Jacobi update x' = c2 x + c3 (sum - b) takes 8.5 float64 operations a point
+// instead of 11 (and no coefficient loads); other points take the
+// reference's expression (jacobi, core/gmg/fortran_multigrid.f90:66-85).
+template <typename T>
+struct SweepUArgs {
+    LevelView<T> L;
+    const uint8_t *uf;
+    T kc, key, kex;  // c3 c, c3 ey, c3 ex
+    T c2, c3u;       // 1 - omega; the uniform points' c3
+    int second, zero_x;
+    const int *active;
+};
+
+template <typename T>
+F2D_DEV void sweepu_body(const SweepUArgs<T> &A, const VB vb) {
+    if (inactive(A.active)) return;
+    const LevelView<T> L = A.L;
+    const int mv = L.mv, nv = L.nv, second = A.second;
+    const int lo = second ? NH : 2, hj = second ? mv - NH - 1 : mv - 3,
+              hi = second ? nv - NH - 1 : nv - 3;
+    const int i = lo + vb.x * LV_TX + (int)threadIdx.x;
+    const int jb = lo + (vb.y * LV_TY + (int)threadIdx.y) * SC_K;
+    if (i > hi || jb > hj) return;
+    const T *__restrict__ q = second ? L.t : L.x;
+    T bq[SC_K];
+    int uq[SC_K], mk[SC_K];
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) {
+        const int j = jb + k;
+        bq[k] = (T)0;
+        uq[k] = 0;
+        mk[k] = -1;
+        if (j <= hj) {
+            const size_t p = off(j, i, nv);
+            bq[k] = L.b[p];
+            uq[k] = A.uf[p];
+            mk[k] = L.msk[p];
+        }
+    }
+    T v[SC_K];
+    bool full = true;
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) full = full && (mk[k] <= 0 || uq[k]);
+    if (!second && A.zero_x) {
+#pragma unroll
+        for (int k = 0; k < SC_K; k++)
+            v[k] = mk[k] < 0 ? (T)0 : jacobi<T, false>(L, nullptr, nullptr, L.b, jb + k, i, (T)0, A.c2);
+    } else if (__all_sync(__activemask(), full)) {
+        T sr[SC_K + 2], mr[SC_K + 2];
+#pragma unroll
+        for (int r = 0; r < SC_K + 2; r++) {
+            const int j = jb - 1 + r;
+            sr[r] = mr[r] = (T)0;
+            if (j <= hj + 1) {
+                const T *row = q + off(j, i, nv);
+                sr[r] = row[-1] + row[1];
+                mr[r] = row[0];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < SC_K; k++) {
+            const T t1 = sr[k] + sr[k + 2], t2 = mr[k] + mr[k + 2];
+            const T u = fma(A.kc, t1, fma(A.key, t2, fma(A.kex, sr[k + 1],
+                                                        fma(A.c2, mr[k + 1], -A.c3u * bq[k]))));
+            v[k] = mk[k] > 0 ? u : (T)0;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < SC_K; k++)
+            v[k] = mk[k] < 0 ? (T)0 : jacobi<T, false>(L, nullptr, q, L.b, jb + k, i, (T)0, A.c2);
+    }
+#pragma unroll
+    for (int k = 0; k < SC_K; k++) {
+        if (mk[k] < 0) break;
+        const int j = jb + k;
+        if (second)
+            store_images(L.x, j, i, mv, nv, v[k]);
+        else
+            L.t[off(j, i, nv)] = v[k];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LV_TX *LV_TY) k_sweepu(SweepUArgs<T> a) {
+    pdl_prologue();
+    sweepu_body<T>(a, F2D_VB_NATIVE);
+}
+
+// whether a level of L's size takes the column form now: the mode on, no
+// step being recorded, and (mode 1) a grid of at least one CTA per SM
+template <typename T>
+bool column_applies(const LevelView<T> &L) {
+    const int mode = separable_mode();
+    if (!mode || recorder() != nullptr) return false;
+    const long long tiles = (long long)((L.nv - 4 + LV_TX - 1) / LV_TX) *
+                            ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K));
+    return mode == 2 || tiles >= sm_count();
+}
+template bool column_applies<double>(const LevelView<double> &);
+template bool column_applies<float>(const LevelView<float> &);
+
+template <typename T>
+int mg_sweeps_uniform(const LevelView<T> &L, const uint8_t *uf, const T *st, T c1, T c2,
+                      bool zero_x, const int *active, cudaStream_t s) {
+    (void)c1;
+    SweepUArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.L = L;
+    a.uf = uf;
+    a.c3u = st[3];
+    a.kc = st[3] * st[0];
+    a.key = st[3] * st[1];
+    a.kex = st[3] * st[2];
+    a.c2 = c2;
+    a.zero_x = zero_x ? 1 : 0;
+    a.active = active;
+    const dim3 b(LV_TX, LV_TY);
+    for (int second = 0; second < 2; second++) {
+        a.second = second;
+        const int lo = second ? NH : 2;
+        const int rows = (second ? L.mv - NH - 1 : L.mv - 3) - lo + 1;
+        const int cols = (second ? L.nv - NH - 1 : L.nv - 3) - lo + 1;
+        const dim3 g((unsigned)((cols + LV_TX - 1) / LV_TX),
+                     (unsigned)((rows + LV_TY * SC_K - 1) / (LV_TY * SC_K)));
+        const int st2 = cuda_status((cudaError_t)launch_pdl(k_sweepu<T>, a, g, b, 0, s),
+                                    "mg_sweeps_uniform");
+        if (st2) return st2;
+    }
+    return OK;
+}
+template int mg_sweeps_uniform<double>(const LevelView<double> &, const uint8_t *, const double *,
+                                       double, double, bool, const int *, cudaStream_t);
+
+// Set-up of a stored level's uniform stencil: the stencil (c, ey, ex, c3)
+// of the points at (1 + 2k) / 8 of the interior, k = 0..3, in both
+// directions, where the stencil has the uniform form (4 corners equal,
+// vertical and horizontal edges pairwise equal); out[5 * n + 4] = 1 there.
+__global__ void k_stencil_samples(const double *A6, const int8_t *msk, int mv, int nv,
+                                  double *out) {
+    const int n = (int)threadIdx.x;
+    if (n >= 16) return;
+    const int j = NH + (mv - 2 * NH) * (1 + 2 * (n / 4)) / 8;
+    const int i = NH + (nv - 2 * NH) * (1 + 2 * (n % 4)) / 8;
+    const size_t pl = (size_t)mv * nv, p = off(j, i, nv);
+    const double *A1 = A6, *A2 = A6 + pl, *A3 = A6 + 2 * pl, *A4 = A6 + 3 * pl;
+    const double a0 = A1[p], a1 = A2[p], a2 = A3[p], a3 = A4[p], a4 = A4[p + 1],
+                 a5 = A3[p + nv - 1], a6 = A2[p + nv], a7 = A1[p + nv + 1];
+    const bool ok = msk[p] != 0 && a0 == a2 && a0 == a5 && a0 == a7 && a1 == a6 && a3 == a4;
+    out[5 * n + 0] = a0;
+    out[5 * n + 1] = a1;
+    out[5 * n + 2] = a3;
+    out[5 * n + 3] = A6[5 * pl + p];
+    out[5 * n + 4] = ok ? 1. : 0.;
+}
+
+// uf = 1 where the point is fluid and its stored stencil is (c, ey, ex, c3)
+// exactly (rows and columns 1 .. m-2; 0 elsewhere)
+__global__ void k_uniform_flags(const double *A6, const int8_t *msk, int mv, int nv, double c,
+                                double ey, double ex, double c3, uint8_t *uf) {
+    const size_t pl = (size_t)mv * nv;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < pl;
+         p += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(p / nv), i = (int)(p % nv);
+        uint8_t f = 0;
+        if (j >= 1 && j <= mv - 2 && i >= 1 && i <= nv - 2 && msk[p] != 0) {
+            const double *A1 = A6, *A2 = A6 + pl, *A3 = A6 + 2 * pl, *A4 = A6 + 3 * pl;
+            f = A1[p] == c && A3[p] == c && A3[p + nv - 1] == c && A1[p + nv + 1] == c &&
+                A2[p] == ey && A2[p + nv] == ey && A4[p] == ex && A4[p + 1] == ex &&
+                A6[5 * pl + p] == c3;
+        }
+        uf[p] = f;
+    }
+}
+
+int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s) {
+    k_stencil_samples<<<1, 32, 0, s>>>(L.A, L.msk, L.mv, L.nv, out);
+    return launch_status("stencil samples");
+}
+
+// the level's uniform stencil st = (c, ey, ex, c3): the form most of the 16
+// samples (host copy h of mg_stencil_samples' output) share; false unless
+// at least half of them share it (coarsened operators whose coefficients
+// carry rounding noise from point to point have no uniform stencil, and the
+// column form would take the general expression nearly everywhere)
+bool mg_uniform_choose(const double *h, double *st) {
+    int best = -1, best_n = 0;
+    for (int a = 0; a < 16; a++) {
+        if (h[5 * a + 4] == 0.) continue;
+        int n = 0;
+        for (int b = 0; b < 16; b++)
+            n += h[5 * b + 4] != 0. && h[5 * b] == h[5 * a] && h[5 * b + 1] == h[5 * a + 1] &&
+                 h[5 * b + 2] == h[5 * a + 2] && h[5 * b + 3] == h[5 * a + 3];
+        if (n > best_n) {
+            best_n = n;
+            best = a;
+        }
+    }
+    if (best < 0 || best_n < 8) return false;
+    for (int k = 0; k < 4; k++) st[k] = h[5 * best + k];
+    return true;
+}
+
+int mg_uniform_flags(const LevelView<double> &L, const double *st, uint8_t *uf, cudaStream_t s) {
+    const size_t pl = (size_t)L.mv * L.nv;
+    const size_t blocks = (pl + 255) / 256;
+    k_uniform_flags<<<(unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s>>>(
+        L.A, L.msk, L.mv, L.nv, st[0], st[1], st[2], st[3], uf);
+    return launch_status("uniform flags");
+}
+
 template <typename T>
 F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;

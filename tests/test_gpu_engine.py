@@ -246,18 +246,19 @@ def test_coarse_operator_matches_the_cycle(eng, name, precision):
                                   "boussinesq-xchannel", "qg-closed", "euler-closed-islands",
                                   "euler-closed-5point"])
 def test_column_sweeps_match_the_sweep_kernels(eng, name, precision):
-    """The float64 finest level's sweeps and residual in column form (four
-    points a thread, neighbourhoods in registers, fluid 3x3 blocks through
-    the separable form of the 9-point operator) compute the reference's
-    function in another order of operations: the states after four steps
-    agree with the sweep and residual kernels (reference order) to the
-    product build's rounding, on periodic and closed domains, islands, the
-    Helmholtz operator of QG and 5-point operators (dx != dy, with and
-    without islands: the reference kernels run, bit for bit); in the mixed
-    form the float64 defect's
-    residual takes the column form.  Mode 2 forces the column form on these
-    grids of fewer CTAs than SMs (ragged last columns of threads and of
-    rows); a replayed graph gives the eager steps' bits."""
+    """The float64 sweeps and residual in column form (four points a thread,
+    neighbourhoods in registers; on the finest level fluid 3x3 blocks go
+    through the separable form of the 9-point operator, on the stored levels
+    points with the level's uniform stencil through its row-sum form)
+    compute the reference's function in another order of operations: the
+    states after four steps agree with the sweep, residual and fused level
+    kernels (reference order) to the product build's rounding, on periodic
+    and closed domains, islands, the Helmholtz operator of QG and 5-point
+    finest operators (dx != dy: there only the stored levels change); in the
+    mixed form the float64 defect's residual takes the column form.  Mode 2
+    forces the column form on these grids of fewer CTAs than SMs (ragged
+    last columns of threads and of rows); a replayed graph gives the eager
+    steps' bits."""
     import torch
     from fluid2d_gb300 import _lib
     from fluid2d_gb300 import workloads as W
@@ -299,11 +300,46 @@ def test_column_sweeps_match_the_sweep_kernels(eng, name, precision):
         scale = vel if k in (2, 3) else max(np.abs(b[k]).max(), 1e-300)
         assert np.abs(a[k] - b[k]).max() <= tol * scale, k
         assert np.array_equal(a[k], g[k]), k
-    # the column form ran where the operator is the 9-point one (the mixed
-    # form's float32 cycles may round both residuals to the same floats)
-    if precision == "fp64" or name in five_point:
+    # the column forms ran (the mixed form's float32 cycles may round both
+    # residuals to the same floats); with dx != dy the finest operator is
+    # the 5-point one and the coarsened ones carry rounding noise from point
+    # to point (no uniform stencil): the reference kernels run everywhere
+    if precision == "fp64":
         assert np.array_equal(a, b) == (name in five_point)
     assert _lib.lib("exact").f2d_set_separable(-1) == 0
+
+
+@pytest.mark.parametrize("geom,islands", [("perio", 0), ("closed", 3), ("xchannel", 2)])
+def test_stored_level_column_sweeps(eng, geom, islands):
+    """A V-cycle from level 1 (no finest-level kernel) with the stored
+    levels' column-form sweeps (points with the level's uniform stencil in
+    row-sum form, the others in the reference's expression) against the
+    fused level smoother: the same function to the product build's rounding,
+    not the same bits (the column form ran), on periodic, closed and channel
+    masks with islands."""
+    import torch
+    from fluid2d_gb300 import _lib
+    P = _lib.lib("product")
+    n = 256
+    msk = C.corner_mask(C.mask(n + 6, n + 6, geom, islands, 4))
+    dx = 1. / n
+
+    def vcycle(mode):
+        old = P.f2d_set_separable(mode)
+        try:
+            G = eng.Gmg(msk, n, n, dx, dx, variant="product")
+            mv, nv = G.shapes[1]
+            G.level_array(1, "x").copy_(torch.from_numpy(C.field(mv, nv, 5)).cuda())
+            G.level_array(1, "b").copy_(torch.from_numpy(C.field(mv, nv, 6, scale=1e5)).cuda())
+            G.Vcycle(1)
+            torch.cuda.synchronize()
+            return G.level_array(1, "x").cpu().numpy()
+        finally:
+            P.f2d_set_separable(old)
+
+    a, b = vcycle(2), vcycle(0)
+    assert relerr(a, b) <= 1e-12
+    assert not np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

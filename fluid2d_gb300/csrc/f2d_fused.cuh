@@ -122,8 +122,13 @@ int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, 
 template <typename T>
 int mg_sweeps_uniform(const LevelView<T> &L, const uint8_t *uf, const T *st, T c1, T c2,
                       bool zero_x, const int *active, cudaStream_t s);
+// a level of L's size takes the column form now: the mode on, no step
+// being recorded, (mode 1) a grid of at least one CTA per SM; the finest
+// level also needs the analytic 9-point operator and its coefficient bits
 template <typename T>
 bool column_applies(const LevelView<T> &L);
+template <typename T>
+bool column_l0_applies(const LevelView<T> &L, const AnalyticT<T> &an);
 // set-up of a stored level's uniform stencil: 16 samples (5 doubles each)
 // of its stencil into out, the choice on the host, the flags on the device
 int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s);

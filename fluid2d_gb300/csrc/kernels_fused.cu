@@ -1087,19 +1087,39 @@ int &separable_mode() {
     return m;
 }
 
+// whether a level of L's size takes the column form now: the mode on, no
+// step being recorded, and (mode 1) a grid of at least one CTA per SM
+template <typename T>
+bool column_applies(const LevelView<T> &L) {
+    const int mode = separable_mode();
+    if (!mode || recorder() != nullptr) return false;
+    const long long tiles = (long long)((L.nv - 4 + LV_TX - 1) / LV_TX) *
+                            ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K));
+    return mode == 2 || tiles >= sm_count();
+}
+template bool column_applies<double>(const LevelView<double> &);
+template bool column_applies<float>(const LevelView<float> &);
+
+// the same for the finest level, whose operator must also be the analytic
+// 9-point one with corners = edges / 2 and have its coefficient bits
+template <typename T>
+bool column_l0_applies(const LevelView<T> &L, const AnalyticT<T> &an) {
+    if (!L.nb || !column_applies(L)) return false;
+    const T e = an.sc[1];
+    return e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e && an.sc[2] == an.sc[0];
+}
+template bool column_l0_applies<double>(const LevelView<double> &, const AnalyticT<double> &);
+
 // The finest level's two sweeps in column form; *done = false and nothing
-// launched when the mode is off, the operator is not the 9-point form with
-// corners = edges / 2, the level has no coefficient bits, or a step is being
-// recorded (a batch takes the sweep kernels: this kernel is not a batched
+// launched where column_l0_applies does not hold (a step being recorded
+// included: a batch takes the sweep kernels, this kernel is not a batched
 // body).
 template <typename T>
 int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, bool zero_x,
                      const int *active, cudaStream_t s, bool *done) {
     *done = false;
-    if (!separable_mode() || recorder() != nullptr || !L.nb) return OK;
+    if (!column_l0_applies(L, an)) return OK;
     const T e = an.sc[1];
-    if (!(e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e && an.sc[2] == an.sc[0]))
-        return OK;
     SweepCArgs<T> a;
     memset(&a, 0, sizeof(a));
     a.L = L;
@@ -1112,12 +1132,6 @@ int mg_sweeps_column(const LevelView<T> &L, const AnalyticT<T> &an, T c1, T c2, 
     a.zero_x = zero_x ? 1 : 0;
     a.active = active;
     const dim3 b(LV_TX, LV_TY);
-    // a grid of fewer CTAs than SMs is latency bound: four points a thread
-    // lose there to the sweep kernels' one
-    if (separable_mode() == 1 &&
-        (long long)((L.nv - 4 + LV_TX - 1) / LV_TX) * ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K)) <
-            sm_count())
-        return OK;
     for (int second = 0; second < 2; second++) {
         a.second = second;
         const int lo = second ? NH : 2;
@@ -1232,18 +1246,6 @@ __global__ void __launch_bounds__(LV_TX *LV_TY) k_sweepu(SweepUArgs<T> a) {
     sweepu_body<T>(a, F2D_VB_NATIVE);
 }
 
-// whether a level of L's size takes the column form now: the mode on, no
-// step being recorded, and (mode 1) a grid of at least one CTA per SM
-template <typename T>
-bool column_applies(const LevelView<T> &L) {
-    const int mode = separable_mode();
-    if (!mode || recorder() != nullptr) return false;
-    const long long tiles = (long long)((L.nv - 4 + LV_TX - 1) / LV_TX) *
-                            ((L.mv - 4 + LV_TY * SC_K - 1) / (LV_TY * SC_K));
-    return mode == 2 || tiles >= sm_count();
-}
-template bool column_applies<double>(const LevelView<double> &);
-template bool column_applies<float>(const LevelView<float> &);
 
 template <typename T>
 int mg_sweeps_uniform(const LevelView<T> &L, const uint8_t *uf, const T *st, T c1, T c2,
@@ -1276,6 +1278,8 @@ int mg_sweeps_uniform(const LevelView<T> &L, const uint8_t *uf, const T *st, T c
 }
 template int mg_sweeps_uniform<double>(const LevelView<double> &, const uint8_t *, const double *,
                                        double, double, bool, const int *, cudaStream_t);
+template int mg_sweeps_uniform<float>(const LevelView<float> &, const uint8_t *, const float *,
+                                      float, float, bool, const int *, cudaStream_t);
 
 // Set-up of a stored level's uniform stencil: the stencil (c, ey, ex, c3)
 // of the points at (1 + 2k) / 8 of the interior, k = 0..3, in both

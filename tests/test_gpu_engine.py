@@ -255,7 +255,8 @@ def test_column_sweeps_match_the_sweep_kernels(eng, name, precision):
     kernels (reference order) to the product build's rounding, on periodic
     and closed domains, islands, the Helmholtz operator of QG and 5-point
     finest operators (dx != dy: there only the stored levels change); in the
-    mixed form the float64 defect's residual takes the column form.  Mode 2
+    mixed form the float64 defect's residual and the float stored levels
+    take the column form.  Mode 2
     forces the column form on these grids of fewer CTAs than SMs (ragged
     last columns of threads and of rows); a replayed graph gives the eager
     steps' bits."""

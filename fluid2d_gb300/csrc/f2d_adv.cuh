@@ -61,12 +61,24 @@ F2D_DEV T upwind_flux(const T *q, const int *mk, T vel, int method, int order,
             d4 = (T)r4(9.f / 20.f), d5 = (T)r4(-1.f / 20.f);
     const T c1 = (T)r4(-1.f / 6.f), c2 = (T)r4(5.f / 6.f), c3 = (T)r4(2.f / 6.f);
     T UU = split_speed(vel, method, c);
-    T up = (T)0.5 * (vel + UU);
-    T um = (T)0.5 * (vel - UU);
     int m5p = mk[0] + mk[1] + mk[2] + mk[3] + mk[4];
     int m3p = mk[1] + mk[2] + mk[3];
     int m5m = mk[1] + mk[2] + mk[3] + mk[4] + mk[5];
     int m3m = mk[2] + mk[3] + mk[4];
+#ifndef F2D_EXACT
+    if (order == 5 && m5p == 5 && m5m == 5) {
+        // product build, both 5th-order reconstructions: the same flux from
+        // their symmetric and antisymmetric sums, up qp + um qm =
+        // (vel (qp + qm) + UU (qp - qm)) / 2 -- 16 operations instead of 20
+        const T s1 = (T)0.5 * d1, s2 = (T)0.5 * (d2 + d5), s3 = (T)0.5 * (d3 + d4);
+        const T a2 = (T)0.5 * (d2 - d5), a3 = (T)0.5 * (d3 - d4);
+        const T S = fma(s1, q[0] + q[5], fma(s2, q[1] + q[4], s3 * (q[2] + q[3])));
+        const T D = fma(s1, q[0] - q[5], fma(a2, q[1] - q[4], a3 * (q[2] - q[3])));
+        return fma(UU, D, vel * S);
+    }
+#endif
+    T up = (T)0.5 * (vel + UU);
+    T um = (T)0.5 * (vel - UU);
     T qp, qm;
     if (m5p == 5 && order == 5)
         qp = d1 * q[0] + d2 * q[1] + d3 * q[2] + d4 * q[3] + d5 * q[4];

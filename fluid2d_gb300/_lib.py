@@ -217,6 +217,7 @@ SIGNATURES.update({
     "f2d_model_graph_kernels": [_P, _PI],
     "f2d_model_coarse_level": [_P, _I, _PI, _PI, _PI],
     "f2d_model_coarse_op": [_P, _I, _PI],
+    "f2d_model_cluster_level": [_P, _PI],
     "f2d_model_reset_graphs": [_P],
     "f2d_batch_create": [ctypes.POINTER(ctypes.c_void_p), _I, _I, _PP],
     "f2d_batch_step": [_P, _I, _P],
@@ -245,6 +246,7 @@ EXTRA = {
     "f2d_set_level_tiles": ([_I], _I),
     "f2d_set_level_threads": ([_I], _I),
     "f2d_set_separable": ([_I], _I),
+    "f2d_set_cluster": ([_I], _I),
     "f2d_fp64_peak": ([ctypes.POINTER(ctypes.c_double)], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),

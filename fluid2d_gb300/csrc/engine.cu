@@ -10,6 +10,7 @@
 //
 // Set-up reuses the drop-in kernels (restrict, fillhalo, coarsenmatrix) to
 // build every level's mask and Galerkin operator on the device.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -277,6 +278,26 @@ struct Gmg {
     template <typename T>
     const T *op(int k) const;
     int build_coarse_op(cudaStream_t s);
+    // the mixed form's cluster sub-cycle (product build): from float level
+    // cl_lev (-1: none) down to the operator's level op_cs
+    int cl_lev = -1;
+    size_t cl_smem = 0;
+    ClArgs cl_tmpl = {};
+    void cluster_setup();
+    bool cluster_from(int l1, int stop) const {
+        return cl_lev >= 0 && cl_lev >= l1 && cl_lev < stop && op_cs == cs && cluster_mode() &&
+               recorder() == nullptr;
+    }
+    int cluster_cycle(LevelView<float> *L, int mode, const int *active, cudaStream_t s) {
+        ClArgs a = cl_tmpl;
+        a.x_top = L[cl_lev].x;
+        a.b_top = L[cl_lev].b;
+        a.op = opf[mode == CYCLE_F ? 1 : 0];
+        a.op_v = opf[0];
+        a.mode = mode;
+        a.active = active;
+        return mg_cluster_cycle(a, cl_smem, s);
+    }
     void free_coarse_op() {
         for (int k = 0; k < 2; k++) {
             if (opd[k]) cudaFree(opd[k]);
@@ -286,6 +307,7 @@ struct Gmg {
         }
         op_cs = -1;
         op_n = 0;
+        cl_lev = -1;
     }
     ~Gmg() {
         for (int k = 0; k < MAX_PROBES; k++)
@@ -390,7 +412,60 @@ int Gmg::build_coarse_op(cudaStream_t s) {
     }
     op_cs = cs;
     op_n = n;
+    cluster_setup();
     return OK;
+#endif
+}
+
+// The cluster sub-cycle's layout: the finest float level Ls >= 1, at most
+// cluster_mode() levels above the operator's level, whose strips (the
+// operator level's interior rows split over CL_NC CTAs, doubled on each
+// finer level, CL_G ghost rows a side; x twice, b, t) and the gathered
+// coarse b fit in CL_SMEM_MAX bytes a CTA.  None with the switch off,
+// without float levels and operator, below CL_NC operator-level rows, or if
+// the device cannot hold such a cluster.
+void Gmg::cluster_setup() {
+    cl_lev = -1;
+#ifndef F2D_EXACT
+    if (!has_f32 || tri || op_cs < 0 || !opf[0] || !opf[1]) return;
+    const int K = op_cs, mc = mv[K] - 2 * NH;
+    if (mc < CL_NC) return;
+    const int above = cluster_mode();  // levels above the operator's level
+    for (int ls = std::max(1, K - above); ls < K; ls++) {
+        const int nl = K - ls + 1;
+        if (nl > CL_MAXLEV) continue;
+        ClArgs a = {};
+        a.nlev = nl;
+        int strip = 0;
+        for (int c = 0; c <= CL_NC; c++) a.p[c] = c * mc / CL_NC;
+        for (int c = 0; c < CL_NC; c++) strip = std::max(strip, a.p[c + 1] - a.p[c]);
+        size_t o = 0;
+        for (int k = 0; k < nl; k++) {
+            const int l = ls + k;
+            ClLevel &v = a.lv[k];
+            v.mv = mv[l];
+            v.nv = nv[l];
+            v.rows = (strip << (nl - 1 - k)) + 2 * CL_G;
+            v.msk = f[l].msk;
+            v.A = f[l].A;
+            const size_t bytes = ((size_t)v.rows * v.nv * sizeof(float) + 15) & ~(size_t)15;
+            v.o_x[0] = (unsigned)o;
+            v.o_x[1] = (unsigned)(o + bytes);
+            v.o_b = (unsigned)(o + 2 * bytes);
+            v.o_t = (unsigned)(o + 3 * bytes);
+            o += 4 * bytes;
+        }
+        a.o_g = (unsigned)o;
+        a.n = op_n;
+        o += ((size_t)op_n * sizeof(float) + 15) & ~(size_t)15;
+        a.c2 = (float)(1. - omega);
+        if (o > CL_SMEM_MAX) continue;
+        if (!mg_cluster_feasible(o)) return;
+        cl_tmpl = a;
+        cl_smem = o;
+        cl_lev = ls;
+        return;
+    }
 #endif
 }
 
@@ -700,7 +775,12 @@ int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cud
     const int deep = nlev - 1;
     if (l1 >= cs) return coarse(L, l1, CYCLE_V, zero_first, active, s);
     const int stop = cs < deep ? cs : deep;
-    for (int l = l1; l < stop; l++) {
+    // levels [lc, stop) and the coarse part as one cluster launch (float
+    // levels, where the first smooth there starts from zero)
+    int lc = stop;
+    if constexpr (sizeof(T) == 4)
+        if (cluster_from(l1, stop) && (zero_first || cl_lev > l1)) lc = cl_lev;
+    for (int l = l1; l < lc; l++) {
         const int xm = (zero_first || l > l1) ? X_ZERO : (l == l1 ? first_mode : X_IN);
         TRY(smooth(L, l, xm, active, s));
         const AnalyticT<T> *a0 = l == 0 ? analytic<T>() : nullptr;
@@ -711,12 +791,14 @@ int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cud
             TRY(mg_restrict<T>(L[l], L[l].r, L[l + 1], L[l + 1].b, active, s));
         }
     }
-    if (cs <= deep) {
+    if (lc < stop) {
+        if constexpr (sizeof(T) == 4) TRY(cluster_cycle(L, CYCLE_V, active, s));
+    } else if (cs <= deep) {
         TRY(coarse(L, cs, CYCLE_V, true, active, s));
     } else {
         for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0 ? X_ZERO : X_IN, active, s));
     }
-    for (int l = stop - 1; l >= l1; l--) TRY(smooth(L, l, X_PLUS_INTERP, active, s));
+    for (int l = lc - 1; l >= l1; l--) TRY(smooth(L, l, X_PLUS_INTERP, active, s));
     return OK;
 }
 
@@ -726,13 +808,18 @@ int Gmg::fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s) {
     const int deep = nlev - 1;
     if (l1 >= cs) return coarse(L, l1, CYCLE_F, false, active, s);
     const int stop = cs < deep ? cs : deep;
-    for (int l = l1; l < stop; l++) TRY(mg_restrict<T>(L[l], L[l].b, L[l + 1], L[l + 1].b, active, s));
-    if (cs <= deep) {
+    int lc = stop;  // levels [lc, stop) and the coarse part as one cluster launch
+    if constexpr (sizeof(T) == 4)
+        if (cluster_from(l1, stop)) lc = cl_lev;
+    for (int l = l1; l < lc; l++) TRY(mg_restrict<T>(L[l], L[l].b, L[l + 1], L[l + 1].b, active, s));
+    if (lc < stop) {
+        if constexpr (sizeof(T) == 4) TRY(cluster_cycle(L, CYCLE_F, active, s));
+    } else if (cs <= deep) {
         TRY(coarse(L, cs, CYCLE_F, false, active, s));
     } else {
         for (int k = 0; k < ndeepest; k++) TRY(smooth(L, deep, k == 0 ? X_ZERO : X_IN, active, s));
     }
-    for (int l = stop - 1; l >= l1; l--) TRY(vcycle(L, l, false, active, s, X_INTERP));
+    for (int l = lc - 1; l >= l1; l--) TRY(vcycle(L, l, false, active, s, X_INTERP));
     return OK;
 }
 
@@ -2106,6 +2193,16 @@ int f2d_model_coarse_op(void *model, int enable, int *n) {
         TRY(rebuild_coarse_op(g));
     }
     if (n) *n = g.op_n;
+    return OK;
+}
+
+// the float level from which the mixed form's small-level cycles run as one
+// cluster launch (-1: none, or the switch off)
+int f2d_model_cluster_level(void *model, int *level) {
+    Model *M = (Model *)model;
+    if (!M || !level) return ERR_ARG;
+    const Gmg &g = M->gmg;
+    *level = (g.cl_lev >= 0 && g.op_cs == g.cs && cluster_mode()) ? g.cl_lev : -1;
     return OK;
 }
 

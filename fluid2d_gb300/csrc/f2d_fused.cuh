@@ -134,6 +134,39 @@ bool column_l0_applies(const LevelView<T> &L, const AnalyticT<T> &an);
 int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s);
 bool mg_uniform_choose(const double *h, double *st);
 int mg_uniform_flags(const LevelView<double> &L, const double *st, uint8_t *uf, cudaStream_t s);
+// The mixed form's cluster sub-cycle (a V-cycle from zero or the F-cycle
+// from level Ls down to the coarse operator's level, float, one launch of a
+// CL_NC-CTA cluster with the levels in distributed shared memory).
+constexpr int CL_NC = 16, CL_THREADS = 1024, CL_G = 2, CL_MAXLEV = 8;
+constexpr size_t CL_SMEM_MAX = 200 * 1024;
+
+struct ClLevel {
+    int mv, nv;
+    int rows;                          // local rows: the largest strip + 2 CL_G
+    unsigned o_x[2], o_b, o_t;         // shared-memory byte offsets
+    const int8_t *msk;
+    const float *A;
+};
+
+struct ClArgs {
+    int nlev;                          // lv[0] = level Ls .. lv[nlev-1] = the operator's level
+    ClLevel lv[CL_MAXLEV];
+    int p[CL_NC + 1];                  // strips of the operator level's interior rows
+    float *x_top;                      // level Ls's x (global): the result
+    const float *b_top;                // level Ls's b (global)
+    const float *op;                   // the coarse operator of the cycle (V or F)
+    const float *op_v;                 // the V-cycle operator (the F-cycle's inner V-cycles)
+    int n;                             // operator size
+    float c2;                          // 1 - omega
+    int mode;                          // CYCLE_V (first smooth from zero) or CYCLE_F
+    unsigned o_g;                      // gathered coarse b (n floats)
+    const int *active;
+};
+
+bool mg_cluster_feasible(size_t smem);
+int mg_cluster_cycle(const ClArgs &a, size_t smem, cudaStream_t s);
+int &cluster_mode();
+
 // residual of L (x, b) restricted into the coarse b2
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,

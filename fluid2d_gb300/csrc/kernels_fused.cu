@@ -15,6 +15,8 @@
 //   restrict = coarse interior + periodic halo;
 //   interpolate + (x += r) = fine rows/cols 1..m-2 (what the next smooth
 //              reads), so the correction array r is never stored.
+#include <cooperative_groups.h>
+
 #include "f2d_common.cuh"
 #include "f2d_fused.cuh"
 #include "f2d_kernels.cuh"
@@ -2374,9 +2376,394 @@ int mg_zero(double *x, size_t n, const int *active, cudaStream_t s) {
     return launch_status("mg_zero");
 }
 
+
+// ------------------------------------------------------------ cluster sub-cycle
+// The float levels of the mixed form from a level Ls down to the coarse
+// operator's level, held in the distributed shared memory of one cluster
+// of CL_NC CTAs: a V-cycle (or the F-cycle) from Ls in one launch instead of
+// two to three launches a level visit (the small levels' launches are the
+// mixed step's latency-bound part).  Each CTA owns a strip of the interior
+// rows of every level (the coarse level's rows split evenly, doubled on
+// each finer level, so a coarse strip covers exactly its fine strip) plus
+// CL_G ghost rows a side; ghost rows are copied from their owners through
+// distributed shared memory after a cluster barrier, halo rows as the
+// periodic images of interior rows (the reference's halo fill).  Every
+// phase evaluates the reference's expressions with the level kernels'
+// device functions (jacobi, residual, restrict_value, interp_value, the
+// coarse operator's dot product in its order), so the result is the launch
+// sequence's bit for bit.  All CTAs run the same sequence of phases and
+// barriers; no CTA leaves early.
+namespace cgx = cooperative_groups;
+
+struct ClCtx {
+    const ClArgs *a;
+    unsigned char *sm;
+    int rank;
+    int cur[CL_MAXLEV];                // x buffer in use, per level
+};
+
+F2D_DEV int cl_r0(const ClArgs &a, int k, int c) { return NH + (a.p[c] << (a.nlev - 1 - k)); }
+
+F2D_DEV int cl_owner(const ClArgs &a, int k, int j) {
+    int q = 0;
+    while (q + 1 < CL_NC && cl_r0(a, k, q + 1) <= j) q++;
+    return q;
+}
+
+// array at byte offset o of level k in this CTA, indexed by global (j, i)
+F2D_DEV float *cl_view(const ClCtx &c, int k, unsigned o) {
+    const ClLevel &L = c.a->lv[k];
+    return (float *)(c.sm + o) - (ptrdiff_t)(cl_r0(*c.a, k, c.rank) - CL_G) * L.nv;
+}
+
+F2D_DEV LevelView<float> cl_level(const ClCtx &c, int k, const float *x, const float *b) {
+    const ClLevel &L = c.a->lv[k];
+    LevelView<float> v;
+    v.mv = L.mv;
+    v.nv = L.nv;
+    v.msk = L.msk;
+    v.A = L.A;
+    v.x = (float *)x;
+    v.b = (float *)b;
+    v.r = nullptr;
+    v.t = nullptr;
+    v.nb = nullptr;
+    return v;
+}
+
+// ghost rows [r0-lo, r0) and [r1, r1+hi) of array o of level k from their
+// owners (rows outside [0, mv) are skipped; halo rows take their images)
+F2D_DEV void cl_fill(const ClCtx &c, cgx::cluster_group &cl, int k, unsigned o, int lo, int hi) {
+    const ClArgs &a = *c.a;
+    const ClLevel &L = a.lv[k];
+    const int nv = L.nv, r0 = cl_r0(a, k, c.rank), r1 = cl_r0(a, k, c.rank + 1);
+    float *loc = cl_view(c, k, o);
+    const int n = (lo + hi) * nv;
+    for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+        const int rr = q / nv, i = q - rr * nv;
+        const int j = rr < lo ? r0 - lo + rr : r1 + rr - lo;
+        if (j < 0 || j >= L.mv) continue;
+        const int src = wrap(j, L.mv, NH);
+        const int w = cl_owner(a, k, src);
+        const float *rem = cl.map_shared_rank((float *)(c.sm + o), w);
+        loc[off(j, i, nv)] = rem[off(src - (cl_r0(a, k, w) - CL_G), i, nv)];
+    }
+}
+
+// value v at (j, i) of a strip array and its images in the same row
+F2D_DEV void cl_put(float *x, int j, int i, int nv, float v) {
+    const int n2 = nv - 2 * NH;
+    x[off(j, i, nv)] = v;
+    if (i >= n2 && i < n2 + NH) x[off(j, i - n2, nv)] = v;
+    if (i >= NH && i < 2 * NH) x[off(j, i + n2, nv)] = v;
+}
+
+// one smoothtwicewitha call on level k: x (the level's current buffer,
+// rows r0-2 .. r1+1 valid) or zero -> t -> the other buffer (strip rows and
+// their row images); b rows r0-1 .. r1 valid
+F2D_DEV void cl_smooth(ClCtx &c, int k, bool zero_x) {
+    const ClArgs &a = *c.a;
+    const ClLevel &L = a.lv[k];
+    const int mv = L.mv, nv = L.nv, r0 = cl_r0(a, k, c.rank), r1 = cl_r0(a, k, c.rank + 1);
+    const float *x = cl_view(c, k, L.o_x[c.cur[k]]);
+    float *t = cl_view(c, k, L.o_t), *y = cl_view(c, k, L.o_x[c.cur[k] ^ 1]);
+    const float *b = cl_view(c, k, L.o_b);
+    const LevelView<float> V = cl_level(c, k, x, b);
+    if (r1 > r0) {
+        const int ja = max(2, r0 - 1), jb = min(mv - 3, r1), w = nv - 4;
+        const int n = (jb - ja + 1) * w;
+        for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+            const int rr = q / w, j = ja + rr, i = 2 + q - rr * w;
+            t[off(j, i, nv)] = jacobi<float, false>(V, nullptr, zero_x ? nullptr : x, b, j, i, 0.f,
+                                                    a.c2);
+        }
+    }
+    __syncthreads();
+    {
+        const LevelView<float> W = cl_level(c, k, t, b);
+        const int w = nv - 2 * NH, n = (r1 - r0) * w;
+        for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+            const int rr = q / w, j = r0 + rr, i = NH + q - rr * w;
+            cl_put(y, j, i, nv, jacobi<float, false>(W, nullptr, t, b, j, i, 0.f, a.c2));
+        }
+    }
+    c.cur[k] ^= 1;
+}
+
+// x of level k (rows r0-2 .. r1+1, columns 1 .. nv-2) = prolongation of
+// level k+1's x (plus x itself unless assign); level k+1's x rows valid
+// from its r0-2 to its r1+1
+F2D_DEV void cl_interp(ClCtx &c, int k, bool assign) {
+    const ClArgs &a = *c.a;
+    const ClLevel &F = a.lv[k], &C = a.lv[k + 1];
+    const int mv = F.mv, nv = F.nv, r0 = cl_r0(a, k, c.rank), r1 = cl_r0(a, k, c.rank + 1);
+    float *x = cl_view(c, k, F.o_x[c.cur[k]]);
+    const float *xc = cl_view(c, k + 1, C.o_x[c.cur[k + 1]]);
+    const int ja = max(1, r0 - CL_G), jb = min(mv - 2, r1 + CL_G - 1), w = nv - 2;
+    const int n = r1 > r0 ? (jb - ja + 1) * w : 0;
+    for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+        const int rr = q / w, j = ja + rr, i = 1 + q - rr * w;
+        const float v = interp_value(F.msk, nv, C.msk, xc, C.nv, j, i);
+        x[off(j, i, nv)] = assign ? v : x[off(j, i, nv)] + v;
+    }
+}
+
+// residual of level k (strip rows and the row above: the restriction's
+// reach) into t, then full weighting into level k+1's b (its strip rows)
+F2D_DEV void cl_resres(ClCtx &c, int k) {
+    const ClArgs &a = *c.a;
+    const ClLevel &F = a.lv[k], &C = a.lv[k + 1];
+    const int mv = F.mv, nv = F.nv, r0 = cl_r0(a, k, c.rank), r1 = cl_r0(a, k, c.rank + 1);
+    const int m2 = mv - 2 * NH, n2 = nv - 2 * NH;
+    const float *x = cl_view(c, k, F.o_x[c.cur[k]]);
+    const float *b = cl_view(c, k, F.o_b);
+    float *r = cl_view(c, k, F.o_t);
+    if (r1 > r0) {
+        // rows r0 .. r1 at interior columns; the row above the top strip is
+        // the halo row whose image is row NH: its operator and mask are row
+        // NH's (the view shifted by m2 rows), its x and b the images here
+        const int w = n2, n = (r1 - r0 + 1) * w;
+        for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+            const int rr = q / w, j = r0 + rr, i = NH + q - rr * w;
+            LevelView<float> V = cl_level(c, k, x, b);
+            if (j >= mv - NH) {
+                V.msk -= (ptrdiff_t)m2 * nv;
+                V.A -= (ptrdiff_t)m2 * nv;
+            }
+            cl_put(r, j, i, nv, residual<float, false>(V, nullptr, x, b, j, i));
+        }
+    }
+    __syncthreads();
+    const int R0 = cl_r0(a, k + 1, c.rank), R1 = cl_r0(a, k + 1, c.rank + 1);
+    float *b2 = cl_view(c, k + 1, C.o_b);
+    const int w2 = C.nv - 2 * NH, n = (R1 - R0) * w2;
+    for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+        const int rr = q / w2, J = R0 + rr, I = NH + q - rr * w2;
+        cl_put(b2, J, I, C.nv, restrict_value(C.msk, C.nv, r, nv, J, I));
+    }
+}
+
+// level k+1's b (strip rows) = full weighting of level k's b (the
+// F-cycle's coarsening of the right-hand side); level k's b rows valid to r1
+F2D_DEV void cl_restrict_b(ClCtx &c, int k) {
+    const ClArgs &a = *c.a;
+    const ClLevel &F = a.lv[k], &C = a.lv[k + 1];
+    const float *b = cl_view(c, k, F.o_b);
+    const int R0 = cl_r0(a, k + 1, c.rank), R1 = cl_r0(a, k + 1, c.rank + 1);
+    float *b2 = cl_view(c, k + 1, C.o_b);
+    const int w2 = C.nv - 2 * NH, n = (R1 - R0) * w2;
+    for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+        const int rr = q / w2, J = R0 + rr, I = NH + q - rr * w2;
+        cl_put(b2, J, I, C.nv, restrict_value(C.msk, C.nv, b, F.nv, J, I));
+    }
+}
+
+// the coarse level's x = op . (its interior b), one warp per point, summed
+// in k_coarse_apply's order
+F2D_DEV void cl_coarse(ClCtx &c, cgx::cluster_group &cl, const float *op) {
+    const ClArgs &a = *c.a;
+    const int k = a.nlev - 1;
+    const ClLevel &L = a.lv[k];
+    const int nv = L.nv, n2 = nv - 2 * NH, n = a.n;
+    float *g = (float *)(c.sm + a.o_g);
+    for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+        const int qj = q / n2, j = NH + qj, i = NH + q - qj * n2;
+        const int w = cl_owner(a, k, j);
+        const float *rem = cl.map_shared_rank((float *)(c.sm + L.o_b), w);
+        g[q] = rem[off(j - (cl_r0(a, k, w) - CL_G), i, nv)];
+    }
+    __syncthreads();
+    float *x = cl_view(c, k, L.o_x[c.cur[k]]);
+    const int r0 = cl_r0(a, k, c.rank), r1 = cl_r0(a, k, c.rank + 1);
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const int np = (r1 - r0) * n2;
+    for (int pt = warp; pt < np; pt += CL_THREADS / 32) {
+        const int rr = pt / n2, j = r0 + rr, i = NH + pt - rr * n2;
+        const int row = (j - NH) * n2 + (i - NH);
+        const float *orow = op + (size_t)row * n;
+        float s0 = 0.f, s1 = 0.f;
+        int q = lane;
+        for (; q + 32 < n; q += 64) {
+            s0 = fma(orow[q], g[q], s0);
+            s1 = fma(orow[q + 32], g[q + 32], s1);
+        }
+        if (q < n) s0 = fma(orow[q], g[q], s0);
+        float v = s0 + s1;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) cl_put(x, j, i, nv, v);
+    }
+}
+
+// a V-cycle from level k0 (its b rows r0-1 .. r1 valid): the first smooth
+// from zero, or (f_interp) from the prolongation of level k0+1's x
+F2D_DEV void cl_vcycle(ClCtx &c, cgx::cluster_group &cl, int k0, bool f_interp) {
+    const ClArgs &a = *c.a;
+    const int K = a.nlev - 1;
+    for (int k = k0; k < K; k++) {
+        if (k == k0 && f_interp) {
+            cl_interp(c, k, true);
+            __syncthreads();
+            cl_smooth(c, k, false);
+        } else {
+            cl_smooth(c, k, true);
+        }
+        cl.sync();
+        cl_fill(c, cl, k, a.lv[k].o_x[c.cur[k]], CL_G, CL_G);
+        __syncthreads();
+        cl_resres(c, k);
+        cl.sync();
+        cl_fill(c, cl, k + 1, a.lv[k + 1].o_b, 1, 1);
+        __syncthreads();
+    }
+    cl_coarse(c, cl, a.op_v);
+    for (int k = K - 1; k >= k0; k--) {
+        cl.sync();
+        cl_fill(c, cl, k + 1, a.lv[k + 1].o_x[c.cur[k + 1]], CL_G, CL_G);
+        __syncthreads();
+        cl_interp(c, k, false);
+        __syncthreads();
+        cl_smooth(c, k, false);
+    }
+}
+
+F2D_DEV void cl_body(const ClArgs &a) {
+    cgx::cluster_group cl = cgx::this_cluster();
+    extern __shared__ __align__(16) unsigned char cl_sm[];
+    ClCtx c;
+    c.a = &a;
+    c.sm = cl_sm;
+    c.rank = (int)cl.block_rank();
+    for (int k = 0; k < CL_MAXLEV; k++) c.cur[k] = 0;
+    const bool skip = inactive(a.active);  // the same in every CTA: no barrier is skipped alone
+    if (skip) return;
+    const ClLevel &L0 = a.lv[0];
+    {   // level Ls's b, strip rows and CL_G ghost rows a side, from global memory
+        const int r0 = cl_r0(a, 0, c.rank), r1 = cl_r0(a, 0, c.rank + 1);
+        const int ja = max(0, r0 - CL_G), jb = min(L0.mv - 1, r1 + CL_G - 1), nv = L0.nv;
+        float *b = cl_view(c, 0, L0.o_b);
+        const int n = (jb - ja + 1) * nv;
+        for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) b[(size_t)ja * nv + q] = a.b_top[(size_t)ja * nv + q];
+    }
+    __syncthreads();
+    const int K = a.nlev - 1;
+    if (a.mode == CYCLE_V) {
+        cl_vcycle(c, cl, 0, false);
+    } else {
+        for (int k = 0; k < K; k++) {
+            cl_restrict_b(c, k);
+            cl.sync();
+            cl_fill(c, cl, k + 1, a.lv[k + 1].o_b, 1, 1);
+            __syncthreads();
+        }
+        cl_coarse(c, cl, a.op);
+        for (int k = K - 1; k >= 0; k--) {
+            cl.sync();
+            cl_fill(c, cl, k + 1, a.lv[k + 1].o_x[c.cur[k + 1]], CL_G, CL_G);
+            __syncthreads();
+            cl_vcycle(c, cl, k, true);
+        }
+    }
+    // level Ls's x: strip rows with their images, to global memory
+    const int r0 = cl_r0(a, 0, c.rank), r1 = cl_r0(a, 0, c.rank + 1), nv = L0.nv;
+    const float *x = cl_view(c, 0, L0.o_x[c.cur[0]]);
+    const int w = nv - 2 * NH, n = (r1 - r0) * w;
+    for (int q = (int)threadIdx.x; q < n; q += CL_THREADS) {
+        const int rr = q / w, j = r0 + rr, i = NH + q - rr * w;
+        store_images(a.x_top, j, i, L0.mv, nv, x[off(j, i, nv)]);
+    }
+    // no CTA leaves while another may still read its shared memory
+    cl.sync();
+}
+
+__global__ void __launch_bounds__(CL_THREADS, 1) k_cluster_cycle(const __grid_constant__ ClArgs a) {
+    pdl_prologue();
+    cl_body(a);
+}
+
+// cluster launch attributes of k_cluster_cycle (CL_NC CTAs: a non-portable
+// cluster size) and `smem` bytes of dynamic shared memory
+static int cl_config(size_t smem, cudaStream_t s, cudaLaunchConfig_t *cfg,
+                     cudaLaunchAttribute *attr) {
+    // the function attributes once (set-up time, outside any stream capture),
+    // for every layout up to CL_SMEM_MAX bytes
+    static int attrs = -1;
+    if (attrs < 0) {
+        int st = cuda_status(cudaFuncSetAttribute(k_cluster_cycle,
+                                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                             "cluster size attribute");
+        if (!st)
+            st = cuda_status(cudaFuncSetAttribute(k_cluster_cycle,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)CL_SMEM_MAX),
+                             "cluster shared memory attribute");
+        attrs = st;
+    }
+    if (attrs) return attrs;
+    if (smem > CL_SMEM_MAX) return ERR_ARG;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->gridDim = dim3(CL_NC);
+    cfg->blockDim = dim3(CL_THREADS);
+    cfg->dynamicSmemBytes = smem;
+    cfg->stream = s;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL_NC;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg->attrs = attr;
+    cfg->numAttrs = pdl_enabled() ? 2 : 1;
+    return OK;
+}
+
+// whether a cluster of k_cluster_cycle with `smem` bytes can be resident
+bool mg_cluster_feasible(size_t smem) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[2];
+    if (cl_config(smem, nullptr, &cfg, attr) != OK) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cluster_cycle, &cfg) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return n > 0;
+}
+
+int mg_cluster_cycle(const ClArgs &a, size_t smem, cudaStream_t s) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[2];
+    int st = cl_config(smem, s, &cfg, attr);
+    if (st) return st;
+    return cuda_status(cudaLaunchKernelEx(&cfg, k_cluster_cycle, a), "mg_cluster_cycle");
+}
+
+// the mixed form's cluster sub-cycle: 0 (the default) off, the level
+// kernels; m >= 1 (product build) one cluster launch a sub-cycle from m
+// levels above the coarse operator's level (fewer if they do not fit).
+// Measured slower than the level kernels at every m on the GB300.
+int &cluster_mode() {
+    static int m = 0;
+    return m;
+}
 }  // namespace f2d
 
 extern "C" {
+
+// the mixed form's cluster sub-cycle: 0 off (the default), m = 1..8 from m
+// levels above the coarse operator's level (product build; the exact build
+// keeps 0); < 0 only queries; returns the previous setting.  It applies to
+// models created after the change.
+int f2d_set_cluster(int mode) {
+    const int prev = f2d::cluster_mode();
+#ifndef F2D_EXACT
+    if (mode >= 0 && mode <= 8) f2d::cluster_mode() = mode;
+#endif
+    return prev;
+}
 
 // the CTA count the multigrid level kernels aim at when they choose their
 // tile: -1 twice the SM count, 0 always the largest tile (the default), > 0

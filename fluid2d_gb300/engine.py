@@ -304,6 +304,13 @@ class Model(object):
                    ctypes.byref(n))
         return n.value
 
+    def cluster_level(self):
+        """The float level from which the mixed form's small-level cycles run
+        as one thread-block-cluster launch (-1: none)."""
+        lev = ctypes.c_int()
+        self._call("f2d_model_cluster_level", self.h, ctypes.byref(lev))
+        return lev.value
+
     def set_islands(self, rhsp, psi):
         """Islands with a prescribed streamfunction: the rhsp and psi arrays of
         core/island.py (``fluid2d_gb300.island.Island.finalize``)."""

@@ -300,6 +300,12 @@ int f2d_model_coarse_level(void *model, int level, int *current, int *first, int
  * (default), 0 off, < 0 query; *n receives the operator's size (0: none). */
 int f2d_model_coarse_op(void *model, int enable, int *n);
 
+/* The float level from which the mixed form's small-level V- and F-cycles
+ * run as one thread-block-cluster launch (f2d_set_cluster), -1 if none (no
+ * float levels, no coarse operator, fewer than 16 coarse rows, the switch
+ * off).  No counterpart in the reference. */
+int f2d_model_cluster_level(void *model, int *level);
+
 /* Drop the model's captured step and loop graphs: the next graph run
  * captures again, with the launch settings then current (level tiles and
  * threads, programmatic dependent launch). */
@@ -330,6 +336,16 @@ int f2d_set_level_tiles(int target);
  * operations.  < 0 queries; returns the previous setting.  The exact build
  * always uses 0; graphs captured before a change keep their kernels. */
 int f2d_set_separable(int mode);
+
+/* The mixed form's small levels (no counterpart in the reference: a launch
+ * structure): m = 1..8 (product build) a V-cycle from zero or the F-cycle
+ * from m levels above the coarse operator's level (fewer where their
+ * strips do not fit) runs as one launch of a 16-CTA thread-block cluster
+ * holding those levels in distributed shared memory, with the level
+ * kernels' arithmetic bit for bit; 0 (the default) the level kernels,
+ * which measured faster.  < 0 queries; returns the previous setting.
+ * Applies to models created after the change; the exact build keeps 0. */
+int f2d_set_cluster(int mode);
 
 /* Threads of the fused level smoother's CTA: 0 one per tile point (the
  * input ring and the first sweep's ring take a second pass; default), 1 one

@@ -64,3 +64,53 @@ def test_mixed_single_and_multi_step_error(name):
     nite, res, st = G.solve_stats()
     if wl["model"] != "boussinesq":
         assert st == 0 and nite <= 4 and res < 1e-8
+
+
+@pytest.mark.parametrize("levels", [8, 1])
+@pytest.mark.parametrize("name", ["turbulence-256", "islands-256", "shear-512x128", "qg-256"])
+def test_cluster_subcycle_equals_the_level_kernels(name, levels):
+    """Mixed form, product build: the small levels' V- and F-cycles as one
+    launch of a 16-CTA cluster (levels in distributed shared memory, ghost
+    rows exchanged between phases) evaluate the level kernels' expressions
+    in their order: the states after three steps equal the level kernels'
+    bit for bit, on periodic, closed-with-islands and channel domains and
+    QG's Helmholtz operator, with every level that fits in the cluster or
+    only the one above the coarse operator's."""
+    import torch
+    from fluid2d_gb300 import _lib, engine
+    from fluid2d_gb300 import workloads as W
+    if name == "turbulence-256":
+        wl = W.turbulence(256, 256, seed=11)
+    elif name == "shear-512x128":
+        wl = W.shear(512, 128, seed=12)
+    else:
+        wl = W.dipole(256, 256, seed=13)
+        if name == "islands-256":
+            from tests import _cases as C
+            wl["msk"] = C.mask(262, 262, "closed", 4, 13)
+            wl["fields"]["vorticity"] = wl["fields"]["vorticity"] * wl["msk"]
+        else:
+            wl["model"] = "quasigeostrophic"
+            wl["fields"] = {"pv": wl["fields"]["vorticity"]}
+    kw = {"Rd": 0.3, "beta": 2.0} if wl["model"] == "quasigeostrophic" else {}
+    P = _lib.lib("product")
+
+    def run(mode):
+        old = P.f2d_set_cluster(mode)
+        try:
+            M = engine.from_workload(wl, dt=1e-3, precision="mixed", **kw)
+            lev = M.cluster_level()
+            M.set_psi_from_vorticity()
+            M.diagnostics()
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                M.run(3, graph=True)
+            s.synchronize()
+            return lev, M.var.state.cpu().numpy()
+        finally:
+            P.f2d_set_cluster(old)
+
+    (lev_on, a), (lev_off, b) = run(levels), run(0)
+    assert lev_on >= 1 and lev_off == -1
+    assert P.f2d_set_cluster(-1) == 0
+    assert np.array_equal(a, b)

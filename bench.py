@@ -528,11 +528,17 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
     import torch
     from oracle import stepper
     n = wl["nx"]
+    from fluid2d_gb300 import _lib as lib
+    from fluid2d_gb300.autotune import tune_coarse_level, tune_level_tiles
+    L = lib.lib()
+    # the level tiles are process settings: tuned for this model, then put
+    # back for the measurements that follow
+    prev = (L.f2d_set_level_tiles(-2), L.f2d_set_level_threads(-1))
     Mm = engine.from_workload(wl, dt=dt, precision="mixed")
     Mm.var.state.copy_(s0)
     Mm.diagnostics()
-    from fluid2d_gb300.autotune import tune_coarse_level
     tune_coarse_level(Mm, steps=3, warmup=1)
+    tiles, _ = tune_level_tiles(Mm, steps=3, warmup=1)
     Mm.var.state.copy_(s0)
     Mm.diagnostics()
     with torch.cuda.stream(stream):
@@ -541,6 +547,8 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
     ms = _timed_graph(Mm, a.steps, stream)
     nite, res, st = Mm.solve_stats()
     del Mm
+    L.f2d_set_level_tiles(prev[0])
+    L.f2d_set_level_threads(prev[1])
     # one step of the mixed form and of the oracle from the oracle's state
     p, O = stepper.from_workload(wl)
     odt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
@@ -558,7 +566,8 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
             "ms_per_step": ms / a.steps, "dtype": "f32 fluxes and multigrid, f64 defect "
             "correction, RK accumulation and diagnostics",
             "single_step_error_vs_f64_oracle": err, "solve_iterations_last_step": nite,
-            "solve_residual_last_step": res}
+            "solve_residual_last_step": res,
+            "level_tiles": {"cta_target": tiles[0], "one_pass_threads": tiles[1]}}
 
 
 def bench_dipole(a, host):

@@ -247,6 +247,7 @@ EXTRA = {
     "f2d_set_level_threads": ([_I], _I),
     "f2d_set_separable": ([_I], _I),
     "f2d_set_cluster": ([_I], _I),
+    "f2d_set_l2_persist": ([_I], _I),
     "f2d_fp64_peak": ([ctypes.POINTER(ctypes.c_double)], _I),
     "f2d_last_error": ([], ctypes.c_char_p),
     "f2d_exact_arithmetic": ([], _I),

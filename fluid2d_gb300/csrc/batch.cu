@@ -35,6 +35,11 @@ bool &pdl_enabled() {
     return on;
 }
 
+cudaAccessPolicyWindow &l2_window() {
+    static thread_local cudaAccessPolicyWindow w = {};
+    return w;
+}
+
 static BatchLaunchFn batch_launcher(int kind) {
     static const BatchLaunchFn table[BK_COUNT] = {
 #define F2D_KIND_FN(n) &batch_launch_##n,

@@ -240,6 +240,72 @@ static std::vector<LevelInfo> gridinfo(int n, int m, double dx, double dy, int n
     return v;
 }
 
+// ---- L2 persisting windows
+// 1 (default): the multigrid cycles' launches carry a persisting L2
+// access-policy window over the hierarchy's small levels (and the coarse
+// operator's application over the operator), so that the finest level's
+// streaming does not evict them between visits; 0: none
+static int &l2_persist_mode() {
+    static int m = 1;
+    return m;
+}
+
+// bytes of L2 set aside for persisting accesses in this process's context
+// (a context limit, released with the context): the device's maximum, at
+// most 32 MB; 0 if unavailable
+static size_t l2_setaside() {
+    static long long bytes = -1;
+    if (bytes < 0) {
+        bytes = 0;
+        int dev = 0, maxb = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&maxb, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
+            maxb > 0) {
+            const size_t want = std::min<size_t>((size_t)maxb, (size_t)32 << 20);
+            if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
+                bytes = (long long)want;
+        }
+        (void)cudaGetLastError();
+    }
+    return (size_t)bytes;
+}
+
+// a persisting window over [p, p + bytes) (hit ratio scaled to the set-aside)
+static cudaAccessPolicyWindow l2_persist_window(void *p, size_t bytes) {
+    cudaAccessPolicyWindow w = {};
+    const size_t aside = l2_setaside();
+    int dev = 0, maxw = 0;
+    if (!aside || !p || !bytes || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess ||
+        maxw <= 0) {
+        (void)cudaGetLastError();
+        return w;
+    }
+    w.base_ptr = p;
+    w.num_bytes = std::min(bytes, (size_t)maxw);
+    w.hitRatio = (float)std::min(1.0, (double)aside / (double)w.num_bytes);
+    w.hitProp = cudaAccessPropertyPersisting;
+    w.missProp = cudaAccessPropertyStreaming;
+    return w;
+}
+
+// the window `w` on this thread's launches for the guard's lifetime (not
+// while a step is being recorded: a merged launch serves many instances)
+struct L2Guard {
+    cudaAccessPolicyWindow prev = {};
+    bool on;
+    explicit L2Guard(const cudaAccessPolicyWindow &w)
+        : on(w.num_bytes > 0 && l2_persist_mode() && recorder() == nullptr) {
+        if (on) {
+            prev = l2_window();
+            l2_window() = w;
+        }
+    }
+    ~L2Guard() {
+        if (on) l2_window() = prev;
+    }
+};
+
 struct Gmg {
     int nlev = 0;
     std::vector<LevelInfo> info;
@@ -308,6 +374,7 @@ struct Gmg {
         op_cs = -1;
         op_n = 0;
         cl_lev = -1;
+        l2w_op[0] = l2w_op[1] = {};
     }
     ~Gmg() {
         for (int k = 0; k < MAX_PROBES; k++)
@@ -331,6 +398,10 @@ struct Gmg {
     // levels >= 1 (float64 product build): flags of the points whose stored
     // stencil is the level's uniform one (null: none) and that stencil
     // (c, ey, ex, c3), for the column-form sweeps
+    // L2 persisting windows: the small levels' arrays (the cycles' launches)
+    // and the coarse operators (their application)
+    static constexpr size_t L2_WINDOW_MAX = 24u << 20;
+    cudaAccessPolicyWindow l2w_levels = {}, l2w_op[2] = {};
     uint8_t *ufl[MAX_LEVELS] = {};
     double ust[MAX_LEVELS][4] = {};
     float ustf[MAX_LEVELS][4] = {};  // the same in float (the float planes are its casts)
@@ -412,6 +483,9 @@ int Gmg::build_coarse_op(cudaStream_t s) {
     }
     op_cs = cs;
     op_n = n;
+    for (int k = 0; k < 2; k++)
+        l2w_op[k] = has_f32 ? l2_persist_window(opf[k], nn * sizeof(float))
+                            : l2_persist_window(opd[k], nn * sizeof(double));
     cluster_setup();
     return OK;
 #endif
@@ -522,7 +596,6 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
         o_msk[l] = mem.add(pl);
         o_A[l] = l > 0 ? mem.add(6 * pl * sizeof(double)) : 0;
         o_Af[l] = (l > 0 && f32) ? mem.add(6 * pl * sizeof(float)) : 0;
-        o_A9[l] = mem.add(9 * pl * sizeof(double));  // set-up only
         o_x[l] = mem.add(pl * sizeof(double));
         o_b[l] = mem.add(pl * sizeof(double));
         o_r[l] = mem.add(pl * sizeof(double));
@@ -534,6 +607,10 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
             o_tf[l] = mem.add(pl * sizeof(float));
         }
     }
+    // the arrays the cycles read, level by level, are contiguous: the small
+    // levels' span is the L2 persisting window (set-up-only arrays follow)
+    const size_t o_levels_end = mem.total;
+    for (int l = 0; l < nlev; l++) o_A9[l] = mem.add(9 * (size_t)mv[l] * nv[l] * sizeof(double));
     size_t o_coef = mem.add(maxpl * sizeof(double));
     size_t o_work = mem.add(sizeof(double) * RED_MAX_BLOCKS * RED_MAX_VALUES);
     size_t o_sums = mem.add(8 * sizeof(double));
@@ -555,6 +632,12 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
     }
 #endif
     TRY(mem.alloc());
+    {   // the L2 window: the finest level >= 1 from which the levels' arrays fit
+        int l2 = 1;
+        while (l2 < nlev && o_levels_end - o_msk[l2] > L2_WINDOW_MAX) l2++;
+        l2w_levels = {};
+        if (l2 < nlev) l2w_levels = l2_persist_window(mem.base + o_msk[l2], o_levels_end - o_msk[l2]);
+    }
     work = mem.at<double>(o_work);
     sums = mem.at<double>(o_sums);
     solve_state = mem.at<SolveState>(o_solve);
@@ -760,6 +843,7 @@ int Gmg::coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int
                 cudaStream_t s) {
     if (op_n > 0 && op_cs == cs && start == cs && (mode == CYCLE_F || zero_first)) {
         const T *o = op<T>(mode == CYCLE_F ? 1 : 0);
+        L2Guard guard(l2w_op[mode == CYCLE_F ? 1 : 0]);
         if (o) return mg_coarse_apply<T>(o, op_n, L[start], active, s);
     }
     size_t smem = coarse_smem_bytes<T>(mv + start, nv + start, nlev - start);
@@ -772,6 +856,7 @@ int Gmg::coarse(LevelView<T> *L, int start, int mode, bool zero_first, const int
 template <typename T>
 int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cudaStream_t s,
                 int first_mode) {
+    L2Guard guard(l2w_levels);
     const int deep = nlev - 1;
     if (l1 >= cs) return coarse(L, l1, CYCLE_V, zero_first, active, s);
     const int stop = cs < deep ? cs : deep;
@@ -805,6 +890,7 @@ int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cud
 // core/gmg/hierarchy.py:131-151
 template <typename T>
 int Gmg::fcycle(LevelView<T> *L, int l1, const int *active, cudaStream_t s) {
+    L2Guard guard(l2w_levels);
     const int deep = nlev - 1;
     if (l1 >= cs) return coarse(L, l1, CYCLE_F, false, active, s);
     const int stop = cs < deep ? cs : deep;
@@ -2194,6 +2280,15 @@ int f2d_model_coarse_op(void *model, int enable, int *n) {
     }
     if (n) *n = g.op_n;
     return OK;
+}
+
+// the multigrid cycles' persisting L2 windows: 1 on (the default), 0 off;
+// < 0 only queries; returns the previous setting.  Read when a step is
+// launched or captured.
+int f2d_set_l2_persist(int mode) {
+    const int prev = l2_persist_mode();
+    if (mode == 0 || mode == 1) l2_persist_mode() = mode;
+    return prev;
 }
 
 // the float level from which the mixed form's small-level cycles run as one

@@ -39,6 +39,11 @@ F2D_DEV void pdl_prologue() { asm volatile("griddepcontrol.wait;" ::: "memory");
 // 2-4 % shorter 1024^2 float64 and mixed steps, 1.5 % on the batched ensemble)
 bool &pdl_enabled();
 
+// The L2 access-policy window the launches of this host thread carry (a
+// persisting window over a multigrid hierarchy's small levels, set by the
+// hierarchy around its cycles; num_bytes 0: none)
+cudaAccessPolicyWindow &l2_window();
+
 template <typename A>
 int launch_pdl(void (*kernel)(A), const A &a, dim3 grid, dim3 block, size_t smem,
                cudaStream_t s) {
@@ -47,11 +52,21 @@ int launch_pdl(void (*kernel)(A), const A &a, dim3 grid, dim3 block, size_t smem
     cfg.blockDim = block;
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchAttribute attr[2];
+    int n = 0;
+    if (pdl_enabled()) {
+        attr[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[n].val.programmaticStreamSerializationAllowed = 1;
+        n++;
+    }
+    const cudaAccessPolicyWindow &w = l2_window();
+    if (w.num_bytes) {
+        attr[n].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[n].val.accessPolicyWindow = w;
+        n++;
+    }
     cfg.attrs = attr;
-    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cfg.numAttrs = n;
     return (int)cudaLaunchKernelEx(&cfg, kernel, a);
 }
 #define F2D_VB_NATIVE \

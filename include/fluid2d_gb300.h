@@ -347,6 +347,14 @@ int f2d_set_separable(int mode);
  * Applies to models created after the change; the exact build keeps 0. */
 int f2d_set_cluster(int mode);
 
+/* Persisting L2 windows (no counterpart in the reference: cache control):
+ * 1 (default) the multigrid cycles' launches mark the hierarchy's small
+ * levels (and the coarse operator's application the operator) for
+ * persisting L2 residency, with up to 32 MB of L2 set aside for the
+ * process's context; 0 off.  < 0 queries; returns the previous setting.
+ * Graphs captured before a change keep their launches. */
+int f2d_set_l2_persist(int mode);
+
 /* Threads of the fused level smoother's CTA: 0 one per tile point (the
  * input ring and the first sweep's ring take a second pass; default), 1 one
  * per input point, so that every phase is one pass, for grids of fewer than

@@ -344,6 +344,36 @@ def test_stored_level_column_sweeps(eng, geom, islands):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_l2_persisting_windows_change_nothing_but_timing(eng, precision):
+    """The persisting L2 access-policy windows on the multigrid cycles'
+    launches (f2d_set_l2_persist) leave every state bit unchanged, eager and
+    replayed from a graph."""
+    import torch
+    from fluid2d_gb300 import _lib
+    from fluid2d_gb300 import workloads as W
+    P = _lib.lib("product")
+    wl = W.turbulence(256, 256, seed=3)
+
+    def run(mode):
+        old = P.f2d_set_l2_persist(mode)
+        try:
+            M = eng.from_workload(wl, dt=1e-3, precision=precision)
+            M.set_psi_from_vorticity()
+            M.diagnostics()
+            M.run(2)
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                M.run(2, graph=True)
+            s.synchronize()
+            return M.var.state.cpu().numpy()
+        finally:
+            P.f2d_set_l2_persist(old)
+
+    assert P.f2d_set_l2_persist(-1) == 1
+    assert np.array_equal(run(1), run(0))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_level_tiles_change_nothing_but_launches(eng, precision):
     """Every CTA tile target and smoother block size of the level kernels
     gives the same state bit for bit (exact build); the tuner keeps one."""

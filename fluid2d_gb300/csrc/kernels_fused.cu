@@ -1045,21 +1045,18 @@ __global__ void __launch_bounds__(LV_TX *LV_TY) k_residualc(ResidualCArgs<T> a) 
     residualc_body<T>(a, F2D_VB_NATIVE);
 }
 
-// false (nothing launched) where the column form does not apply: the
-// separable mode off, no coefficient bits, not the 9-point operator with
-// corners = edges / 2, a step being recorded, a grid of fewer CTAs than SMs
+// false (nothing launched) where the column form does not apply
+// (column_l0_applies: the separable mode off, no coefficient bits, not the
+// 9-point operator with corners = edges / 2, a step being recorded, a grid
+// of fewer CTAs than SMs)
 template <typename T>
 bool residual_column(const LevelView<T> &L, const AnalyticT<T> &an, const T *x, const T *b, T *r,
                      float *rf, const int *active, cudaStream_t s, int *st) {
     *st = OK;
-    if (!separable_mode() || recorder() != nullptr || !L.nb) return false;
-    const T e = an.sc[1];
-    if (!(e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e && an.sc[2] == an.sc[0]))
-        return false;
+    if (!column_l0_applies(L, an)) return false;
     const int rows = L.mv - 2 * NH, cols = L.nv - 2 * NH;
     const dim3 g((unsigned)((cols + LV_TX - 1) / LV_TX),
                  (unsigned)((rows + LV_TY * SC_K - 1) / (LV_TY * SC_K)));
-    if (separable_mode() == 1 && (long long)g.x * g.y < sm_count()) return false;
     ResidualCArgs<T> a;
     memset(&a, 0, sizeof(a));
     a.L = L;

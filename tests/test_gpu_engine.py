@@ -362,6 +362,7 @@ def test_l2_persisting_windows_change_nothing_but_timing(eng, precision):
             M.diagnostics()
             M.run(2)
             s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())  # the eager steps first
             with torch.cuda.stream(s):
                 M.run(2, graph=True)
             s.synchronize()

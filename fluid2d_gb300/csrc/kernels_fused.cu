@@ -1567,10 +1567,38 @@ F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
     const int tid = (int)threadIdx.x;
     const int mv = F.mv, nv = F.nv;
     const float inv = 1.0f / (float)RW;
+#ifndef F2D_EXACT
+    // the analytic finest level (product build): a warp whose points all
+    // have fluid 3x3 blocks takes the separable form of the 9-point operator,
+    // r = b + kv V + kx x (kv = -e/2, kx = 2e - a5 for edges e and corners
+    // e/2), without the coefficient selects
+    const T e = an.sc[1];
+    const bool nine = L0 && F.nb && e != (T)0 && an.sc[3] == e && an.sc[0] == (T)0.5 * e &&
+                      an.sc[2] == an.sc[0];
+    const T kv = -an.sc[0], kx = (T)4 * an.sc[0] - an.a5;
+#endif
     for (int q = tid; q < RH * RW; q += NT) {
         const int qj = small_div(q, inv);
         const int jf = jf0 + qj, iff = if0 + (q - qj * RW);
-        if (jf > mv - 3 || iff > nv - 3) continue;  // beyond the last coarse point's stencil
+        const bool in = jf <= mv - 3 && iff <= nv - 3;  // within the last coarse point's stencil
+#ifndef F2D_EXACT
+        if (nine) {
+            const int jw = in ? wrap(jf, mv, NH) : NH, iw = in ? wrap(iff, nv, NH) : NH;
+            const size_t p = off(jw, iw, nv);
+            const bool full = !in || F.nb[p] == 511u;
+            if (__all_sync(__activemask(), full)) {
+                if (in) {
+                    const T *x = F.x + p;
+                    const T corners = (x[-nv - 1] + x[-nv + 1]) + (x[nv - 1] + x[nv + 1]);
+                    const T edges = (x[-nv] + x[nv]) + (x[-1] + x[1]);
+                    const T V = fma((T)4, x[0], fma((T)2, edges, corners));
+                    rs[q] = fma(kv, V, fma(kx, x[0], F.b[p]));
+                }
+                continue;
+            }
+        }
+#endif
+        if (!in) continue;
         rs[q] = residual<T, L0>(F, &an, F.x, F.b, wrap(jf, mv, NH), wrap(iff, nv, NH));
     }
     __syncthreads();

@@ -358,24 +358,21 @@ def run_ours(a, rank, world, local):
     roofline = smoother_roofline(n, probe_ms, nprobe)
 
     # ---- e2e through the public API with host buffers: every step uploads
-    # the state (Var.state) from pinned memory, steps, reads it back
+    # the state (Var.state's layout) from pinned memory, steps, reads it back
+    # (Model.run_host: one call a step; the copies and the step are one graph)
     state_host = torch.empty(M.var.state.shape, dtype=torch.float64).pin_memory()
     state_host.copy_(M.var.state.cpu())
     h2d = d2h = state_host.numel() * 8
     with torch.cuda.stream(stream):
         for _ in range(2):
-            M.var.state.copy_(state_host, non_blocking=True)
-            M.run(1, graph=True)
-            state_host.copy_(M.var.state, non_blocking=True)
+            M.run_host(1, state_host)
         stream.synchronize()
         barrier()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         for _ in range(a.e2e_steps):
-            M.var.state.copy_(state_host, non_blocking=True)
-            M.run(1, graph=True)
-            state_host.copy_(M.var.state, non_blocking=True)
+            M.run_host(1, state_host)
         f1.record(stream)
         f1.synchronize()
     e2e_ms = f0.elapsed_time(f1)

@@ -208,6 +208,7 @@ SIGNATURES.update({
     "f2d_model_diagnostics": [_P, _P],
     "f2d_model_step": [_P, _I, _P],
     "f2d_model_step_graph": [_P, _I, _P],
+    "f2d_model_step_host": [_P, _I, ctypes.c_void_p, ctypes.c_void_p],
     "f2d_model_set_dt": [_P, _D],
     "f2d_model_solve_stats": [_P, _PI, _PDd, _PI],
     "f2d_model_status": [_P, _I, _PI, _P],

@@ -1342,6 +1342,18 @@ struct Model {
     int probe_per_step = -1;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // the step with the state uploaded from and read back to host memory
+    // hptr, captured as one graph (f2d_model_step_host)
+    cudaGraph_t hgraph = nullptr;
+    cudaGraphExec_t hexec = nullptr;
+    double *hptr = nullptr;
+    void drop_host_graph() {
+        if (hexec) cudaGraphExecDestroy(hexec);
+        if (hgraph) cudaGraphDestroy(hgraph);
+        hexec = nullptr;
+        hgraph = nullptr;
+        hptr = nullptr;
+    }
 
     double *plane(double *base, const char *name) {
         for (int k = 0; k < nvar; k++)
@@ -2083,6 +2095,7 @@ int f2d_model_destroy(void *model) {
     if (!M) return OK;
     if (M->gexec) cudaGraphExecDestroy(M->gexec);
     if (M->graph) cudaGraphDestroy(M->graph);
+    M->drop_host_graph();
     delete M->loop;
     delete M->flux;
     delete M->noslip;
@@ -2168,6 +2181,7 @@ int f2d_model_set_dt(void *model, double dt) {
         M->gexec = nullptr;
         M->graph = nullptr;
     }
+    M->drop_host_graph();
     if (M->loop) {
         M->loop->k.dt0 = dt;
         if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
@@ -2205,6 +2219,51 @@ int f2d_model_step_graph(void *model, int nsteps, void *stream) {
     return OK;
 }
 
+// nsteps steps of the model whose state lives in host memory `host`
+// (page-locked, the state's layout: nvar planes of (ny+6) x (nx+6) float64):
+// every step uploads it, steps and reads it back, the three captured as one
+// graph (for this host buffer) and replayed, so that no host-side gap
+// separates the copies from the step.
+int f2d_model_step_host(void *model, int nsteps, double *host, void *stream) {
+    Model *M = (Model *)model;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!M || nsteps < 0 || !s || !host) {
+        set_error("f2d_model_step_host: needs a model, a host buffer and a non-default stream");
+        return ERR_ARG;
+    }
+    if (M->hexec && M->hptr != host) M->drop_host_graph();
+    if (!M->hexec) {
+        const size_t bytes = (size_t)M->nvar * M->pl * sizeof(double);
+        TRY(cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                        "begin capture"));
+        int st = cuda_status(cudaMemcpyAsync(M->X, host, bytes, cudaMemcpyHostToDevice, s),
+                             "state upload (the host buffer must be page-locked)");
+        if (!st) st = M->step(s);
+        if (!st)
+            st = cuda_status(cudaMemcpyAsync(host, M->X, bytes, cudaMemcpyDeviceToHost, s),
+                             "state read-back");
+        cudaGraph_t g = nullptr;
+        const int st2 = cuda_status(cudaStreamEndCapture(s, &g), "end capture");
+        if (st || st2) {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            return st ? st : st2;
+        }
+        cudaGraphExec_t e = nullptr;
+        const int st3 = cuda_status(cudaGraphInstantiate(&e, g, 0), "graph instantiate");
+        if (st3) {
+            cudaGraphDestroy(g);
+            return st3;
+        }
+        M->hgraph = g;
+        M->hexec = e;
+        M->hptr = host;
+    }
+    for (int k = 0; k < nsteps; k++)
+        TRY(cuda_status(cudaGraphLaunch(M->hexec, s), "graph launch"));
+    return OK;
+}
+
 // Where the hierarchy switches to the single-CTA coarse solve: any level from
 // the finest whose suffix fits the CTA's shared memory to nlev (no CTA).  The
 // arithmetic is the same either way; only the launch structure changes.
@@ -2217,6 +2276,7 @@ static void drop_graphs(Model *M) {
     if (M->graph) cudaGraphDestroy(M->graph);
     M->gexec = nullptr;
     M->graph = nullptr;
+    M->drop_host_graph();
     if (M->loop) {
         if (M->loop->exec) cudaGraphExecDestroy(M->loop->exec);
         if (M->loop->graph) cudaGraphDestroy(M->loop->graph);

@@ -245,6 +245,18 @@ class Model(object):
         else:
             self._call("f2d_model_step", self.h, int(nsteps), _stream())
 
+    def run_host(self, nsteps, state_host):
+        """nsteps steps with the state in host memory: ``state_host`` (a
+        page-locked float64 tensor shaped like ``var.state``) is uploaded,
+        stepped and read back every step, as one captured graph replayed on
+        the current (non-default) stream.  Asynchronous."""
+        if (state_host.device.type != "cpu" or state_host.dtype != torch.float64
+                or tuple(state_host.shape) != tuple(self.var.state.shape)
+                or not state_host.is_contiguous() or not state_host.is_pinned()):
+            raise ValueError("run_host: needs a page-locked contiguous float64 host tensor "
+                             "shaped like var.state")
+        self._call("f2d_model_step_host", self.h, int(nsteps), state_host.data_ptr(), _stream())
+
     def probe(self, enable=None):
         """Enable/disable the finest-level smoother probe, or (enable=None)
         return (count, mean ms) over the probed calls of the last step."""

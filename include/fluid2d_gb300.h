@@ -254,6 +254,15 @@ int f2d_model_diagnostics(void *model, void *stream);
 int f2d_model_step(void *model, int nsteps, void *stream);
 /* the same, replaying one step captured in a CUDA graph (non-default stream) */
 int f2d_model_step_graph(void *model, int nsteps, void *stream);
+
+/* nsteps steps of a model whose state lives in host memory: every step
+ * uploads the state from `host` (page-locked; the layout of the model's
+ * state: nvar planes of (ny+6) x (nx+6) float64), steps and reads it back,
+ * the three captured once as one graph for this buffer and replayed on
+ * `stream` (non-default).  Asynchronous; the reference's Python holds its
+ * state in host arrays and calls the kernels on them every step (no
+ * single counterpart: core/fluid2d.py:235-265 over the drop-in modules). */
+int f2d_model_step_host(void *model, int nsteps, double *host, void *stream);
 int f2d_model_set_dt(void *model, double dt);
 int f2d_model_solve_stats(void *model, int *nite, double *res, int *status);
 /* The model's status word: F2D_STATUS_* bits that the diagnostics set after

@@ -122,6 +122,30 @@ def test_graph_replay_matches_eager(eng, name):
     assert torch.equal(A.var.state, B.var.state)
 
 
+def test_run_host_equals_the_device_steps(eng):
+    """Model.run_host (the state uploaded from page-locked host memory,
+    stepped and read back every step, one captured graph) gives the device
+    path's state bit for bit, in the host buffer and on the device."""
+    import torch
+    wl = _workloads()["euler-perio-turb"]
+    A = eng.from_workload(wl, variant="product", dt=1e-3)
+    B = eng.from_workload(wl, variant="product", dt=1e-3)
+    for M in (A, B):
+        M.set_psi_from_vorticity()
+        M.diagnostics()
+    host = torch.empty(B.var.state.shape, dtype=torch.float64).pin_memory()
+    host.copy_(B.var.state.cpu())
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        A.run(3, graph=True)
+        B.run_host(3, host)
+    s.synchronize()
+    assert torch.equal(A.var.state.cpu(), host)
+    assert torch.equal(A.var.state, B.var.state)
+    with pytest.raises(ValueError):
+        B.run_host(1, torch.zeros(B.var.state.shape, dtype=torch.float64))
+
+
 def test_gmg_twovcycle_and_solve(eng):
     import torch
     from oracle import stepper

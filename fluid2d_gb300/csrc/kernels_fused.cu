@@ -175,20 +175,12 @@ F2D_DEV T restrict_value(const int8_t *msk2, int nv2, const T *r, int nv1, int J
         + (T)0.0625 * (r[c - nv1 - 1] + r[c - nv1 + 1] + r[c + nv1 - 1] + r[c + nv1 + 1]);
 }
 
-// bilinear prolongation value at fine (J1, I1), nh = 3
+// the bilinear prolongation of a fine point of parity (dj, di) and mask m1
+// from the four coarse points of its cell (masks k.., values x..)
 // (core/gmg/fortran_multigrid.f90:449-496)
 template <typename T>
-F2D_DEV T interp_value(const int8_t *msk1, int nv1, const int8_t *msk2, const T *x2, int nv2,
-                       int J1, int I1) {
-    const int J2 = (J1 >> 1) + 1, I2 = (I1 >> 1) + 1;
-    const int dj = J1 & 1, di = I1 & 1;
-    const size_t q = off(J2, I2, nv2);
-    // every operand is read up front (one memory round trip; the four coarse
-    // points exist for every fine point of rows/cols 1..m-2), and the weight
-    // tables are selects rather than indexed local arrays
-    const int m1 = msk1[off(J1, I1, nv1)];
-    const int k00 = msk2[q], k01 = msk2[q + 1], k10 = msk2[q + nv2], k11 = msk2[q + nv2 + 1];
-    const T x00 = x2[q], x01 = x2[q + 1], x10 = x2[q + nv2], x11 = x2[q + nv2 + 1];
+F2D_DEV T interp_combine(int m1, int dj, int di, int k00, int k01, int k10, int k11, T x00, T x01,
+                         T x10, T x11) {
     if (m1 <= 0) return (T)0;
     if (!dj && !di) return x00;
     if (!dj || !di) {
@@ -203,6 +195,23 @@ F2D_DEV T interp_value(const int8_t *msk1, int nv1, const int8_t *msk2, const T 
                                                : sm4 == 3 ? (T)r4(0.3333333333333333333333333333f)
                                                           : (T)0.25;
     return c * (x00 + x01 + x10 + x11);
+}
+
+// bilinear prolongation value at fine (J1, I1), nh = 3
+// (core/gmg/fortran_multigrid.f90:449-496)
+template <typename T>
+F2D_DEV T interp_value(const int8_t *msk1, int nv1, const int8_t *msk2, const T *x2, int nv2,
+                       int J1, int I1) {
+    const int J2 = (J1 >> 1) + 1, I2 = (I1 >> 1) + 1;
+    const int dj = J1 & 1, di = I1 & 1;
+    const size_t q = off(J2, I2, nv2);
+    // every operand is read up front (one memory round trip; the four coarse
+    // points exist for every fine point of rows/cols 1..m-2), and the weight
+    // tables are selects rather than indexed local arrays
+    const int m1 = msk1[off(J1, I1, nv1)];
+    const int k00 = msk2[q], k01 = msk2[q + 1], k10 = msk2[q + nv2], k11 = msk2[q + nv2 + 1];
+    const T x00 = x2[q], x01 = x2[q + 1], x10 = x2[q + nv2], x11 = x2[q + nv2 + 1];
+    return interp_combine<T>(m1, dj, di, k00, k01, k10, k11, x00, x01, x10, x11);
 }
 
 // store an interior value and its periodic halo images
@@ -1378,21 +1387,45 @@ F2D_DEV void smooth_l0_body(const SmoothFusedArgs<T> &A, const VB vb) {
     // the rings are walked as flat index ranges (full warps; the constant
     // widths make the row/column split a multiply-shift)
     const int tid = (int)threadIdx.x;
-    if (xmode != X_ZERO) {
+    if (xmode == X_IN) {
         const T *xg = L.x + o2;
         for (int q = tid; q < SL_XW * SL_XW; q += SL_THREADS) {
             const int r = q / SL_XW, c = q - r * SL_XW;
             const int j = j0 - 2 + r, i = i0 - 2 + c;
             if (j < 1 || j > mv - 2 || i < 1 || i > nv - 2) continue;
-            const int o = r * nv + c;
-            T v;
-            if (xmode == X_IN) {
-                v = xg[o];
-            } else {
-                const T cv = interp_value(L.msk, nv, A.cs.msk, A.cs.x, A.cs.nv, j, i);
-                v = xmode == X_PLUS_INTERP ? xg[o] + cv : cv;
+            xs[q] = xg[r * nv + c];
+        }
+    } else if (xmode != X_ZERO) {
+        // the prolongation by coarse cells: the fine points (2J-2+dj, 2I-2+di)
+        // of cell (J, I) share its four coarse values and masks (one load of
+        // each a cell instead of a point); the ring's rows/cols 1..m-2 only
+        const T *xg = L.x + o2;
+        const int ja = max(1, j0 - 2), jb = min(mv - 2, j0 + SL_XW - 3);
+        const int ia = max(1, i0 - 2), ib = min(nv - 2, i0 + SL_XW - 3);
+        const int Ja = (ja >> 1) + 1, Ia = (ia >> 1) + 1;
+        const int ch = (jb >> 1) + 1 - Ja + 1, cw = (ib >> 1) + 1 - Ia + 1;
+        const int nc2 = A.cs.nv;
+        for (int q = tid; q < ch * cw; q += SL_THREADS) {
+            const int cr = q / cw, J = Ja + cr, I = Ia + q - cr * cw;
+            const size_t p2 = off(J, I, nc2);
+            const int k00 = A.cs.msk[p2], k01 = A.cs.msk[p2 + 1], k10 = A.cs.msk[p2 + nc2],
+                      k11 = A.cs.msk[p2 + nc2 + 1];
+            const T x00 = A.cs.x[p2], x01 = A.cs.x[p2 + 1], x10 = A.cs.x[p2 + nc2],
+                    x11 = A.cs.x[p2 + nc2 + 1];
+#pragma unroll
+            for (int dj = 0; dj < 2; dj++) {
+                const int j = 2 * J - 2 + dj;
+                if (j < ja || j > jb) continue;
+#pragma unroll
+                for (int di = 0; di < 2; di++) {
+                    const int i = 2 * I - 2 + di;
+                    if (i < ia || i > ib) continue;
+                    const int r = j - (j0 - 2), c = i - (i0 - 2);
+                    const T cv = interp_combine<T>(L.msk[off(j, i, nv)], dj, di, k00, k01, k10,
+                                                   k11, x00, x01, x10, x11);
+                    xs[r * SL_XW + c] = xmode == X_PLUS_INTERP ? xg[r * nv + c] + cv : cv;
+                }
             }
-            xs[q] = v;
         }
     }
     // bits, mask and b of the first sweep's points (rows/cols 2..m-3)

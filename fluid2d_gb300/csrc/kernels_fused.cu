@@ -658,7 +658,8 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     const int i0 = NH + vb.x * TX, j0 = NH + vb.y * TY;
     const int tid = (int)threadIdx.x;
     // input x on [j0-2, j0+TY+1] x [i0-2, i0+TX+1], inside rows/cols 1..m-2
-    if (xmode != X_ZERO) {
+    // (float64: point by point; its register budget has no room for a cell)
+    if (xmode == X_IN || (xmode != X_ZERO && sizeof(T) == 8)) {
         const float inv = 1.0f / (float)XW;
         for (int q = tid; q < XH * XW; q += NT) {
             const int qj = small_div(q, inv);
@@ -673,6 +674,37 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
                 v = xmode == X_PLUS_INTERP ? L.x[p] + c : c;
             }
             xs[q] = v;
+        }
+    } else if (xmode != X_ZERO) {
+        // the prolongation by coarse cells (the fine points 2J-2+dj,
+        // 2I-2+di of cell (J, I) share its four coarse values and masks)
+        const int ja = max(1, j0 - 2), jb = min(mv - 2, j0 + TY + 1);
+        const int ia = max(1, i0 - 2), ib = min(nv - 2, i0 + TX + 1);
+        const int Ja = (ja >> 1) + 1, Ia = (ia >> 1) + 1;
+        const int ch = (jb >> 1) + 1 - Ja + 1, cw = (ib >> 1) + 1 - Ia + 1;
+        const int nc2 = cs.nv;
+        for (int q = tid; q < ch * cw; q += NT) {
+            const int cr = q / cw, J = Ja + cr, I = Ia + q - cr * cw;
+            const size_t p2 = off(J, I, nc2);
+            const int k00 = cs.msk[p2], k01 = cs.msk[p2 + 1], k10 = cs.msk[p2 + nc2],
+                      k11 = cs.msk[p2 + nc2 + 1];
+            const T x00 = cs.x[p2], x01 = cs.x[p2 + 1], x10 = cs.x[p2 + nc2],
+                    x11 = cs.x[p2 + nc2 + 1];
+#pragma unroll
+            for (int dj = 0; dj < 2; dj++) {
+                const int j = 2 * J - 2 + dj;
+                if (j < ja || j > jb) continue;
+#pragma unroll
+                for (int di = 0; di < 2; di++) {
+                    const int i = 2 * I - 2 + di;
+                    if (i < ia || i > ib) continue;
+                    const size_t p = off(j, i, nv);
+                    const T c = interp_combine<T>(L.msk[p], dj, di, k00, k01, k10, k11, x00, x01,
+                                                  x10, x11);
+                    xs[(j - (j0 - 2)) * XW + (i - (i0 - 2))] =
+                        xmode == X_PLUS_INTERP ? L.x[p] + c : c;
+                }
+            }
         }
     }
     __syncthreads();

@@ -658,22 +658,13 @@ F2D_DEV void smooth_fused_body(const SmoothFusedArgs<T> &A, const VB vb) {
     const int i0 = NH + vb.x * TX, j0 = NH + vb.y * TY;
     const int tid = (int)threadIdx.x;
     // input x on [j0-2, j0+TY+1] x [i0-2, i0+TX+1], inside rows/cols 1..m-2
-    // (float64: point by point; its register budget has no room for a cell)
-    if (xmode == X_IN || (xmode != X_ZERO && sizeof(T) == 8)) {
+    if (xmode == X_IN) {
         const float inv = 1.0f / (float)XW;
         for (int q = tid; q < XH * XW; q += NT) {
             const int qj = small_div(q, inv);
             const int j = j0 - 2 + qj, i = i0 - 2 + (q - qj * XW);
             if (j < 1 || j > mv - 2 || i < 1 || i > nv - 2) continue;
-            const size_t p = off(j, i, nv);
-            T v;
-            if (xmode == X_IN) {
-                v = L.x[p];
-            } else {
-                const T c = interp_value(L.msk, nv, cs.msk, cs.x, cs.nv, j, i);
-                v = xmode == X_PLUS_INTERP ? L.x[p] + c : c;
-            }
-            xs[q] = v;
+            xs[q] = L.x[off(j, i, nv)];
         }
     } else if (xmode != X_ZERO) {
         // the prolongation by coarse cells (the fine points 2J-2+dj,

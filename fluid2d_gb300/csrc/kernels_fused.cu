@@ -453,15 +453,34 @@ struct InterpArgs {
     const int *active;
 };
 
+// one thread per coarse cell (J, I): its fine points (2J-2+dj, 2I-2+di) in
+// rows/cols 1..m-2 share the cell's four coarse values and masks
 template <typename T>
 F2D_DEV void interp_body(const InterpArgs<T> &A, const VB vb) {
     if (inactive(A.active)) return;
-    const int I1 = 1 + vb.x * LV_TX + threadIdx.x;
-    const int J1 = 1 + vb.y * LV_TY + threadIdx.y;
-    if (I1 > A.nv1 - 2 || J1 > A.mv1 - 2) return;
-    const T v = interp_value(A.msk1, A.nv1, A.msk2, A.x2, A.nv2, J1, I1);
-    const size_t p = off(J1, I1, A.nv1);
-    A.dst[p] = A.assign ? v : A.dst[p] + v;
+    const int I = 1 + vb.x * LV_TX + threadIdx.x;
+    const int J = 1 + vb.y * LV_TY + threadIdx.y;
+    const int jmax = A.mv1 - 2, imax = A.nv1 - 2;
+    if (2 * I - 2 > imax || 2 * J - 2 > jmax) return;
+    const int nv2 = A.nv2;
+    const size_t p2 = off(J, I, nv2);
+    const int k00 = A.msk2[p2], k01 = A.msk2[p2 + 1], k10 = A.msk2[p2 + nv2],
+              k11 = A.msk2[p2 + nv2 + 1];
+    const T x00 = A.x2[p2], x01 = A.x2[p2 + 1], x10 = A.x2[p2 + nv2], x11 = A.x2[p2 + nv2 + 1];
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++) {
+        const int j = 2 * J - 2 + dj;
+        if (j < 1 || j > jmax) continue;
+#pragma unroll
+        for (int di = 0; di < 2; di++) {
+            const int i = 2 * I - 2 + di;
+            if (i < 1 || i > imax) continue;
+            const size_t p = off(j, i, A.nv1);
+            const T v = interp_combine<T>(A.msk1[p], dj, di, k00, k01, k10, k11, x00, x01, x10,
+                                          x11);
+            A.dst[p] = A.assign ? v : A.dst[p] + v;
+        }
+    }
 }
 
 template <typename T>
@@ -566,7 +585,8 @@ int mg_restrict(const LevelView<T> &fine, const T *src, const LevelView<T> &coar
 template <typename T>
 int mg_interp(const LevelView<T> &coarse, const T *src, const LevelView<T> &fine, T *dst,
               bool assign, const int *active, cudaStream_t s) {
-    dim3 g = lv_grid(fine.mv - 2, fine.nv - 2), b(LV_TX, LV_TY);
+    // coarse cells 1 .. (m-2)/2 + 1 hold the fine rows/cols 1 .. m-2
+    dim3 g = lv_grid(((fine.mv - 2) >> 1) + 1, ((fine.nv - 2) >> 1) + 1), b(LV_TX, LV_TY);
     InterpArgs<T> a{fine.msk, fine.mv, fine.nv, coarse.msk, src, coarse.nv, dst,
                     assign ? 1 : 0, active};
     return launch_body<BInterp<T>>(k_interp<T>, a, g, b, 0, s, "mg_interp");

@@ -456,7 +456,8 @@ def smoother_roofline(n, probe_ms, nprobe):
     Jacobi sweeps of core/gmg/fortran_multigrid.f90:2-127) against its bound,
     the float64 pipe: 19 flops per point per sweep (1 mul, 7 fma, 1 sub,
     1 mul, 1 fma), two sweeps per call, over the call's mean CUDA-event
-    duration inside the replayed step graph; peak = float64 FMA chains
+    duration inside the replayed step graph (the call after a coarse
+    correction also holds its prolongation); peak = float64 FMA chains
     measured live on this GPU (f2d_fp64_peak).  The flops are the
     algorithm's: the column form (k_sweepc) executes fewer float64
     instructions for the same sweep.  Beside it, the same call

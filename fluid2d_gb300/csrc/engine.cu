@@ -403,8 +403,8 @@ struct Gmg {
     static constexpr size_t L2_WINDOW_MAX = 24u << 20;
     cudaAccessPolicyWindow l2w_levels = {}, l2w_op[2] = {};
     uint8_t *ufl[MAX_LEVELS] = {};
-    double ust[MAX_LEVELS][4] = {};
-    float ustf[MAX_LEVELS][4] = {};  // the same in float (the float planes are its casts)
+    double ust[MAX_LEVELS][5] = {};  // (c, ey, ex, c3, a5)
+    float ustf[MAX_LEVELS][5] = {};  // the same in float (the float planes are its casts)
     template <typename T>
     const T *uniform_stencil(int l) const;
     template <typename T>
@@ -628,7 +628,7 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
 #ifndef F2D_EXACT
     if (!tri) {
         for (int l = 1; l < nlev; l++) o_uf[l] = mem.add((size_t)mv[l] * nv[l]);
-        o_smp = mem.add(sizeof(double) * 80 * MAX_LEVELS);
+        o_smp = mem.add(sizeof(double) * 96 * MAX_LEVELS);
     }
 #endif
     TRY(mem.alloc());
@@ -733,16 +733,16 @@ int Gmg::setup(const int8_t *mskp_host, int nx, int ny, double dx, double dy, do
     // the stored levels' uniform stencils (product build, column-form sweeps)
     if (!tri && nlev > 1) {
         double *smp = mem.at<double>(o_smp);
-        for (int l = 1; l < nlev; l++) TRY(mg_stencil_samples(d[l], smp + 80 * l, s));
-        double h[80 * MAX_LEVELS];
-        TRY(cuda_status(cudaMemcpyAsync(h, smp, sizeof(double) * 80 * nlev,
+        for (int l = 1; l < nlev; l++) TRY(mg_stencil_samples(d[l], smp + 96 * l, s));
+        double h[96 * MAX_LEVELS];
+        TRY(cuda_status(cudaMemcpyAsync(h, smp, sizeof(double) * 96 * nlev,
                                         cudaMemcpyDeviceToHost, s),
                         "stencil samples copy"));
         TRY(cuda_status(cudaStreamSynchronize(s), "stencil samples sync"));
         for (int l = 1; l < nlev; l++) {
             ufl[l] = nullptr;
-            if (!mg_uniform_choose(h + 80 * l, ust[l])) continue;
-            for (int k = 0; k < 4; k++) ustf[l][k] = (float)ust[l][k];
+            if (!mg_uniform_choose(h + 96 * l, ust[l])) continue;
+            for (int k = 0; k < 5; k++) ustf[l][k] = (float)ust[l][k];
             ufl[l] = mem.at<uint8_t>(o_uf[l]);
             TRY(mg_uniform_flags(d[l], ust[l], ufl[l], s));
         }
@@ -870,7 +870,8 @@ int Gmg::vcycle(LevelView<T> *L, int l1, bool zero_first, const int *active, cud
         TRY(smooth(L, l, xm, active, s));
         const AnalyticT<T> *a0 = l == 0 ? analytic<T>() : nullptr;
         if (fused<T>(l)) {
-            TRY(mg_resres<T>(L[l], a0, L[l + 1], L[l + 1].b, active, s));
+            TRY(mg_resres<T>(L[l], a0, L[l + 1], L[l + 1].b, active, s, l > 0 ? ufl[l] : nullptr,
+                             l > 0 ? uniform_stencil<T>(l) : nullptr));
         } else {
             TRY(mg_residual<T>(L[l], a0, L[l].x, L[l].b, L[l].r, active, s));
             TRY(mg_restrict<T>(L[l], L[l].r, L[l + 1], L[l + 1].b, active, s));

@@ -129,7 +129,7 @@ template <typename T>
 bool column_applies(const LevelView<T> &L);
 template <typename T>
 bool column_l0_applies(const LevelView<T> &L, const AnalyticT<T> &an);
-// set-up of a stored level's uniform stencil: 16 samples (5 doubles each)
+// set-up of a stored level's uniform stencil: 16 samples (6 doubles each)
 // of its stencil into out, the choice on the host, the flags on the device
 int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s);
 bool mg_uniform_choose(const double *h, double *st);
@@ -170,7 +170,8 @@ int &cluster_mode();
 // residual of L (x, b) restricted into the coarse b2
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
-              const int *active, cudaStream_t s);
+              const int *active, cudaStream_t s, const uint8_t *uf = nullptr,
+              const T *ust = nullptr);
 template <typename T>
 size_t coarse_smem_bytes(const int *mv, const int *nv, int nlev);
 

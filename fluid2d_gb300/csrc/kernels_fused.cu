@@ -1332,10 +1332,10 @@ template int mg_sweeps_uniform<double>(const LevelView<double> &, const uint8_t 
 template int mg_sweeps_uniform<float>(const LevelView<float> &, const uint8_t *, const float *,
                                       float, float, bool, const int *, cudaStream_t);
 
-// Set-up of a stored level's uniform stencil: the stencil (c, ey, ex, c3)
-// of the points at (1 + 2k) / 8 of the interior, k = 0..3, in both
+// Set-up of a stored level's uniform stencil: the stencil (c, ey, ex, c3,
+// a5) of the points at (1 + 2k) / 8 of the interior, k = 0..3, in both
 // directions, where the stencil has the uniform form (4 corners equal,
-// vertical and horizontal edges pairwise equal); out[5 * n + 4] = 1 there.
+// vertical and horizontal edges pairwise equal); out[6 * n + 5] = 1 there.
 __global__ void k_stencil_samples(const double *A6, const int8_t *msk, int mv, int nv,
                                   double *out) {
     const int n = (int)threadIdx.x;
@@ -1347,17 +1347,18 @@ __global__ void k_stencil_samples(const double *A6, const int8_t *msk, int mv, i
     const double a0 = A1[p], a1 = A2[p], a2 = A3[p], a3 = A4[p], a4 = A4[p + 1],
                  a5 = A3[p + nv - 1], a6 = A2[p + nv], a7 = A1[p + nv + 1];
     const bool ok = msk[p] != 0 && a0 == a2 && a0 == a5 && a0 == a7 && a1 == a6 && a3 == a4;
-    out[5 * n + 0] = a0;
-    out[5 * n + 1] = a1;
-    out[5 * n + 2] = a3;
-    out[5 * n + 3] = A6[5 * pl + p];
-    out[5 * n + 4] = ok ? 1. : 0.;
+    out[6 * n + 0] = a0;
+    out[6 * n + 1] = a1;
+    out[6 * n + 2] = a3;
+    out[6 * n + 3] = A6[5 * pl + p];
+    out[6 * n + 4] = A6[4 * pl + p];
+    out[6 * n + 5] = ok ? 1. : 0.;
 }
 
-// uf = 1 where the point is fluid and its stored stencil is (c, ey, ex, c3)
-// exactly (rows and columns 1 .. m-2; 0 elsewhere)
+// uf = 1 where the point is fluid and its stored stencil is (c, ey, ex, c3,
+// a5) exactly (rows and columns 1 .. m-2; 0 elsewhere)
 __global__ void k_uniform_flags(const double *A6, const int8_t *msk, int mv, int nv, double c,
-                                double ey, double ex, double c3, uint8_t *uf) {
+                                double ey, double ex, double c3, double a5, uint8_t *uf) {
     const size_t pl = (size_t)mv * nv;
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < pl;
          p += (size_t)gridDim.x * blockDim.x) {
@@ -1367,7 +1368,7 @@ __global__ void k_uniform_flags(const double *A6, const int8_t *msk, int mv, int
             const double *A1 = A6, *A2 = A6 + pl, *A3 = A6 + 2 * pl, *A4 = A6 + 3 * pl;
             f = A1[p] == c && A3[p] == c && A3[p + nv - 1] == c && A1[p + nv + 1] == c &&
                 A2[p] == ey && A2[p + nv] == ey && A4[p] == ex && A4[p + 1] == ex &&
-                A6[5 * pl + p] == c3;
+                A6[5 * pl + p] == c3 && A6[4 * pl + p] == a5;
         }
         uf[p] = f;
     }
@@ -1378,26 +1379,28 @@ int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s) 
     return launch_status("stencil samples");
 }
 
-// the level's uniform stencil st = (c, ey, ex, c3): the form most of the 16
-// samples (host copy h of mg_stencil_samples' output) share; false unless
+// the level's uniform stencil st = (c, ey, ex, c3, a5): the form most of the
+// 16 samples (host copy h of mg_stencil_samples' output) share; false unless
 // at least half of them share it (coarsened operators whose coefficients
 // carry rounding noise from point to point have no uniform stencil, and the
 // column form would take the general expression nearly everywhere)
 bool mg_uniform_choose(const double *h, double *st) {
     int best = -1, best_n = 0;
     for (int a = 0; a < 16; a++) {
-        if (h[5 * a + 4] == 0.) continue;
+        if (h[6 * a + 5] == 0.) continue;
         int n = 0;
-        for (int b = 0; b < 16; b++)
-            n += h[5 * b + 4] != 0. && h[5 * b] == h[5 * a] && h[5 * b + 1] == h[5 * a + 1] &&
-                 h[5 * b + 2] == h[5 * a + 2] && h[5 * b + 3] == h[5 * a + 3];
+        for (int b = 0; b < 16; b++) {
+            bool same = h[6 * b + 5] != 0.;
+            for (int k = 0; k < 5; k++) same = same && h[6 * b + k] == h[6 * a + k];
+            n += same;
+        }
         if (n > best_n) {
             best_n = n;
             best = a;
         }
     }
     if (best < 0 || best_n < 8) return false;
-    for (int k = 0; k < 4; k++) st[k] = h[5 * best + k];
+    for (int k = 0; k < 5; k++) st[k] = h[6 * best + k];
     return true;
 }
 
@@ -1405,7 +1408,7 @@ int mg_uniform_flags(const LevelView<double> &L, const double *st, uint8_t *uf, 
     const size_t pl = (size_t)L.mv * L.nv;
     const size_t blocks = (pl + 255) / 256;
     k_uniform_flags<<<(unsigned)(blocks > 4096 ? 4096 : blocks), 256, 0, s>>>(
-        L.A, L.msk, L.mv, L.nv, st[0], st[1], st[2], st[3], uf);
+        L.A, L.msk, L.mv, L.nv, st[0], st[1], st[2], st[3], st[4], uf);
     return launch_status("uniform flags");
 }
 
@@ -1624,6 +1627,11 @@ struct ResresArgs {
     T *b2;
     const int *active;
     int tx, ty;  // the coarse tile
+    // a stored level's uniform stencil (product build; uf null: none): the
+    // flagged points' residual b - (c corners + ey vertical + ex horizontal
+    // + a5 x), without the coefficient loads
+    const uint8_t *uf;
+    T uc, uey, uex, ua5;
 };
 
 template <typename T, bool L0>
@@ -1675,7 +1683,18 @@ F2D_DEV void resres_body(const ResresArgs<T> &A, const VB vb) {
         }
 #endif
         if (!in) continue;
-        rs[q] = residual<T, L0>(F, &an, F.x, F.b, wrap(jf, mv, NH), wrap(iff, nv, NH));
+        const int jw = wrap(jf, mv, NH), iw = wrap(iff, nv, NH);
+        if (!L0 && A.uf) {
+            const size_t p = off(jw, iw, nv);
+            if (A.uf[p]) {
+                const T *x = F.x + p;
+                const T corners = (x[-nv - 1] + x[-nv + 1]) + (x[nv - 1] + x[nv + 1]);
+                const T vert = x[-nv] + x[nv], horiz = x[-1] + x[1];
+                rs[q] = F.b[p] - fma(A.uc, corners, fma(A.uey, vert, fma(A.uex, horiz, A.ua5 * x[0])));
+                continue;
+            }
+        }
+        rs[q] = residual<T, L0>(F, &an, F.x, F.b, jw, iw);
     }
     __syncthreads();
     const float invt = 1.0f / (float)TX;
@@ -1718,13 +1737,23 @@ F2D_BATCH_ENTRY(ResresF1, BResresF1)
 
 template <typename T>
 int mg_resres(const LevelView<T> &F, const AnalyticT<T> *an, const LevelView<T> &C, T *b2,
-              const int *active, cudaStream_t s) {
+              const int *active, cudaStream_t s, const uint8_t *uf, const T *ust) {
     const dim3 tile = level_tile(C.mv - 2 * NH, C.nv - 2 * NH, RR_TX, RR_TY);
     const dim3 g = grid2d(C.mv - 2 * NH, C.nv - 2 * NH, tile);
     const dim3 b(resres_threads(tile));
     const size_t smem = resres_smem<T>(tile);
     ResresArgs<T> a{F,  an ? *an : AnalyticT<T>{}, C.msk, C.mv, C.nv, b2, active,
-                    (int)tile.x, (int)tile.y};
+                    (int)tile.x, (int)tile.y, nullptr, (T)0, (T)0, (T)0, (T)0};
+    // float64 levels of at least one CTA per SM (measured: 1024^2 step -1.4 %;
+    // on the small levels of a 128^2 hierarchy the flag's extra load made the
+    // step 5 % slower, and the float levels of the mixed form gained nothing)
+    if (uf && ust && !an && sizeof(T) == 8 && column_applies(F)) {
+        a.uf = uf;
+        a.uc = ust[0];
+        a.uey = ust[1];
+        a.uex = ust[2];
+        a.ua5 = ust[4];
+    }
     if (an)
         return launch_body<BResres<T, true>>(k_resres<T, true>, a, g, b, smem, s, "mg_resres");
     return launch_body<BResres<T, false>>(k_resres<T, false>, a, g, b, smem, s, "mg_resres");
@@ -2364,7 +2393,7 @@ int vec_axpy_const(double *x, double area, const double *sum, size_t count, cuda
     template int mg_smooth_fused<T>(const LevelView<T> &, const AnalyticT<T> *, T, T, int,       \
                                     const LevelView<T> *, T *, const int *, cudaStream_t);       \
     template int mg_resres<T>(const LevelView<T> &, const AnalyticT<T> *, const LevelView<T> &,  \
-                              T *, const int *, cudaStream_t);                                   \
+                              T *, const int *, cudaStream_t, const uint8_t *, const T *);       \
     template size_t coarse_smem_bytes<T>(const int *, const int *, int);
 F2D_INST(double)
 F2D_INST(float)

@@ -75,7 +75,9 @@ def test_cluster_subcycle_equals_the_level_kernels(name, levels):
     in their order: the states after three steps equal the level kernels'
     bit for bit, on periodic, closed-with-islands and channel domains and
     QG's Helmholtz operator, with every level that fits in the cluster or
-    only the one above the coarse operator's."""
+    only the one above the coarse operator's.  Both run the level kernels in
+    the reference's order (f2d_set_separable 0: no column or uniform-stencil
+    forms), which the cluster reproduces."""
     import torch
     from fluid2d_gb300 import _lib, engine
     from fluid2d_gb300 import workloads as W
@@ -97,6 +99,7 @@ def test_cluster_subcycle_equals_the_level_kernels(name, levels):
 
     def run(mode):
         old = P.f2d_set_cluster(mode)
+        old_sep = P.f2d_set_separable(0)
         try:
             M = engine.from_workload(wl, dt=1e-3, precision="mixed", **kw)
             lev = M.cluster_level()
@@ -109,6 +112,7 @@ def test_cluster_subcycle_equals_the_level_kernels(name, levels):
             return lev, M.var.state.cpu().numpy()
         finally:
             P.f2d_set_cluster(old)
+            P.f2d_set_separable(old_sep)
 
     (lev_on, a), (lev_off, b) = run(levels), run(0)
     assert lev_on >= 1 and lev_off == -1

@@ -1381,9 +1381,10 @@ int mg_stencil_samples(const LevelView<double> &L, double *out, cudaStream_t s) 
 
 // the level's uniform stencil st = (c, ey, ex, c3, a5): the form most of the
 // 16 samples (host copy h of mg_stencil_samples' output) share; false unless
-// at least half of them share it (coarsened operators whose coefficients
-// carry rounding noise from point to point have no uniform stencil, and the
-// column form would take the general expression nearly everywhere)
+// at least half of them share it (a level whose coarsening rounds the
+// stencil out of its symmetric form, or whose samples are mostly next to
+// walls, has no uniform stencil, and the column form would take the general
+// expression nearly everywhere)
 bool mg_uniform_choose(const double *h, double *st) {
     int best = -1, best_n = 0;
     for (int a = 0; a < 16; a++) {

@@ -19,6 +19,9 @@
  *    library (allocated on first use, grown on demand, one per device);
  *    such calls must not overlap on the GPU with another (scratch) call on
  *    the same device.
+ *  - The f2d_set_* switches are process-wide settings without locking: set
+ *    them from one host thread, before the models or graphs they are to
+ *    affect are created or captured, not while another thread launches.
  *
  * Each declaration names the reference routine it replaces (file:line in
  * pvthinker/Fluid2d).

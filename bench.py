@@ -568,35 +568,61 @@ def bench_mixed(engine, wl, dt, s0, a, stream, world):
             "level_tiles": {"cta_target": tiles[0], "one_pass_threads": tiles[1]}}
 
 
+def _device_start(engine, wl, **kw):
+    """A model of the workload with psi inverted and dt set on the device
+    (dt = 0.8 min(dx, dy) / maxspeed), and a copy of its state."""
+    import torch
+    M = engine.from_workload(wl, dt=1e-3, **kw)
+    M.set_psi_from_vorticity()
+    dt = 0.8 * min(M.dx, M.dy) / M.diagnostics()["maxspeed"]
+    M.set_dt(dt)
+    s0 = M.var.state.clone()
+    torch.cuda.synchronize()  # the copy is complete before other streams step M
+    return M, dt, s0
+
+
+def _oracle_start(engine, stepper, wl, **kw):
+    """The checker's start: the oracle's model of the workload and a GPU
+    model holding the oracle's state and dt."""
+    import torch
+    p, O = stepper.from_workload(wl)
+    dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
+    G = engine.from_workload(wl, dt=dt, **kw)
+    G.var.state.copy_(torch.from_numpy(O.state).cuda())
+    G.diagnostics()
+    return p, O, dt, G
+
+
 def bench_dipole(a, host):
     """Euler dipole, closed 128x128, 200 steps (the reference's CPU-runnable
-    case): the float64 GPU path from the oracle's initial state, timed as a
-    graph; the oracle's own 200 steps on one core give the CPU rate and the
-    parity of the final state; the CPU path on every core (one copy each)
-    gives the host's aggregate rate."""
-    import numpy as np
+    case): the float64 GPU path from its own initial state (psi inverted on
+    the device), timed as a graph; parity: the GPU path and the oracle both
+    from the oracle's state, compared after the 200 steps, which on one core
+    also give the CPU rate; the CPU path on every core (one copy each) gives
+    the host's aggregate rate."""
     import torch
     from fluid2d_gb300 import engine, workloads as W
     from oracle import stepper
     steps = a.dipole_steps
     wl = W.dipole(128, 128)
-    p, O = stepper.from_workload(wl)
-    dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
-    G = engine.from_workload(wl, dt=dt)
-    G.var.state.copy_(torch.from_numpy(O.state).cuda())
-    G.diagnostics()
     stream = torch.cuda.Stream()
-    ms = _timed_graph(G, steps, stream)  # the first replay captures the graph
-    final = G.var.state.cpu().numpy()
-    G.var.state.copy_(torch.from_numpy(O.state).cuda())
-    G.diagnostics()
+    G, dt, s0 = _device_start(engine, wl)
     with torch.cuda.stream(stream):
-        G.run(5, graph=True)
+        G.run(5, graph=True)  # capture, warm up
     stream.synchronize()
+    G.var.state.copy_(s0)
+    G.diagnostics()
     ms = _timed_graph(G, steps, stream)
-    stepper.run(O, p, steps, dt)
+    del G
+    p, O, odt, P = _oracle_start(engine, stepper, wl)
+    with torch.cuda.stream(stream):
+        P.run(steps, graph=True)
+    stream.synchronize()
+    final = P.var.state.cpu().numpy()
+    stepper.run(O, p, steps, odt)
     parity = {nm: _rel(final[k], O.state[k])["rel_linf"]
-              for k, nm in enumerate(G.var.varname_list) if nm in ("vorticity", "psi", "u", "v")}
+              for k, nm in enumerate(P.var.varname_list) if nm in ("vorticity", "psi", "u", "v")}
+    del P
     one, res1 = cpu_run([("dipole", None, None, 0, steps)], 1)
     cores = host["nproc"]
     allc, _ = cpu_run([("dipole", None, None, 0, steps)] * cores, cores)
@@ -623,24 +649,23 @@ def bench_shear(a, host):
     from oracle import stepper
     wl = W.shear(2048, 512)
     cells = 2048 * 512
-    p, O = stepper.from_workload(wl)
-    dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]
-    s0 = torch.from_numpy(O.state).cuda()
-    A = engine.from_workload(wl, dt=dt)
-    B = engine.from_workload(wl, dt=dt, precision="mixed")
     stream = torch.cuda.Stream()
-    # parity of the float64 form with the oracle over the first steps
-    A.var.state.copy_(s0)
-    A.diagnostics()
+    # parity of the float64 form with the oracle over the first steps, both
+    # from the oracle's state
+    p, O, odt, P = _oracle_start(engine, stepper, wl)
     ncpu = a.shear_cpu_steps
-    A.run(ncpu)
+    P.run(ncpu)
     t0 = time.perf_counter()
-    stepper.run(O, p, ncpu, dt)
+    stepper.run(O, p, ncpu, odt)
     t_oracle = time.perf_counter() - t0
-    got = A.var.state.cpu().numpy()
+    got = P.var.state.cpu().numpy()
     parity = {nm: _rel(got[k], O.state[k])["rel_linf"]
-              for k, nm in enumerate(A.var.varname_list)
+              for k, nm in enumerate(P.var.varname_list)
               if nm in ("vorticity", "psi", "u", "v", "buoyancy")}
+    del P, O
+    # the timed runs start from the state prepared on the device
+    A, dt, s0 = _device_start(engine, wl)
+    B = engine.from_workload(wl, dt=dt, precision="mixed")
     # 1000 steps of each form, 100 at a time
     for M in (A, B):
         M.var.state.copy_(s0)

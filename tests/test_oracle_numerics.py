@@ -16,6 +16,8 @@ its design order on smooth periodic fields.
 * the flux form moves a constant field by nothing under a velocity that
   comes from a streamfunction: to rounding on periodic domains, to the
   REAL*4 reconstruction weights' sums (1e-8) next to walls;
+* cell <-> corner averages and the multigrid's interpolation and
+  restriction, second order with their staggering;
 * the multigrid solve (core/gmg/hierarchy.py:169-188 over the 9-point
   operator of core/gmg/level.py:261-302) converges to the continuous
   solution at second order and to 1e-12 in a few F-cycles.
@@ -159,4 +161,57 @@ def test_poisson_solve_second_order():
         assert nite <= 8 and res <= 1e-12, (n, nite, res)
         e = _inner(x) - _inner(x).mean() - (_inner(psi) - _inner(psi).mean())
         errs.append(np.abs(e).max())
+    assert all(abs(r - 2) < 0.1 for r in _orders(errs)), errs
+
+
+def _smooth(X, Y):
+    return np.sin(2 * np.pi * X) * np.cos(2 * np.pi * Y) + 0.3 * np.sin(2 * np.pi * (X + Y))
+
+
+@pytest.mark.parametrize("kind", ["celltocorner", "cornertocell"])
+def test_cell_corner_averages_second_order(kind):
+    """celltocorner / cornertocell (core/fortran_operators.f90:44-64,
+    102-122): the corner (j, i) is the upper-right corner of cell (j, i)."""
+    errs = []
+    for n in SIDES:
+        _, Xc, Yc = _grid(n, 0.5)
+        _, Xk, Yk = _grid(n, 1.0)
+        out = np.zeros(Xc.shape)
+        if kind == "celltocorner":
+            K().celltocorner(_smooth(Xc, Yc), out)
+            want = _smooth(Xk, Yk)
+        else:
+            K().cornertocell(_smooth(Xk, Yk), out)
+            want = _smooth(Xc, Yc)
+        errs.append(np.abs(_inner(out - want)).max())
+    assert all(abs(r - 2) < 0.1 for r in _orders(errs)), errs
+
+
+@pytest.mark.parametrize("kind", ["interpolate", "restrict"])
+def test_transfer_operators_second_order(kind):
+    """interpolate / restrict (core/gmg/fortran_multigrid.f90:415-546)
+    between the finest level and level 1 of the oracle's hierarchy: a coarse
+    point sits midway between the two fine points it covers in each
+    direction (fine point i at (i - 3) h, coarse point I at (I - 3) 2h + h)."""
+    from oracle import stepper
+    errs = []
+    for n in (32, 64, 128):
+        h = 1. / n
+        msk = C.corner_mask(C.mask(n + 2 * NH, n + 2 * NH, "perio", 0, 1))
+        G = stepper.Gmg({'nh': NH, 'n': n, 'm': n, 'omega': 8. / 9., 'dx': h, 'dy': h},
+                        msk * 1.)
+        fine, coarse = G.grid[0], G.grid[1]
+        xf = (np.arange(fine.nv) - NH) * h
+        xc = (np.arange(coarse.nv) - NH) * 2 * h + h
+        Xf, Yf = np.meshgrid(xf, xf)
+        Xc, Yc = np.meshgrid(xc, xc)
+        if kind == "interpolate":
+            out = np.zeros((fine.mv, fine.nv))
+            K().interpolate(fine.msk, coarse.msk, _smooth(Xc, Yc), NH, out)
+            want = _smooth(Xf, Yf)
+        else:
+            out = np.zeros((coarse.mv, coarse.nv))
+            K().restrict(coarse.msk, _smooth(Xf, Yf), NH, out)
+            want = _smooth(Xc, Yc)
+        errs.append(np.abs(_inner(out - want)).max())
     assert all(abs(r - 2) < 0.1 for r in _orders(errs)), errs

@@ -215,3 +215,52 @@ def test_transfer_operators_second_order(kind):
             want = _smooth(Xc, Yc)
         errs.append(np.abs(_inner(out - want)).max())
     assert all(abs(r - 2) < 0.1 for r in _orders(errs)), errs
+
+
+@pytest.mark.parametrize("hydroepsilon", [1.0, 0.1])
+def test_smoothers_keep_the_discrete_solution(hydroepsilon):
+    """One smoothing call leaves x unchanged where A x = b: damped Jacobi
+    (smoothtwicewithA, core/gmg/fortran_multigrid.f90:2-127) and, for
+    hydroepsilon dy/dx <= 0.2, the line relaxation (smoothtridiag,
+    :215-288) on a closed domain; the Jacobi form damps the checkerboard
+    mode by more than 10."""
+    from oracle import stepper
+    n = 64
+    h = 1. / n
+    msk = C.corner_mask(C.mask(n + 2 * NH, n + 2 * NH, "closed", 0, 3))
+    G = stepper.Gmg({'nh': NH, 'n': n, 'm': n, 'omega': 8. / 9., 'dx': h, 'dy': h,
+                     'hydroepsilon': hydroepsilon}, msk * 1.)
+    g = G.grid[0]
+    assert g.relaxation == ("tridiagonal" if hydroepsilon < 0.2 else "default")
+    x = C.field(n + 2 * NH, n + 2 * NH, 4) * g.msk
+    K().fillhalo(x, NH)
+    r = np.zeros_like(x)
+    K().computeresidualwitha(g.msk, g.A, x, np.zeros_like(x), r)   # r = -A x
+    b = -r
+    x1 = x.copy()
+    g.smooth(x1, b, 1)
+    assert np.abs(x1 - x)[g.msk != 0].max() <= 1e-13 * np.abs(x).max()
+    if hydroepsilon == 1.0:
+        J, I = np.indices(x.shape)
+        e = (-1.) ** (J + I) * g.msk
+        g.smooth(e, np.zeros_like(e), 1)
+        assert np.abs(_inner(e)).max() < 0.1
+
+
+def test_line_relaxation_across_an_island_is_not_finite():
+    """The reference's line relaxation divides by the diagonal of every point
+    of a column whose first interior row is fluid (smoothtridiag and tridiag,
+    core/gmg/fortran_multigrid.f90:240-317), so a column that crosses an
+    island (zero diagonal) gets non-finite values: it is meant for columns
+    fluid from wall to wall.  The restatement keeps that behaviour."""
+    from oracle import stepper
+    n = 64
+    h = 1. / n
+    msk = C.corner_mask(C.mask(n + 2 * NH, n + 2 * NH, "closed", 2, 3))
+    G = stepper.Gmg({'nh': NH, 'n': n, 'm': n, 'omega': 8. / 9., 'dx': h, 'dy': h,
+                     'hydroepsilon': 0.1}, msk * 1.)
+    g = G.grid[0]
+    x = C.field(n + 2 * NH, n + 2 * NH, 4) * g.msk
+    with np.errstate(all="ignore"):
+        K().smoothtridiag(g.msk, g.A, x, np.zeros_like(x))
+    assert not np.all(np.isfinite(x))

@@ -6,6 +6,15 @@ reference's ``operators.py``, ``fluxes.py``, ``gmg/*.py`` and models import
 the GB300 kernels under the module names they already use:
 ``fortran_advection``, ``fortran_operators``, ``fortran_diag``,
 ``fortran_fluxes`` and ``gmg.fortran_multigrid``.
+
+Every routine the reference's Python calls is provided.  Not provided: the
+routines it names only in commented-out lines (``smoothoncewitha``,
+core/gmg/level.py:354-355; ``celltocornerbicubic``, core/operators.py:441;
+``computewallshear``, core/operators.py:241; and
+``computenoslipsourceterm_regularized``), and the MPI halo packers
+``halotobuffer``, ``buffertohalo`` and ``buffertodomain``
+(core/gmg/fortran_multigrid.f90:549-703), which serve the domain
+decomposition this single-GPU path does not do.
 """
 import os
 import sys

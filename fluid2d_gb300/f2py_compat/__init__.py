@@ -8,10 +8,10 @@ the GB300 kernels under the module names they already use:
 ``fortran_fluxes`` and ``gmg.fortran_multigrid``.
 
 Every routine the reference's Python calls is provided.  Not provided: the
-routines it names only in commented-out lines (``smoothoncewitha``,
-core/gmg/level.py:354-355; ``celltocornerbicubic``, core/operators.py:441;
-``computewallshear``, core/operators.py:241; and
-``computenoslipsourceterm_regularized``), and the MPI halo packers
+routines it never calls (``smoothoncewitha`` and ``celltocornerbicubic``
+and ``computewallshear`` appear only in commented-out lines,
+core/gmg/level.py:354-355, core/operators.py:441, core/operators.py:241;
+``computenoslipsourceterm_regularized`` nowhere), and the MPI halo packers
 ``halotobuffer``, ``buffertohalo`` and ``buffertodomain``
 (core/gmg/fortran_multigrid.f90:549-703), which serve the domain
 decomposition this single-GPU path does not do.

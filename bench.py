@@ -582,8 +582,8 @@ def _device_start(engine, wl, **kw):
 
 
 def _oracle_start(engine, stepper, wl, **kw):
-    """The checker's start: the oracle's model of the workload and a GPU
-    model holding the oracle's state and dt."""
+    """The parity check's start: the oracle's model of the workload and a
+    GPU model holding the oracle's state and dt."""
     import torch
     p, O = stepper.from_workload(wl)
     dt = 0.8 * min(O.grid.dx, O.grid.dy) / O.diags["maxspeed"]

@@ -9,12 +9,12 @@ if ROOT not in sys.path:
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300 box)")
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (a GB300)")
     config.addinivalue_line("markers", "slow: long-running parity case")
 
 
 # where CPU tests look for the reference's core/ sources (read-only); tests
-# that need them skip themselves when they are absent (on the GPU machine)
+# that need them skip themselves when they are absent
 REFERENCE_CORE = os.environ.get("FLUID2D_CORE", "/root/reference/core")
 
 

@@ -12,7 +12,7 @@
   the mixed form (float32 fluxes and cycles in float64 defect correction)
   from the oracle's state within 1e-6 relative L2 of the oracle's step.
 
-The oracle is the checker; every state the GPU computes starts from the
+The oracle is the parity reference; every state the GPU computes starts from the
 oracle's state (the workload generators use numpy transcendentals, which
 round differently on other CPU architectures).
 """

@@ -79,7 +79,7 @@ def test_package_never_imports_the_oracle():
 # the functions that may load the oracle: bench.py's CPU-baseline legs and
 # reference arm, and its checkers (the parity of the named workloads, started
 # from the oracle's state: _oracle_start); __graft_entry__'s smoke check, and
-# its build(), which compiles the checker without running it.  The
+# its build(), which compiles the oracle without running it.  The
 # timed GPU runs (run_ours, _device_start, _timed_graph) are not among them.
 ORACLE_USERS = {"bench.py": {"_cpu_worker", "cpu_run", "cpu_baseline", "run_reference",
                              "bench_mixed", "bench_dipole", "bench_shear", "_oracle_start"},

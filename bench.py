@@ -262,6 +262,18 @@ def cpu_descr(cores, sample, val, host):
             "host_cpu": host["cpu"], "host_nproc": host["nproc"]}
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The largest `value` over the ranks of the process group (every rank
+    gets it); the value itself when there is one rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(a, rank, world):
     if rank != 0:
         return
@@ -332,11 +344,7 @@ def run_ours(a, rank, world, local):
         e1.synchronize()
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
     ms_step = ms / a.steps
     value = world * n * n * a.steps / (ms * 1e-3)
     nite, res, st = M.solve_stats()
@@ -375,11 +383,7 @@ def run_ours(a, rank, world, local):
             M.run_host(1, state_host)
         f1.record(stream)
         f1.synchronize()
-    e2e_ms = f0.elapsed_time(f1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(f0.elapsed_time(f1), world)
     e2e_val = world * n * n * a.e2e_steps / (e2e_ms * 1e-3)
     del M
     torch.cuda.synchronize()
